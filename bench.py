@@ -1,0 +1,325 @@
+"""Throughput of the gb300 MLS-MPM substep on the mixed-materials workload; prints one JSON line.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Workload: a 1 m box at 128^3 (dx = 1/128, padded grid 134^3), 8 particles per cell: a von Mises sphere
+r = 0.12 (E 2e4, nu 0.45, yield 300 Pa, rho 600), a Drucker-Prager column 0.15 x 0.4 x 0.15 (E 3.5e5,
+nu 0.3, 35 deg, rho 1600), a snowball r = 0.08 thrown at (3, 1, 0) m/s (E 1.4e5, nu 0.2, hardening 10,
+theta_c 2.5e-2, theta_s 7.5e-3, max hardening 20, rho 400) and one static seeded perturbed icosphere
+collider of 5,120 triangles; about 304k particles; synthetic, seeded data.
+
+A step is one substep (dt = 5e-5) of the whole scene with the state resident in HBM (``value``). The
+L2 cache (129 MB) is larger than this state, so a 256 MiB buffer is written between timed steps and only
+the substeps are timed. ``e2e`` is the same metric through the public solver API with host buffers: one
+24 fps frame per step (set_collider_transforms, advance(1/24) at the CFL time step, get_particles and
+save_state back to host memory, as the reference's bake runner does every frame).
+
+``--impl reference`` times the CPU implementation of the same substep on all host cores. The reference's
+own backend needs warp-lang, which cannot be installed here, so that arm runs the project's C restatement
+of the reference kernels (the oracle), labelled as such.
+
+Several GPUs run independent replicas of the scene, one per rank (there is no data exchange in this path).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "tests"))
+
+METRIC = "particle-substeps/s on 1 GB300, batched vs plain; p50/p99 frame latency"
+UNIT = "particle-substeps/s"
+DT = 5e-5
+FRAME_DT = 1 / 24
+G2P_BYTES = 156   # per particle: read x, F, Jp, mat (56 B) + write x, v, C, F, Jp (100 B)
+P2G_BYTES = 104   # per particle: read x, v, C, F, Jp, mat
+SUBSTEP_BYTES = 204
+WORKLOAD = "mixed materials 128^3: von Mises sphere + Drucker-Prager column + snowball + 5120-triangle collider"
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[4:8]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_scene(seed: int = 0):
+    from scenes import mix_scene
+
+    return mix_scene(res=128, seed=seed)
+
+
+def make_gpu_solver(device: str):
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+    from mpm_plugin_gb300.solver import Gb300Solver
+    from scenes import add
+
+    d, mats, groups, (cv, ct, xf) = build_scene()
+    s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+    for pos, m, vel in groups:
+        add(s, pos, m, m, vel)
+    s.set_colliders([ColliderGeometry(MeshData(cv, ct), True, 0.5)])
+    s.set_collider_transforms(xf[None], xf[None])
+    return s, xf
+
+
+def cpu_oracle_time(threads: int, budget_s: float):
+    """FP32 oracle (C restatement of the reference kernels, OpenMP) on the same scene; returns rate, sample."""
+    from oracle.oracle import OracleSolver
+    from scenes import add
+
+    d, mats, groups, (cv, ct, xf) = build_scene()
+    o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f32", threads=threads)
+    for pos, m, vel in groups:
+        add(o, pos, m, m, vel)
+    o.set_colliders([(cv, ct, True, 0.5)])
+    o.set_collider_transforms(xf[None], xf[None])
+    n = o.particle_count
+    o.substep(DT, 1.0)  # warm-up
+    t0 = time.perf_counter()
+    o.substep(DT, 1.0)
+    t1 = time.perf_counter() - t0
+    k = max(1, min(200, int(budget_s / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        o.substep(DT, 1.0)
+    el = time.perf_counter() - t0
+    return n * k / el, n, k, el
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from oracle.oracle import OracleSolver
+    from scenes import add
+
+    d, mats, groups, (cv, ct, xf) = build_scene()
+    o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f32", threads=threads)
+    for pos, m, vel in groups:
+        add(o, pos, m, m, vel)
+    o.set_colliders([(cv, ct, True, 0.5)])
+    o.set_collider_transforms(xf[None], xf[None])
+    n = o.particle_count
+    for _ in range(args.warmup):
+        o.substep(DT, 1.0)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.substep(DT, 1.0)
+    el = time.perf_counter() - t0
+    v = n * args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "particles": n, "grid": 128, "dt": DT},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} substeps of the full {n}-particle scene on {threads} threads; "
+                                       "the reference's Warp backend cannot be installed (no warp-lang), so this "
+                                       "is the C restatement of its kernels"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+
+    device = f"cuda:{local}"
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device(device))
+    from mpm_plugin_gb300 import _abi
+
+    solver, xf = make_gpu_solver(device)
+    n = solver.particle_count
+    stream = torch.cuda.ExternalStream(solver.stream, device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+    for _ in range(args.warmup):
+        solver.substep(DT, 1.0, FRAME_DT)
+    solver.synchronize()
+
+    # timed region: K substeps, L2 written between them, per-kernel CUDA events on the solver's stream
+    solver.set_option(_abi.OPT_KERNEL_TIMING, 1)
+    solver.kernel_times(reset=True)
+    launches0 = solver.launch_count()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.fill_(float(k))
+                starts[k].record(stream)
+                solver.substep(DT, 1.0, FRAME_DT)
+                ends[k].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    launches = solver.launch_count() - launches0
+    ktimes = solver.kernel_times(reset=True)
+    solver.set_option(_abi.OPT_KERNEL_TIMING, 0)
+
+    # end to end through the solver API: one bake frame per step, host buffers
+    e2e_frames, frame_ms, substeps = max(2, min(args.steps, 6)), [], 0
+    h2d = 2 * 64  # the collider's start and end world matrices
+    d2h = n * (12 + 12 + 4 + 4) + n * (12 + 12 + 36 + 36 + 4 + 4 + 4)  # get_particles + save_state
+    solver.advance(FRAME_DT)  # warm the CFL path and the graph
+    for _ in range(e2e_frames):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.set_collider_transforms(xf[None], xf[None])
+        st = solver.advance(FRAME_DT)
+        solver.get_particles()
+        solver.save_state()
+        frame_ms.append(1e3 * (time.perf_counter() - t0))
+        substeps += st.substeps
+    e2e = n * substeps / (sum(frame_ms) / 1e3)
+
+    times = torch.tensor([total_ms, sum(frame_ms)], dtype=torch.float64, device=device)
+    rates = torch.tensor([float(n), e2e], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(rates, op=torch.distributed.ReduceOp.SUM)
+    if rank != 0:
+        return
+    total_ms, _ = times.tolist()
+    n_all, e2e_all = rates.tolist()
+    value = n_all * args.steps / (total_ms / 1e3)
+
+    names = {"p2g": P2G_BYTES, "g2p": G2P_BYTES}
+    dom = max(("p2g", "grid_update", "g2p"), key=lambda k: ktimes[k][0])
+    avg_ms = {k: (ktimes[k][0] / max(ktimes[k][1], 1)) for k in ktimes}
+    peak, peak_kind = peaks()
+    bytes_per_launch = names.get(dom, 16) * n
+    achieved = bytes_per_launch / (avg_ms[dom] / 1e3) / 1e9
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            traffic = json.loads(tfile.read_text()).get(dom)
+        except Exception:
+            traffic = None
+    cpu_rate, cpu_n, cpu_k, cpu_el = cpu_oracle_time(os.cpu_count() or 1, args.cpu_budget)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "particles": n, "grid": 128, "dt": DT, "parallelism": f"replicas{world}",
+                   "l2": "256 MiB written between timed substeps (state is smaller than L2)"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": bytes_per_launch},
+        "kernels_ms_per_launch": avg_ms,
+        "substep_bytes": {"algorithmic_per_particle": SUBSTEP_BYTES,
+                          "achieved_gbs": SUBSTEP_BYTES * n * args.steps / (total_ms / 1e3) / 1e9},
+        "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"{cpu_k} substeps of the full {cpu_n}-particle scene, {cpu_el:.1f} s"},
+        "e2e": {"value": e2e_all, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "step": "one 24 fps frame via the solver API", "substeps_per_frame": substeps / e2e_frames},
+        "frame_latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "fp64_svd_lanes": solver.fp64_lanes(),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

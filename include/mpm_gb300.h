@@ -1,0 +1,144 @@
+/* mpm_gb300: C-ABI of the GB300 (sm_103a) MLS-MPM substep backend.
+ *
+ * This library is the device side of a new backend for the reference's solver interface
+ * (mpm_core/solver.py:37-82 of jonatanhedborg/mpm_plugin). Its Python binding (mpm_plugin_gb300/_abi.py, ctypes)
+ * implements mpm_core.solver.Solver on top of these calls and registers it with
+ * mpm_core.backends.register_backend (mpm_core/backends/__init__.py:21-22). Each entry point below names the
+ * reference interface it replaces (file:line in the reference project).
+ *
+ * Conventions: plain pointers and sizes only. Every call returns an int status (MPM_OK = 0) and, on failure,
+ * mpm_last_error(h) describes it (mpm_last_error(NULL) for failures before a handle exists). Host arrays are
+ * C-contiguous row-major float32/int32: positions and velocities (N,3), C and F (N,3,3), Jp (N,). Particle
+ * order is the reference's: insertion order, with removed particles dropped and the rest kept in order.
+ * One handle is one domain on one GPU; a handle is used by one host thread at a time.
+ */
+#ifndef MPM_GB300_H
+#define MPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MPM_OK = 0,
+    MPM_ERR_VALUE = 1,           /* maps to ValueError (bad ids, sizes, transform counts) */
+    MPM_ERR_NOT_IMPLEMENTED = 2, /* maps to NotImplementedError (unknown material model) */
+    MPM_ERR_CUDA = 3,            /* a CUDA runtime error; message has the CUDA error string */
+    MPM_ERR_ARGUMENT = 4,        /* null handle or pointer */
+    MPM_ERR_MEMORY = 5           /* device allocation failed */
+};
+
+enum { MPM_MODEL_ELASTIC = 0, MPM_MODEL_VON_MISES = 1, MPM_MODEL_DRUCKER_PRAGER = 2, MPM_MODEL_SNOW = 3 };
+
+/* mpm_core/scene.py:36-67 Domain: axis-aligned box, resolution along its longest side, six walls. */
+typedef struct MpmDomainDesc {
+    double min[3], max[3];
+    int32_t resolution;
+    int32_t wall_lo[3]; /* x-, y-, z-: 1 = wall, 0 = open side */
+    int32_t wall_hi[3]; /* x+, y+, z+ */
+    double wall_friction;
+} MpmDomainDesc;
+
+/* mpm_core/materials.py:24-59 MaterialParams (model as MPM_MODEL_*). */
+typedef struct MpmMaterialDesc {
+    int32_t model;
+    double youngs_modulus, poisson_ratio, density;
+    double yield_stress, friction_angle_deg, hardening, critical_compression, critical_stretch, max_hardening;
+} MpmMaterialDesc;
+
+/* mpm_core/solver.py:30-34 ColliderGeometry: a triangle mesh in the collider's local space. */
+typedef struct MpmColliderDesc {
+    int32_t n_verts, n_tris;
+    const float *verts;   /* (n_verts, 3) */
+    const int32_t *tris;  /* (n_tris, 3) */
+    int32_t closed;
+    double friction;
+} MpmColliderDesc;
+
+/* mpm_core/solver.py:23-27 AdvanceStats. */
+typedef struct MpmAdvanceStats {
+    int32_t substeps;
+    double dt;
+    int32_t removed;
+} MpmAdvanceStats;
+
+/* Replaces WarpSolver.__init__ (mpm_core/backends/warp/solver.py:27-78), reached through
+ * create_solver (mpm_core/backends/__init__.py:25-28). MPM_ERR_NOT_IMPLEMENTED for an unknown model. */
+int mpm_create(const MpmDomainDesc *domain, const MpmMaterialDesc *materials, int32_t n_materials,
+               const double gravity[3], int32_t particles_per_cell, int32_t device, void **handle);
+int mpm_destroy(void *handle);
+const char *mpm_last_error(void *handle);
+
+/* Solver.add_particles (mpm_core/solver.py:52-54; warp/solver.py:100-125). n == 0 is a no-op;
+ * MPM_ERR_VALUE "material id out of range" for a bad id. New particles get C = 0, F = I, Jp = 1. */
+int mpm_add_particles(void *handle, int64_t n, const float *x, const float *v, const int32_t *material_ids,
+                      const int32_t *emitter_ids);
+
+/* Solver.set_colliders (mpm_core/solver.py:56-58; warp/solver.py:142-152): replaces all colliders and
+ * resets their transforms to identity. */
+int mpm_set_colliders(void *handle, int32_t n, const MpmColliderDesc *colliders);
+
+/* Solver.set_collider_transforms (mpm_core/solver.py:60-62; warp/solver.py:154-172): (n,4,4) row-major
+ * world matrices at the start and end of the next advance. MPM_ERR_VALUE if n != collider count. */
+int mpm_set_collider_transforms(void *handle, int32_t n, const float *start16, const float *end16);
+
+/* Solver.advance (mpm_core/solver.py:64-65; warp/solver.py:176-240): CFL time step, substeps, removal of
+ * particles past open sides. With no particles: {0, frame_dt, 0}. */
+int mpm_advance(void *handle, double frame_dt, MpmAdvanceStats *stats);
+
+/* One substep with a given dt and substep fraction s (WarpSolver._substep, warp/solver.py:187-211), for
+ * fixed-dt runs and parity checks. frame_dt is the advance duration the collider velocities refer to. */
+int mpm_substep(void *handle, double dt, double s, double frame_dt);
+
+/* Solver.particle_count (mpm_core/solver.py:67-69). */
+int mpm_particle_count(void *handle, int64_t *n);
+
+/* Solver.get_particles (mpm_core/solver.py:71-72; warp/solver.py:131-132). Any output may be NULL. */
+int mpm_get_particles(void *handle, float *x, float *v, int32_t *material_ids, int32_t *emitter_ids);
+
+/* Solver.is_occupied (mpm_core/solver.py:74-76; warp/solver.py:244-255; kernels.py:272-298). */
+int mpm_is_occupied(void *handle, int64_t m, const float *points, uint8_t *out);
+
+/* Solver.save_state / load_state (mpm_core/solver.py:78-82; warp/solver.py:134-138): keys x, v, C, F, Jp,
+ * mat, emitter. load_state replaces every particle; MPM_ERR_VALUE for an out-of-range material id. */
+int mpm_save_state(void *handle, float *x, float *v, float *C, float *F, float *Jp, int32_t *mat, int32_t *emitter);
+int mpm_load_state(void *handle, int64_t n, const float *x, const float *v, const float *C, const float *F,
+                   const float *Jp, const int32_t *mat, const int32_t *emitter);
+
+/* Runtime options (no reference counterpart; tuning and measurement of this backend). */
+enum {
+    MPM_OPT_USE_GRAPH = 1,     /* 1 (default): replay a captured CUDA graph per substep */
+    MPM_OPT_KERNEL_TIMING = 2  /* 1: record CUDA events around each kernel of every substep */
+};
+int mpm_set_option(void *handle, int32_t option, int64_t value);
+
+/* The CUDA stream (cudaStream_t) all work of this handle runs on, for callers that time or order it. */
+int mpm_get_stream(void *handle, void **stream);
+int mpm_synchronize(void *handle);
+
+/* Per-kernel totals since the last reset, when MPM_OPT_KERNEL_TIMING is on: names are
+ * "p2g", "grid_update", "g2p", "other"; ms[i] total milliseconds and launches[i] counts. */
+int mpm_kernel_times(void *handle, int32_t n_slots, float *ms, int64_t *launches, int32_t reset);
+
+/* Read-back for checks and tooling (no reference counterpart; the reference's grid lives in Warp arrays
+ * grid_v / grid_m, warp/solver.py:73-74). mpm_grid_dims: padded node counts (grid_shape + 6).
+ * mpm_read_grid: dims[0]*dims[1]*dims[2] nodes in C order, 4 floats each: velocity xyz after the grid update
+ * (momentum where the mass is zero) and mass, as left by the last substep.
+ * mpm_read_collider_pose: collider c's pose of the last substep as 3x4 row-major matrices: the world
+ * transform M, its inverse, and dM, the time derivative the collider velocity is taken from. */
+int mpm_grid_dims(void *handle, int32_t dims[3]);
+int mpm_read_grid(void *handle, float *out);
+int mpm_read_collider_pose(void *handle, int32_t c, float *M12, float *Minv12, float *dM12);
+
+/* Kernels of this library launched on the handle's stream since it was created. */
+int mpm_launch_count(void *handle, int64_t *launches);
+
+/* Number of SVD lanes that took the FP64 path since the handle was created. */
+int mpm_fp64_lanes(void *handle, int64_t *lanes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

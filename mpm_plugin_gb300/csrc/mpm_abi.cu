@@ -1,0 +1,966 @@
+// Host side of the C-ABI in include/mpm_gb300.h: device memory, host-side constants, collider BVHs, the
+// substep launch sequence (captured once into a CUDA graph and replayed per substep), CFL time stepping,
+// removal of escaped particles and state I/O.
+//
+// The host constants follow mpm_core/backends/warp/solver.py:37-71 in float64 and are rounded to FP32
+// when stored for the kernels, as the reference's launches do.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mpm_gb300.h"
+#include "mpm_bvh.h"
+#include "mpm_internal.h"
+
+using namespace mpm;
+
+namespace {
+
+constexpr double kCFL = 0.4;                // warp/solver.py:19
+constexpr double kColliderThickness = 2.0;  // warp/solver.py:20
+constexpr int kFields = 28;                 // x3 v3 C9 F9 Jp mat emitter id
+
+thread_local std::string g_last_error;
+
+struct Status {
+    int code = MPM_OK;
+    std::string msg;
+};
+
+struct Handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    MpmDomainDesc dom{};
+    double dx = 0, inv_dx = 0, p_vol = 0;
+    double origin[3] = {0, 0, 0};
+    int dims[3] = {0, 0, 0};
+    GridDesc g{};
+    int ppc = 8;
+    std::vector<MpmMaterialDesc> mat_desc;
+    std::vector<double> wave;          // P-wave speed per material incl. worst-case snow hardening
+    std::vector<int64_t> mat_count;    // particles per material ("present" materials)
+    Material* d_mats = nullptr;
+
+    Particles P{}, spare{};
+    void* arena = nullptr;
+    void* spare_arena = nullptr;
+
+    float4* grid = nullptr;
+    int64_t grid_nodes = 0;
+    float* vol = nullptr;              // occupancy scratch, one float per node
+
+    StepParams* d_sp = nullptr;
+    unsigned int* d_counters = nullptr;  // [0] vmax bits, [1] fp64 lanes, [2..] removed per material
+    unsigned int* h_counters = nullptr;  // pinned
+
+    int n_col = 0;
+    std::vector<ColliderDev> cols;
+    std::vector<std::vector<float>> col_verts;
+    ColliderDev* d_cols = nullptr;
+    BvhNode* d_nodes = nullptr;
+    MeshTri* d_tris = nullptr;
+    double frame_dt = 1.0;
+
+    // removal scratch
+    int32_t* d_keep = nullptr;  // keep_phys | keep_by_id | dst_index | new_id, each cap entries
+    int32_t* d_scan_tmp = nullptr;
+    int64_t keep_cap = 0, scan_cap = 0;
+
+    void* stage = nullptr;  // device staging for host-order arrays
+    size_t stage_bytes = 0;
+
+    int64_t launches = 0;       // kernels of this library launched so far (graph replays count their kernels)
+    int64_t graph_kernels = 0;  // kernels in the captured substep graph
+
+    bool use_graph = true;
+    cudaGraphExec_t graph = nullptr;
+    int64_t graph_key[4] = {-1, -1, -1, -1};
+
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::vector<cudaEvent_t>> ev_pending;  // per substep: 4 events around p2g / grid / g2p
+    double t_ms[4] = {0, 0, 0, 0};
+    int64_t t_launches[4] = {0, 0, 0, 0};
+
+    std::string err;
+};
+
+#define CK(call)                                                                                     \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return Status{MPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+    } while (0)
+
+#define TRY(expr)                            \
+    do {                                     \
+        Status s_ = (expr);                  \
+        if (s_.code != MPM_OK) return s_;    \
+    } while (0)
+
+int finish(Handle* h, Status s) {
+    if (s.code != MPM_OK) {
+        if (h) h->err = s.msg;
+        g_last_error = s.msg;
+    }
+    return s.code;
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur;
+        if (cudaGetDevice(&cur) == cudaSuccess && prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// ---- particles -------------------------------------------------------------------------------------
+
+Particles bind_arena(void* base, int64_t cap, int64_t n) {
+    Particles P{};
+    float* f = static_cast<float*>(base);
+    for (int a = 0; a < 3; ++a) P.x[a] = f + (int64_t)a * cap;
+    for (int a = 0; a < 3; ++a) P.v[a] = f + (int64_t)(3 + a) * cap;
+    for (int e = 0; e < 9; ++e) P.C[e] = f + (int64_t)(6 + e) * cap;
+    for (int e = 0; e < 9; ++e) P.F[e] = f + (int64_t)(15 + e) * cap;
+    P.Jp = f + (int64_t)24 * cap;
+    P.mat = reinterpret_cast<int32_t*>(f + (int64_t)25 * cap);
+    P.emitter = reinterpret_cast<int32_t*>(f + (int64_t)26 * cap);
+    P.id = reinterpret_cast<int32_t*>(f + (int64_t)27 * cap);
+    P.n = n;
+    P.cap = cap;
+    return P;
+}
+
+void invalidate_graph(Handle* h) {
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+    h->graph_key[0] = -1;
+}
+
+Status ensure_capacity(Handle* h, int64_t need) {
+    if (need <= h->P.cap) return {};
+    int64_t cap = std::max<int64_t>({need, 2 * h->P.cap, 4096});
+    void* fresh = nullptr;
+    if (cudaMalloc(&fresh, (size_t)cap * kFields * 4) != cudaSuccess) {
+        cudaGetLastError();
+        return {MPM_ERR_MEMORY, "device allocation of particle storage failed"};
+    }
+    Particles np = bind_arena(fresh, cap, h->P.n);
+    if (h->P.n > 0) {  // keep the live particles: copy each field's first n entries
+        const float* src = static_cast<const float*>(h->arena);
+        float* dst = static_cast<float*>(fresh);
+        for (int f = 0; f < kFields; ++f)
+            CK(cudaMemcpyAsync(dst + (int64_t)f * cap, src + (int64_t)f * h->P.cap, (size_t)h->P.n * 4,
+                               cudaMemcpyDeviceToDevice, h->stream));
+    }
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->arena) cudaFree(h->arena);
+    if (h->spare_arena) cudaFree(h->spare_arena);
+    h->spare_arena = nullptr;
+    h->arena = fresh;
+    h->P = np;
+    h->spare = Particles{};
+    invalidate_graph(h);
+    return {};
+}
+
+Status ensure_stage(Handle* h, size_t bytes) {
+    if (bytes <= h->stage_bytes) return {};
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->stage) cudaFree(h->stage);
+    h->stage = nullptr;
+    size_t b = std::max(bytes, h->stage_bytes * 2);
+    if (cudaMalloc(&h->stage, b) != cudaSuccess) {
+        cudaGetLastError();
+        h->stage_bytes = 0;
+        return {MPM_ERR_MEMORY, "device allocation of the staging buffer failed"};
+    }
+    h->stage_bytes = b;
+    return {};
+}
+
+// ---- host pose math (mpm_core/geometry.py:30-50, warp/solver.py:154-172) ----------------------------
+
+void svd3_host(const double A[9], double U[9], double s[3], double V[9]) {  // one-sided Jacobi, float64
+    double B[9];
+    std::memcpy(B, A, sizeof B);
+    for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+    const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        bool rotated = false;
+        for (auto& r : pq) {
+            int p = r[0], q = r[1];
+            double al = 0, be = 0, ga = 0;
+            for (int i = 0; i < 3; ++i) {
+                al += B[i * 3 + p] * B[i * 3 + p];
+                be += B[i * 3 + q] * B[i * 3 + q];
+                ga += B[i * 3 + p] * B[i * 3 + q];
+            }
+            if (ga == 0.0 || std::fabs(ga) <= 1e-17 * std::sqrt(al * be)) continue;
+            rotated = true;
+            double zeta = (be - al) / (2.0 * ga);
+            double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+            double c = 1.0 / std::sqrt(1.0 + t * t), sn = c * t;
+            for (int i = 0; i < 3; ++i) {
+                double bp = B[i * 3 + p], bq = B[i * 3 + q];
+                B[i * 3 + p] = c * bp - sn * bq;
+                B[i * 3 + q] = sn * bp + c * bq;
+                double vp = V[i * 3 + p], vq = V[i * 3 + q];
+                V[i * 3 + p] = c * vp - sn * vq;
+                V[i * 3 + q] = sn * vp + c * vq;
+            }
+        }
+        if (!rotated) break;
+    }
+    double n[3];
+    for (int k = 0; k < 3; ++k) n[k] = std::sqrt(B[k] * B[k] + B[3 + k] * B[3 + k] + B[6 + k] * B[6 + k]);
+    int ord[3] = {0, 1, 2};
+    std::sort(ord, ord + 3, [&](int a, int b) { return n[a] > n[b]; });
+    double B2[9], V2[9];
+    for (int k = 0; k < 3; ++k) {
+        s[k] = n[ord[k]];
+        for (int i = 0; i < 3; ++i) {
+            B2[i * 3 + k] = B[i * 3 + ord[k]];
+            V2[i * 3 + k] = V[i * 3 + ord[k]];
+        }
+    }
+    std::memcpy(V, V2, sizeof V2);
+    for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < 3; ++i) U[i * 3 + k] = s[k] > 0 ? B2[i * 3 + k] / s[k] : (i == k ? 1.0 : 0.0);
+}
+
+double det3(const double m[9]) {
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+// World matrix -> translation, rotation quaternion (x, y, z, w), symmetric stretch; M = [R S | t].
+void decompose(const float* m16, double t[3], double q[4], double S[9], double* min_sv) {
+    double A[9];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) A[r * 3 + c] = m16[r * 4 + c];
+    for (int r = 0; r < 3; ++r) t[r] = m16[r * 4 + 3];
+    double U[9], s[3], V[9];
+    svd3_host(A, U, s, V);
+    *min_sv = s[2];
+    double R[9];
+    auto make_R = [&]() {
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) R[r * 3 + c] = U[r * 3] * V[c * 3] + U[r * 3 + 1] * V[c * 3 + 1] + U[r * 3 + 2] * V[c * 3 + 2];
+    };
+    make_R();
+    if (det3(R) < 0) {  // mirrored: R stays a proper rotation, the flip goes into S
+        for (int r = 0; r < 3; ++r) U[r * 3 + 2] = -U[r * 3 + 2];
+        s[2] = -s[2];
+        make_R();
+    }
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) S[r * 3 + c] = V[r * 3] * s[0] * V[c * 3] + V[r * 3 + 1] * s[1] * V[c * 3 + 1] + V[r * 3 + 2] * s[2] * V[c * 3 + 2];
+    // quaternion: magnitudes from the diagonal, signs from the antisymmetric part (mpm_core/geometry.py:42-50)
+    double w = std::sqrt(std::max(0.0, 1 + R[0] + R[4] + R[8])) / 2;
+    double x = std::copysign(std::sqrt(std::max(0.0, 1 + R[0] - R[4] - R[8])) / 2, R[7] - R[5]);
+    double y = std::copysign(std::sqrt(std::max(0.0, 1 - R[0] + R[4] - R[8])) / 2, R[2] - R[6]);
+    double z = std::copysign(std::sqrt(std::max(0.0, 1 - R[0] - R[4] + R[8])) / 2, R[3] - R[1]);
+    double nq = std::sqrt(x * x + y * y + z * z + w * w);
+    q[0] = x / nq; q[1] = y / nq; q[2] = z / nq; q[3] = w / nq;
+}
+
+// ---- substep sequence ---------------------------------------------------------------------------------
+
+void free_colliders(Handle* h) {
+    if (h->d_cols) cudaFree(h->d_cols);
+    if (h->d_nodes) cudaFree(h->d_nodes);
+    if (h->d_tris) cudaFree(h->d_tris);
+    h->d_cols = nullptr;
+    h->d_nodes = nullptr;
+    h->d_tris = nullptr;
+}
+
+cudaEvent_t take_event(Handle* h) {
+    if (!h->ev_pool.empty()) {
+        cudaEvent_t e = h->ev_pool.back();
+        h->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+
+constexpr int kSubstepKernels = 4;  // step_begin, p2g, grid_update, g2p
+
+Status enqueue_substep(Handle* h, std::vector<cudaEvent_t>* ev) {
+    cudaStream_t st = h->stream;
+    launch_step_begin(st, h->d_sp, h->d_cols, h->n_col);
+    CK(cudaMemsetAsync(h->grid, 0, (size_t)h->grid_nodes * sizeof(float4), st));
+    if (ev) CK(cudaEventRecord((*ev)[0], st));
+    launch_p2g(st, h->P, h->d_mats, h->g, h->d_sp, h->grid, h->d_counters + 1);
+    if (ev) CK(cudaEventRecord((*ev)[1], st));
+    launch_grid_update(st, h->g, h->grid, h->d_sp, h->d_cols, h->n_col, h->d_nodes, h->d_tris);
+    if (ev) CK(cudaEventRecord((*ev)[2], st));
+    launch_g2p(st, h->P, h->d_mats, h->g, h->d_sp, h->grid, h->d_cols, h->n_col, h->d_nodes, h->d_tris,
+               h->d_counters + 1);
+    if (ev) CK(cudaEventRecord((*ev)[3], st));
+    CK(cudaGetLastError());
+    return {};
+}
+
+Status run_substep(Handle* h) {
+    if (h->timing) {
+        std::vector<cudaEvent_t> ev(4);
+        for (auto& e : ev) e = take_event(h);
+        TRY(enqueue_substep(h, &ev));
+        h->ev_pending.push_back(ev);
+        h->launches += kSubstepKernels;
+        return {};
+    }
+    if (!h->use_graph) {
+        h->launches += kSubstepKernels;
+        return enqueue_substep(h, nullptr);
+    }
+    int64_t key[4] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena};
+    if (!h->graph || std::memcmp(key, h->graph_key, sizeof key) != 0) {
+        invalidate_graph(h);
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        Status s = enqueue_substep(h, nullptr);
+        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+        if (s.code != MPM_OK) return s;
+        CK(e);
+        e = cudaGraphInstantiate(&h->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(e);
+        std::memcpy(h->graph_key, key, sizeof key);
+    }
+    CK(cudaGraphLaunch(h->graph, h->stream));
+    h->launches += kSubstepKernels;
+    return {};
+}
+
+Status set_step(Handle* h, double dt, double s, double frame_dt, int steps) {
+    StepParams sp{};
+    sp.dt = (float)dt;
+    sp.s = (float)s;
+    sp.inv_frame_dt = (float)(1.0 / frame_dt);
+    sp.k = -1;
+    sp.steps = steps;
+    // a pageable source is staged by the driver before this call returns, so `sp` may go out of scope
+    CK(cudaMemcpyAsync(h->d_sp, &sp, sizeof sp, cudaMemcpyHostToDevice, h->stream));
+    return {};
+}
+
+Status remove_escaped(Handle* h, int32_t* removed_out) {
+    *removed_out = 0;
+    EscapeBounds eb{};
+    bool any = false;
+    for (int a = 0; a < 3; ++a) {
+        eb.open_lo[a] = !h->dom.wall_lo[a];
+        eb.open_hi[a] = !h->dom.wall_hi[a];
+        eb.lo[a] = (float)(h->dom.min[a] - h->dx);
+        eb.hi[a] = (float)(h->dom.max[a] + h->dx);
+        any = any || eb.open_lo[a] || eb.open_hi[a];
+    }
+    if (!any || h->P.n == 0) return {};
+    const int64_t n = h->P.n;
+    if (h->keep_cap < n) {
+        if (h->d_keep) cudaFree(h->d_keep);
+        h->d_keep = nullptr;
+        h->keep_cap = std::max<int64_t>(n, h->P.cap);
+        if (cudaMalloc(&h->d_keep, (size_t)h->keep_cap * 4 * sizeof(int32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            h->keep_cap = 0;
+            return {MPM_ERR_MEMORY, "device allocation of removal scratch failed"};
+        }
+    }
+    int64_t tiles = scan_tile_count(n) + 1;
+    if (h->scan_cap < tiles) {
+        if (h->d_scan_tmp) cudaFree(h->d_scan_tmp);
+        h->scan_cap = std::max<int64_t>(tiles, 1024);
+        if (cudaMalloc(&h->d_scan_tmp, (size_t)(h->scan_cap + 2) * sizeof(int32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            h->scan_cap = 0;
+            return {MPM_ERR_MEMORY, "device allocation of scan scratch failed"};
+        }
+    }
+    int32_t* keep_phys = h->d_keep;
+    int32_t* keep_by_id = h->d_keep + h->keep_cap;
+    int32_t* dst_index = h->d_keep + 2 * h->keep_cap;
+    int32_t* new_id = h->d_keep + 3 * h->keep_cap;
+    const int nm = (int)h->mat_desc.size();
+    CK(cudaMemsetAsync(h->d_counters + 2, 0, sizeof(unsigned int) * nm, h->stream));
+    launch_flag_escaped(h->stream, h->P, eb, keep_phys, keep_by_id, h->d_counters + 2);
+    h->launches += 1;
+    CK(cudaMemcpyAsync(h->h_counters + 2, h->d_counters + 2, sizeof(unsigned int) * nm, cudaMemcpyDeviceToHost,
+                       h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    int64_t removed = 0;
+    for (int m = 0; m < nm; ++m) removed += h->h_counters[2 + m];
+    if (removed == 0) return {};
+    launch_exclusive_scan(h->stream, keep_phys, n, dst_index, h->d_scan_tmp, h->d_scan_tmp + h->scan_cap);
+    launch_exclusive_scan(h->stream, keep_by_id, n, new_id, h->d_scan_tmp, h->d_scan_tmp + h->scan_cap);
+    if (!h->spare_arena) {
+        if (cudaMalloc(&h->spare_arena, (size_t)h->P.cap * kFields * 4) != cudaSuccess) {
+            cudaGetLastError();
+            h->spare_arena = nullptr;
+            return {MPM_ERR_MEMORY, "device allocation of particle storage failed"};
+        }
+    }
+    Particles dst = bind_arena(h->spare_arena, h->P.cap, n - removed);
+    launch_compact(h->stream, h->P, dst, keep_phys, dst_index, new_id);
+    h->launches += 7;  // two three-pass scans and the compaction
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(h->stream));
+    std::swap(h->arena, h->spare_arena);
+    h->P = dst;
+    for (int m = 0; m < nm; ++m) h->mat_count[m] -= h->h_counters[2 + m];
+    invalidate_graph(h);
+    *removed_out = (int32_t)removed;
+    return {};
+}
+
+Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
+    if (h->P.n == 0) {
+        *stats = MpmAdvanceStats{0, frame_dt, 0};
+        return {};
+    }
+    h->frame_dt = frame_dt;
+    // CFL time step (warp/solver.py:176-185): max |v| on the device, one 4-byte read back
+    CK(cudaMemsetAsync(h->d_counters, 0, sizeof(unsigned int), h->stream));
+    launch_max_speed(h->stream, h->P, h->d_counters);
+    h->launches += 1;
+    CK(cudaMemcpyAsync(h->h_counters, h->d_counters, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    float vmax_f;
+    std::memcpy(&vmax_f, &h->h_counters[0], 4);
+    double vmax = std::isfinite(vmax_f) ? (double)vmax_f : 0.0;
+    double c = 0.0;
+    for (size_t m = 0; m < h->wave.size(); ++m)
+        if (h->mat_count[m] > 0) c = std::max(c, h->wave[m]);
+    double dt = std::min(kCFL * h->dx / (c + vmax), frame_dt);
+    int steps = (int)std::ceil(frame_dt / dt - 1e-9);
+    dt = frame_dt / steps;
+    TRY(set_step(h, dt, 0.0, frame_dt, steps));
+    for (int k = 0; k < steps; ++k) TRY(run_substep(h));
+    int32_t removed = 0;
+    TRY(remove_escaped(h, &removed));
+    CK(cudaStreamSynchronize(h->stream));
+    *stats = MpmAdvanceStats{steps, dt, removed};
+    return {};
+}
+
+Status check_mats(Handle* h, int64_t n, const int32_t* mat) {
+    const int nm = (int)h->mat_desc.size();
+    for (int64_t i = 0; i < n; ++i)
+        if (mat[i] < 0 || mat[i] >= nm) return {MPM_ERR_VALUE, "material id out of range"};
+    return {};
+}
+
+Status upload_particles(Handle* h, int64_t off, int64_t n, const float* x, const float* v, const float* C,
+                        const float* F, const float* Jp, const int32_t* mat, const int32_t* emitter) {
+    size_t per = (3 + 3 + (C ? 9 : 0) + (F ? 9 : 0) + (Jp ? 1 : 0) + 2) * 4;
+    TRY(ensure_stage(h, per * (size_t)n));
+    char* s = static_cast<char*>(h->stage);
+    auto put = [&](const void* src, size_t bytes) -> void* {
+        void* dst = s;
+        cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, h->stream);
+        s += bytes;
+        return dst;
+    };
+    const float* dx_ = (const float*)put(x, (size_t)n * 12);
+    const float* dv = (const float*)put(v, (size_t)n * 12);
+    const float* dC = C ? (const float*)put(C, (size_t)n * 36) : nullptr;
+    const float* dF = F ? (const float*)put(F, (size_t)n * 36) : nullptr;
+    const float* dJ = Jp ? (const float*)put(Jp, (size_t)n * 4) : nullptr;
+    const int32_t* dm = (const int32_t*)put(mat, (size_t)n * 4);
+    const int32_t* de = (const int32_t*)put(emitter, (size_t)n * 4);
+    CK(cudaGetLastError());
+    launch_state_in(h->stream, h->P, off, n, dx_, dv, dC, dF, dJ, dm, de);
+    h->launches += 1;
+    CK(cudaGetLastError());
+    return {};
+}
+
+Status download_particles(Handle* h, float* x, float* v, float* C, float* F, float* Jp, int32_t* mat,
+                          int32_t* emitter) {
+    const int64_t n = h->P.n;
+    if (n == 0) return {};
+    size_t per = ((x ? 3 : 0) + (v ? 3 : 0) + (C ? 9 : 0) + (F ? 9 : 0) + (Jp ? 1 : 0) + (mat ? 1 : 0) + (emitter ? 1 : 0)) * 4;
+    TRY(ensure_stage(h, per * (size_t)n));
+    char* s = static_cast<char*>(h->stage);
+    auto slot = [&](const void* host, size_t bytes) -> void* {
+        if (!host) return nullptr;
+        void* d = s;
+        s += bytes;
+        return d;
+    };
+    float* dx_ = (float*)slot(x, (size_t)n * 12);
+    float* dv = (float*)slot(v, (size_t)n * 12);
+    float* dC = (float*)slot(C, (size_t)n * 36);
+    float* dF = (float*)slot(F, (size_t)n * 36);
+    float* dJ = (float*)slot(Jp, (size_t)n * 4);
+    int32_t* dm = (int32_t*)slot(mat, (size_t)n * 4);
+    int32_t* de = (int32_t*)slot(emitter, (size_t)n * 4);
+    launch_state_out(h->stream, h->P, dx_, dv, dC, dF, dJ, dm, de);
+    h->launches += 1;
+    CK(cudaGetLastError());
+    auto get = [&](void* host, const void* dev, size_t bytes) -> cudaError_t {
+        return host ? cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, h->stream) : cudaSuccess;
+    };
+    CK(get(x, dx_, (size_t)n * 12));
+    CK(get(v, dv, (size_t)n * 12));
+    CK(get(C, dC, (size_t)n * 36));
+    CK(get(F, dF, (size_t)n * 36));
+    CK(get(Jp, dJ, (size_t)n * 4));
+    CK(get(mat, dm, (size_t)n * 4));
+    CK(get(emitter, de, (size_t)n * 4));
+    CK(cudaStreamSynchronize(h->stream));
+    return {};
+}
+
+Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_mat, const double gravity[3], int32_t ppc,
+              int32_t device, Handle** out) {
+    if (!dom || !gravity || !out || (n_mat > 0 && !mats)) return {MPM_ERR_ARGUMENT, "null argument"};
+    if (n_mat > kMaxMaterials) return {MPM_ERR_VALUE, "too many materials"};
+    if (ppc <= 0) return {MPM_ERR_VALUE, "particles_per_cell must be positive"};
+    for (int m = 0; m < n_mat; ++m)
+        if (mats[m].model < 0 || mats[m].model > 3)
+            return {MPM_ERR_NOT_IMPLEMENTED, "material model is not supported by the gb300 backend"};
+    Handle* h = new Handle();
+    *out = h;
+    h->device = device;
+    DeviceGuard guard(device);
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->dom = *dom;
+    h->ppc = ppc;
+    // domain constants (mpm_core/scene.py:60-67; warp/solver.py:37-53), float64
+    double size[3], longest = 0;
+    for (int a = 0; a < 3; ++a) {
+        size[a] = dom->max[a] - dom->min[a];
+        longest = std::max(longest, size[a]);
+    }
+    h->dx = longest / dom->resolution;
+    h->inv_dx = 1.0 / h->dx;
+    h->p_vol = std::pow(h->dx, 3.0) / ppc;
+    GridDesc& g = h->g;
+    for (int a = 0; a < 3; ++a) {
+        int shape = std::max(1, (int)std::ceil(size[a] / h->dx - 1e-6));
+        h->dims[a] = shape + 2 * kPad;
+        h->origin[a] = dom->min[a] - kPad * h->dx;
+        g.dims[a] = h->dims[a];
+        g.nb[a] = (h->dims[a] + kBlock - 1) / kBlock;
+        g.origin[a] = (float)h->origin[a];
+        g.gravity[a] = (float)gravity[a];
+        g.lo_on[a] = dom->wall_lo[a] ? 1 : 0;
+        g.hi_on[a] = dom->wall_hi[a] ? 1 : 0;
+        g.wall_lo[a] = (float)dom->min[a];
+        g.wall_hi[a] = (float)dom->max[a];
+        g.clamp_lo[a] = (float)(h->origin[a] + h->dx);
+        g.clamp_hi[a] = (float)(h->origin[a] + (h->dims[a] - 2) * h->dx);
+        g.wall_lo_node[a] = (int)std::floor((dom->min[a] - h->origin[a]) / h->dx + 1e-3);
+        g.wall_hi_node[a] = (int)std::ceil((dom->max[a] - h->origin[a]) / h->dx - 1e-3);
+    }
+    g.dx = (float)h->dx;
+    g.inv_dx = (float)h->inv_dx;
+    g.p_vol = (float)h->p_vol;
+    g.wall_friction = (float)dom->wall_friction;
+    g.thickness = (float)(kColliderThickness * h->dx);
+    g.band = (float)h->dx;
+    // material tables (warp/solver.py:56-71; mpm_core/materials.py:48-51)
+    std::vector<Material> table(std::max(1, (int)n_mat));
+    h->mat_desc.assign(mats, mats + n_mat);
+    h->mat_count.assign(n_mat, 0);
+    for (int m = 0; m < n_mat; ++m) {
+        const MpmMaterialDesc& d = mats[m];
+        double e = d.youngs_modulus, nu = d.poisson_ratio;
+        double mu = e / (2 * (1 + nu)), lam = e * nu / ((1 + nu) * (1 - 2 * nu));
+        double sphi = std::sin(d.friction_angle_deg * (M_PI / 180.0));
+        double alpha = std::sqrt(2.0 / 3.0) * 2 * sphi / (3 - sphi);
+        Material& t = table[m];
+        t.model = d.model;
+        t.mu = (float)mu;
+        t.lam = (float)lam;
+        t.yield_stress = (float)d.yield_stress;
+        t.alpha = (float)alpha;
+        t.hardening = (float)d.hardening;
+        t.max_hardening = (float)d.max_hardening;
+        t.clamp_lo = 1.0f - (float)d.critical_compression;
+        t.clamp_hi = 1.0f + (float)d.critical_stretch;
+        t.p_mass = (float)d.density * (float)h->p_vol;
+        h->wave.push_back(std::sqrt((lam + 2 * mu) * (d.model == MPM_MODEL_SNOW ? d.max_hardening : 1.0) / d.density));
+    }
+    CK(cudaMalloc(&h->d_mats, sizeof(Material) * table.size()));
+    CK(cudaMemcpy(h->d_mats, table.data(), sizeof(Material) * table.size(), cudaMemcpyHostToDevice));
+    h->grid_nodes = (int64_t)g.nb[0] * g.nb[1] * g.nb[2] * 64;
+    if (cudaMalloc(&h->grid, (size_t)h->grid_nodes * sizeof(float4)) != cudaSuccess) {
+        cudaGetLastError();
+        return {MPM_ERR_MEMORY, "device allocation of the grid failed"};
+    }
+    CK(cudaMemset(h->grid, 0, (size_t)h->grid_nodes * sizeof(float4)));
+    CK(cudaMalloc(&h->d_sp, sizeof(StepParams)));
+    CK(cudaMemset(h->d_sp, 0, sizeof(StepParams)));
+    CK(cudaMalloc(&h->d_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
+    CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * (2 + kMaxMaterials)));
+    CK(cudaMallocHost(&h->h_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
+    TRY(ensure_capacity(h, 4096));
+    return {};
+}
+
+void destroy(Handle* h) {
+    if (!h) return;
+    DeviceGuard guard(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    invalidate_graph(h);
+    for (auto& v : h->ev_pending)
+        for (auto e : v) cudaEventDestroy(e);
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    free_colliders(h);
+    cudaFree(h->arena);
+    cudaFree(h->spare_arena);
+    cudaFree(h->grid);
+    cudaFree(h->vol);
+    cudaFree(h->d_mats);
+    cudaFree(h->d_sp);
+    cudaFree(h->d_counters);
+    cudaFree(h->d_keep);
+    cudaFree(h->d_scan_tmp);
+    cudaFree(h->stage);
+    if (h->h_counters) cudaFreeHost(h->h_counters);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+Status set_transforms(Handle* h, int32_t n, const float* start16, const float* end16) {
+    if (n != h->n_col) return {MPM_ERR_VALUE, "expected " + std::to_string(h->n_col) + " collider transforms"};
+    if (n == 0) return {};
+    if (!start16 || !end16) return {MPM_ERR_ARGUMENT, "null transform array"};
+    for (int c = 0; c < n; ++c) {
+        double t0[3], q0[4], S0[9], t1[3], q1[4], S1[9], sv0, sv1;
+        decompose(start16 + 16 * c, t0, q0, S0, &sv0);
+        decompose(end16 + 16 * c, t1, q1, S1, &sv1);
+        if (q0[0] * q1[0] + q0[1] * q1[1] + q0[2] * q1[2] + q0[3] * q1[3] < 0)
+            for (double& v : q1) v = -v;  // slerp the short way round
+        ColliderDev& col = h->cols[c];
+        for (int k = 0; k < 3; ++k) { col.t0[k] = (float)t0[k]; col.t1[k] = (float)t1[k]; }
+        for (int k = 0; k < 4; ++k) { col.q0[k] = (float)q0[k]; col.q1[k] = (float)q1[k]; }
+        for (int k = 0; k < 9; ++k) { col.S0[k] = (float)S0[k]; col.S1[k] = (float)S1[k]; }
+        // AABB early-out margin: three cells in local units under the strongest shrink of either pose
+        double inv_scale = std::max(1.0 / std::max(sv0, 1e-12), 1.0 / std::max(sv1, 1e-12));
+        col.margin = (float)(3.0 * h->dx * inv_scale);
+    }
+    CK(cudaMemcpyAsync(h->d_cols, h->cols.data(), sizeof(ColliderDev) * n, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    return {};
+}
+
+Status set_colliders(Handle* h, int32_t n, const MpmColliderDesc* cs) {
+    if (n < 0 || (n > 0 && !cs)) return {MPM_ERR_ARGUMENT, "bad collider list"};
+    CK(cudaStreamSynchronize(h->stream));
+    free_colliders(h);
+    invalidate_graph(h);
+    h->cols.assign(n, ColliderDev{});
+    h->n_col = n;
+    std::vector<BvhNode> all_nodes;
+    std::vector<MeshTri> all_tris;
+    for (int c = 0; c < n; ++c) {
+        const MpmColliderDesc& d = cs[c];
+        if (d.n_tris < 0 || d.n_verts < 0 || (d.n_tris > 0 && (!d.tris || !d.verts)))
+            return {MPM_ERR_VALUE, "bad collider mesh"};
+        for (int i = 0; i < 3 * d.n_tris; ++i)
+            if (d.tris[i] < 0 || d.tris[i] >= d.n_verts) return {MPM_ERR_VALUE, "collider triangle index out of range"};
+        ColliderDev& col = h->cols[c];
+        col.closed = d.closed ? 1 : 0;
+        col.friction = (float)d.friction;
+        col.node_offset = (int)all_nodes.size();
+        col.tri_offset = (int)all_tris.size();
+        col.n_tris = d.n_tris;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int i = 0; i < d.n_verts; ++i)
+            for (int a = 0; a < 3; ++a) {
+                lo[a] = std::min(lo[a], d.verts[3 * i + a]);
+                hi[a] = std::max(hi[a], d.verts[3 * i + a]);
+            }
+        for (int a = 0; a < 3; ++a) { col.aabb_lo[a] = lo[a]; col.aabb_hi[a] = hi[a]; }
+        col.mesh_scale = 0.0f;
+        for (int a = 0; a < 3 && d.n_verts > 0; ++a) col.mesh_scale = std::max({col.mesh_scale, std::fabs(lo[a]), std::fabs(hi[a])});
+        std::vector<BvhNode> nodes;
+        std::vector<MeshTri> tris;
+        build_mesh(MeshInput{d.n_verts, d.n_tris, d.verts, d.tris}, nodes, tris);
+        all_nodes.insert(all_nodes.end(), nodes.begin(), nodes.end());  // child indices stay collider-local
+        all_tris.insert(all_tris.end(), tris.begin(), tris.end());
+    }
+    if (n > 0) {
+        CK(cudaMalloc(&h->d_cols, sizeof(ColliderDev) * n));
+        CK(cudaMalloc(&h->d_nodes, sizeof(BvhNode) * std::max<size_t>(1, all_nodes.size())));
+        CK(cudaMalloc(&h->d_tris, sizeof(MeshTri) * std::max<size_t>(1, all_tris.size())));
+        CK(cudaMemcpy(h->d_nodes, all_nodes.data(), sizeof(BvhNode) * all_nodes.size(), cudaMemcpyHostToDevice));
+        if (!all_tris.empty())
+            CK(cudaMemcpy(h->d_tris, all_tris.data(), sizeof(MeshTri) * all_tris.size(), cudaMemcpyHostToDevice));
+        std::vector<float> eye(16 * (size_t)n, 0.0f);
+        for (int c = 0; c < n; ++c)
+            for (int k = 0; k < 4; ++k) eye[16 * c + 5 * k] = 1.0f;
+        TRY(set_transforms(h, n, eye.data(), eye.data()));
+    }
+    return {};
+}
+
+}  // namespace
+
+// ============================================================================================================
+// C-ABI
+// ============================================================================================================
+extern "C" {
+
+int mpm_create(const MpmDomainDesc* domain, const MpmMaterialDesc* materials, int32_t n_materials,
+               const double gravity[3], int32_t particles_per_cell, int32_t device, void** handle) {
+    Handle* h = nullptr;
+    Status s = create(domain, materials, n_materials, gravity, particles_per_cell, device, &h);
+    if (s.code != MPM_OK) {
+        destroy(h);
+        if (handle) *handle = nullptr;
+        return finish(nullptr, s);
+    }
+    *handle = h;
+    return MPM_OK;
+}
+
+int mpm_destroy(void* handle) {
+    destroy(static_cast<Handle*>(handle));
+    return MPM_OK;
+}
+
+const char* mpm_last_error(void* handle) {
+    return handle ? static_cast<Handle*>(handle)->err.c_str() : g_last_error.c_str();
+}
+
+#define HANDLE_OR_FAIL(hv)                                                                     \
+    Handle* h = static_cast<Handle*>(hv);                                                      \
+    if (!h) return finish(nullptr, Status{MPM_ERR_ARGUMENT, "null handle"});                   \
+    DeviceGuard guard_(h->device)
+
+int mpm_add_particles(void* handle, int64_t n, const float* x, const float* v, const int32_t* material_ids,
+                      const int32_t* emitter_ids) {
+    HANDLE_OR_FAIL(handle);
+    if (n == 0) return MPM_OK;
+    if (n < 0 || !x || !v || !material_ids || !emitter_ids) return finish(h, {MPM_ERR_ARGUMENT, "bad particle arrays"});
+    auto run = [&]() -> Status {
+        TRY(check_mats(h, n, material_ids));
+        TRY(ensure_capacity(h, h->P.n + n));
+        TRY(upload_particles(h, h->P.n, n, x, v, nullptr, nullptr, nullptr, material_ids, emitter_ids));
+        CK(cudaStreamSynchronize(h->stream));
+        h->P.n += n;
+        for (int64_t i = 0; i < n; ++i) h->mat_count[material_ids[i]] += 1;
+        invalidate_graph(h);
+        return {};
+    };
+    return finish(h, run());
+}
+
+int mpm_set_colliders(void* handle, int32_t n, const MpmColliderDesc* colliders) {
+    HANDLE_OR_FAIL(handle);
+    return finish(h, set_colliders(h, n, colliders));
+}
+
+int mpm_set_collider_transforms(void* handle, int32_t n, const float* start16, const float* end16) {
+    HANDLE_OR_FAIL(handle);
+    return finish(h, set_transforms(h, n, start16, end16));
+}
+
+int mpm_advance(void* handle, double frame_dt, MpmAdvanceStats* stats) {
+    HANDLE_OR_FAIL(handle);
+    if (!stats) return finish(h, {MPM_ERR_ARGUMENT, "null stats"});
+    if (!(frame_dt > 0)) return finish(h, {MPM_ERR_VALUE, "frame_dt must be positive"});
+    return finish(h, do_advance(h, frame_dt, stats));
+}
+
+int mpm_substep(void* handle, double dt, double s, double frame_dt) {
+    HANDLE_OR_FAIL(handle);
+    auto run = [&]() -> Status {
+        if (h->P.n == 0) return {};
+        h->frame_dt = frame_dt;
+        TRY(set_step(h, dt, s, frame_dt, 0));
+        return run_substep(h);
+    };
+    return finish(h, run());
+}
+
+int mpm_particle_count(void* handle, int64_t* n) {
+    HANDLE_OR_FAIL(handle);
+    if (!n) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    *n = h->P.n;
+    return MPM_OK;
+}
+
+int mpm_get_particles(void* handle, float* x, float* v, int32_t* material_ids, int32_t* emitter_ids) {
+    HANDLE_OR_FAIL(handle);
+    return finish(h, download_particles(h, x, v, nullptr, nullptr, nullptr, material_ids, emitter_ids));
+}
+
+int mpm_save_state(void* handle, float* x, float* v, float* C, float* F, float* Jp, int32_t* mat, int32_t* emitter) {
+    HANDLE_OR_FAIL(handle);
+    return finish(h, download_particles(h, x, v, C, F, Jp, mat, emitter));
+}
+
+int mpm_load_state(void* handle, int64_t n, const float* x, const float* v, const float* C, const float* F,
+                   const float* Jp, const int32_t* mat, const int32_t* emitter) {
+    HANDLE_OR_FAIL(handle);
+    if (n < 0 || (n > 0 && (!x || !v || !C || !F || !Jp || !mat || !emitter)))
+        return finish(h, {MPM_ERR_ARGUMENT, "bad state arrays"});
+    auto run = [&]() -> Status {
+        TRY(check_mats(h, n, mat));
+        CK(cudaStreamSynchronize(h->stream));
+        h->P.n = 0;
+        TRY(ensure_capacity(h, n));
+        if (n > 0) TRY(upload_particles(h, 0, n, x, v, C, F, Jp, mat, emitter));
+        CK(cudaStreamSynchronize(h->stream));
+        h->P.n = n;
+        std::fill(h->mat_count.begin(), h->mat_count.end(), 0);
+        for (int64_t i = 0; i < n; ++i) h->mat_count[mat[i]] += 1;
+        invalidate_graph(h);
+        return {};
+    };
+    return finish(h, run());
+}
+
+int mpm_is_occupied(void* handle, int64_t m, const float* points, uint8_t* out) {
+    HANDLE_OR_FAIL(handle);
+    if (m == 0) return MPM_OK;
+    if (m < 0 || !points || !out) return finish(h, {MPM_ERR_ARGUMENT, "bad query arrays"});
+    auto run = [&]() -> Status {
+        if (!h->vol) {
+            if (cudaMalloc(&h->vol, (size_t)h->grid_nodes * sizeof(float)) != cudaSuccess) {
+                cudaGetLastError();
+                h->vol = nullptr;
+                return {MPM_ERR_MEMORY, "device allocation of the occupancy grid failed"};
+            }
+        }
+        TRY(ensure_stage(h, (size_t)m * 13));
+        float* dpts = static_cast<float*>(h->stage);
+        uint8_t* dout = reinterpret_cast<uint8_t*>(dpts + 3 * m);
+        CK(cudaMemsetAsync(h->vol, 0, (size_t)h->grid_nodes * sizeof(float), h->stream));
+        launch_scatter_volume(h->stream, h->P, h->g, h->vol);
+        CK(cudaMemcpyAsync(dpts, points, (size_t)m * 12, cudaMemcpyHostToDevice, h->stream));
+        launch_query_fill(h->stream, h->g, h->vol, (float)std::pow(h->dx, 3.0), m, dpts, dout);
+        h->launches += 2;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(out, dout, (size_t)m, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return {};
+    };
+    return finish(h, run());
+}
+
+int mpm_set_option(void* handle, int32_t option, int64_t value) {
+    HANDLE_OR_FAIL(handle);
+    switch (option) {
+        case MPM_OPT_USE_GRAPH:
+            h->use_graph = value != 0;
+            if (!h->use_graph) invalidate_graph(h);
+            return MPM_OK;
+        case MPM_OPT_KERNEL_TIMING:
+            h->timing = value != 0;
+            return MPM_OK;
+        default:
+            return finish(h, {MPM_ERR_VALUE, "unknown option"});
+    }
+}
+
+int mpm_get_stream(void* handle, void** stream) {
+    HANDLE_OR_FAIL(handle);
+    if (!stream) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    *stream = h->stream;
+    return MPM_OK;
+}
+
+int mpm_synchronize(void* handle) {
+    HANDLE_OR_FAIL(handle);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
+    return MPM_OK;
+}
+
+int mpm_kernel_times(void* handle, int32_t n_slots, float* ms, int64_t* launches, int32_t reset) {
+    HANDLE_OR_FAIL(handle);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
+    for (auto& ev : h->ev_pending) {
+        for (int k = 0; k < 3; ++k) {
+            float t = 0;
+            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+            h->t_ms[k] += t;
+            h->t_launches[k] += 1;
+        }
+        for (auto x : ev) h->ev_pool.push_back(x);
+    }
+    h->ev_pending.clear();
+    for (int i = 0; i < n_slots && i < 4; ++i) {
+        if (ms) ms[i] = (float)h->t_ms[i];
+        if (launches) launches[i] = h->t_launches[i];
+    }
+    if (reset)
+        for (int i = 0; i < 4; ++i) { h->t_ms[i] = 0; h->t_launches[i] = 0; }
+    return MPM_OK;
+}
+
+int mpm_grid_dims(void* handle, int32_t dims[3]) {
+    HANDLE_OR_FAIL(handle);
+    if (!dims) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    for (int a = 0; a < 3; ++a) dims[a] = h->dims[a];
+    return MPM_OK;
+}
+
+int mpm_read_grid(void* handle, float* out) {
+    HANDLE_OR_FAIL(handle);
+    if (!out) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    auto run = [&]() -> Status {
+        size_t bytes = (size_t)h->dims[0] * h->dims[1] * h->dims[2] * sizeof(float4);
+        TRY(ensure_stage(h, bytes));
+        launch_grid_unblock(h->stream, h->g, h->grid, static_cast<float4*>(h->stage));
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(out, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return {};
+    };
+    return finish(h, run());
+}
+
+int mpm_read_collider_pose(void* handle, int32_t c, float* M12, float* Minv12, float* dM12) {
+    HANDLE_OR_FAIL(handle);
+    if (c < 0 || c >= h->n_col) return finish(h, {MPM_ERR_VALUE, "collider index out of range"});
+    auto run = [&]() -> Status {
+        ColliderDev col;
+        CK(cudaMemcpyAsync(&col, h->d_cols + c, sizeof col, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (M12) std::memcpy(M12, col.M, sizeof col.M);
+        if (Minv12) std::memcpy(Minv12, col.Minv, sizeof col.Minv);
+        if (dM12) std::memcpy(dM12, col.dM, sizeof col.dM);
+        return {};
+    };
+    return finish(h, run());
+}
+
+int mpm_launch_count(void* handle, int64_t* launches) {
+    HANDLE_OR_FAIL(handle);
+    if (!launches) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    *launches = h->launches;
+    return MPM_OK;
+}
+
+int mpm_fp64_lanes(void* handle, int64_t* lanes) {
+    HANDLE_OR_FAIL(handle);
+    cudaError_t e = cudaMemcpyAsync(h->h_counters + 1, h->d_counters + 1, sizeof(unsigned int),
+                                    cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
+    if (lanes) *lanes = h->h_counters[1];
+    return MPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,509 @@
+// Device-side math of the MLS-MPM substep: 3x3 SVD, quadratic B-spline weights, constitutive models and
+// return mappings, mesh closest-point queries. Each function names the reference code it computes the
+// same result as (mpm_core/backends/warp/kernels.py, colliders.py).
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mpm_types.h"
+
+// The math below also compiles for the host (tests check the SVD's accuracy on the CPU).
+#define MPM_HD __host__ __device__ __forceinline__
+
+namespace mpm {
+
+// ---------------------------------------------------------------------------------------------------------
+// 3x3 SVD with the convention of Warp's svd3 (called at kernels.py:35,57,252): U and V proper rotations,
+// singular values in decreasing order, the sign of det(A) carried by the last one.
+//
+// Method: cyclic Jacobi eigen-decomposition of a symmetric 3x3 with exact rotation angles (the Numerical
+// Recipes 11.1 update) for V, then a Givens QR of A V for U (McAdams et al. 2011 use this split, with
+// approximate angles). The FP32 instance reports how far its QR factor is from diagonal; the rare lanes
+// that did not converge are redone in FP64.
+// ---------------------------------------------------------------------------------------------------------
+template <typename T>
+MPM_HD T rsqrt_t(T x);
+#ifdef __CUDA_ARCH__
+template <>
+MPM_HD float rsqrt_t<float>(float x) { return rsqrtf(x); }
+template <>
+MPM_HD double rsqrt_t<double>(double x) { return rsqrt(x); }
+#else
+template <>
+MPM_HD float rsqrt_t<float>(float x) { return 1.0f / sqrtf(x); }
+template <>
+MPM_HD double rsqrt_t<double>(double x) { return 1.0 / sqrt(x); }
+#endif
+
+template <typename T>
+MPM_HD T sqrt_t(T x) { return sqrt(x); }
+
+template <typename T>
+MPM_HD void jacobi_rotate(T S[3][3], T V[3][3], int p, int q) {
+    const int r = 3 - p - q;
+    T apq = S[p][q];
+    if (apq == T(0)) return;
+    T zeta = (S[q][q] - S[p][p]) / (T(2) * apq);
+    T az = fabs(zeta);
+    // t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)); for huge |zeta| the square would overflow, t -> 1/(2 zeta)
+    T t = az > T(1e18) ? T(0.5) / zeta : copysign(T(1), zeta) / (az + sqrt_t(T(1) + zeta * zeta));
+    T c = rsqrt_t(T(1) + t * t);
+    T s = t * c;
+    S[p][p] -= t * apq;
+    S[q][q] += t * apq;
+    S[p][q] = S[q][p] = T(0);
+    T srp = S[r][p], srq = S[r][q];
+    S[r][p] = S[p][r] = c * srp - s * srq;
+    S[r][q] = S[q][r] = s * srp + c * srq;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T vp = V[i][p], vq = V[i][q];
+        V[i][p] = c * vp - s * vq;
+        V[i][q] = s * vp + c * vq;
+    }
+}
+
+// Givens rotation zeroing B[b][col] against B[a][col]; accumulates U <- U G^T.
+template <typename T>
+MPM_HD void givens_qr_step(T B[3][3], T U[3][3], int a, int b, int col) {
+    T x = B[a][col], y = B[b][col];
+    T rr = x * x + y * y;
+    T c = T(1), s = T(0);
+    if (rr > T(0)) {
+        T inv = rsqrt_t(rr);
+        c = x * inv;
+        s = y * inv;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        T ba = B[a][j], bb = B[b][j];
+        B[a][j] = c * ba + s * bb;
+        B[b][j] = -s * ba + c * bb;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T ua = U[i][a], ub = U[i][b];
+        U[i][a] = c * ua + s * ub;
+        U[i][b] = -s * ua + c * ub;
+    }
+}
+
+template <typename T>
+MPM_HD void swap_cols(T M[3][3], int a, int b, bool negate) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T t = M[i][a];
+        M[i][a] = negate ? -M[i][b] : M[i][b];
+        M[i][b] = t;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// SVD in deviation form, for the MPM regime F ~ I. The eigenvalues of E = A^T A - I, formed as
+// G + G^T + G^T G from G = A - I (exact in FP32 near I), give d = sigma - 1 to full relative accuracy,
+// so strains of 1e-4 keep ~7 significant digits where sigma itself would keep 3 (singular values below 0.5
+// come from the QR diagonal instead, where sqrt(1 + e) would cancel). V: Jacobi eigenvectors of E;
+// U: Givens QR of A V (proper rotation; the QR factor's last diagonal carries sign(det A)).
+// Returns the largest off-diagonal of the QR factor relative to sigma_0 (a convergence measure).
+// ---------------------------------------------------------------------------------------------------------
+template <typename T, int SWEEPS>
+MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) {
+    T G[3][3], E[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) G[i][j] = A[i][j] - (i == j ? T(1) : T(0));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            E[i][j] = G[i][j] + G[j][i] + (G[0][i] * G[0][j] + G[1][i] * G[1][j] + G[2][i] * G[2][j]);
+            V[i][j] = i == j ? T(1) : T(0);
+            U[i][j] = i == j ? T(1) : T(0);
+        }
+#pragma unroll
+    for (int sw = 0; sw < SWEEPS; ++sw) {
+        jacobi_rotate(E, V, 0, 1);
+        jacobi_rotate(E, V, 0, 2);
+        jacobi_rotate(E, V, 1, 2);
+    }
+    T e0 = E[0][0], e1 = E[1][1], e2 = E[2][2];
+    // descending eigenvalues; a swap negates one column so det(V) stays +1
+    if (e0 < e1) { swap_cols(V, 0, 1, true); T t = e0; e0 = e1; e1 = t; }
+    if (e0 < e2) { swap_cols(V, 0, 2, true); T t = e0; e0 = e2; e2 = t; }
+    if (e1 < e2) { swap_cols(V, 1, 2, true); T t = e1; e1 = e2; e2 = t; }
+    const T e[3] = {e0, e1, e2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        T r = sqrt_t(fmax(T(1) + e[i], T(0)));
+        d[i] = e[i] / (T(1) + r);  // sigma - 1 without cancellation
+        sig[i] = T(1) + d[i];
+    }
+    T B[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) B[i][j] = A[i][0] * V[0][j] + A[i][1] * V[1][j] + A[i][2] * V[2][j];
+    givens_qr_step(B, U, 0, 1, 0);
+    givens_qr_step(B, U, 0, 2, 0);
+    givens_qr_step(B, U, 1, 2, 1);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        if (T(1) + e[i] < T(0.25)) {  // sigma < 0.5: sqrt(1 + e) cancels, the QR diagonal is accurate
+            sig[i] = fabs(B[i][i]);
+            d[i] = sig[i] - T(1);
+        }
+    if (B[2][2] < T(0)) {  // inverted: the last singular value carries the sign of det(A)
+        sig[2] = -sig[2];
+        d[2] = sig[2] - T(1);
+    }
+    T off = fmax(fmax(fabs(B[0][1]), fabs(B[0][2])), fabs(B[1][2]));
+    T scale = fabs(sig[0]);
+    return scale > T(0) ? off / scale : T(0);
+}
+
+// FP32 deviation-form SVD; lanes whose Jacobi sweeps did not diagonalise E to 4e-6 (relative to
+// sigma_0) are redone in FP64 and counted when a counter is given.
+MPM_HD void svd3(const float A[3][3], float U[3][3], float sig[3], float d[3], float V[3][3],
+                 unsigned int* fp64_lanes) {
+    float off = svd3_dev_core<float, 4>(A, U, sig, d, V);
+    if (!(off <= 4e-6f)) {  // also taken for NaN input, which then stays NaN
+        double Ad[3][3], Ud[3][3], sd[3], dd[3], Vd[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Ad[i][j] = A[i][j];
+        svd3_dev_core<double, 8>(Ad, Ud, sd, dd, Vd);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            sig[i] = (float)sd[i];
+            d[i] = (float)dd[i];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                U[i][j] = (float)Ud[i][j];
+                V[i][j] = (float)Vd[i][j];
+            }
+        }
+#ifdef __CUDA_ARCH__
+        if (fp64_lanes) atomicAdd(fp64_lanes, 1u);
+#else
+        if (fp64_lanes) *fp64_lanes += 1u;
+#endif
+    }
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// Quadratic B-spline weights and stencil base: kernels.py:16-27
+// ---------------------------------------------------------------------------------------------------------
+// Stencil base along one axis: floor(xp - 0.5) (kernels.py:25-27). Returns false when the 3-node stencil
+// would leave the padded grid, which also catches NaN and inf positions; such a particle neither scatters
+// nor gathers, so a blown-up particle can never address memory outside the grid.
+MPM_HD bool stencil_axis(float xp, int dims, int* base, float* fx) {
+    float b = floorf(xp - 0.5f);
+    bool ok = b >= 0.0f && b <= (float)(dims - 3);
+    *base = ok ? (int)b : 0;
+    *fx = xp - b;
+    return ok;
+}
+
+MPM_HD void bspline_weights(float fx, float w[3]) {
+    w[0] = 0.5f * (1.5f - fx) * (1.5f - fx);
+    w[1] = 0.75f - (fx - 1.0f) * (fx - 1.0f);
+    w[2] = 0.5f * (fx - 0.5f) * (fx - 0.5f);
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// Kirchhoff stress, written on the left singular basis so no F - R cancellation occurs:
+//   fixed-corotated (kernels.py:30-38): 2 mu (F - R) F^T + lam J (J - 1) I = U diag(2 mu (s-1) s + lam J (J-1)) U^T
+//   Hencky / St. Venant-Kirchhoff (kernels.py:51-60): U diag(2 mu eps + lam tr eps) U^T, eps = log max(s, 1e-4)
+// ---------------------------------------------------------------------------------------------------------
+MPM_HD float jm1(const float d[3]) {  // J - 1 = prod(1 + d) - 1, expanded so small strains keep their digits
+    return d[0] + d[1] + d[2] + (d[0] * d[1] + d[0] * d[2] + d[1] * d[2]) + d[0] * d[1] * d[2];
+}
+
+MPM_HD void sym_from_diag(const float U[3][3], const float g[3], float tau[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tau[i][j] = U[i][0] * g[0] * U[j][0] + U[i][1] * g[1] * U[j][1] + U[i][2] * g[2] * U[j][2];
+}
+
+MPM_HD void fixed_corotated_tau(const float F[3][3], float mu, float lam, float tau[3][3], unsigned int* fp64) {
+    float U[3][3], sig[3], d[3], V[3][3];
+    svd3(F, U, sig, d, V, fp64);
+    float Jm1 = jm1(d);
+    float iso = lam * (1.0f + Jm1) * Jm1;
+    float g[3] = {2.0f * mu * d[0] * sig[0] + iso, 2.0f * mu * d[1] * sig[1] + iso, 2.0f * mu * d[2] * sig[2] + iso};
+    sym_from_diag(U, g, tau);
+}
+
+MPM_HD float safe_log_dev(float s, float d) {  // log(max(s, 1e-4)) from d = s - 1 (kernels.py:41-43)
+    return s > 1.0e-4f ? log1pf(d) : logf(1.0e-4f);
+}
+
+MPM_HD void hencky_tau(const float F[3][3], float mu, float lam, float tau[3][3], unsigned int* fp64) {
+    float U[3][3], sig[3], d[3], V[3][3];
+    svd3(F, U, sig, d, V, fp64);
+    float e0 = safe_log_dev(sig[0], d[0]), e1 = safe_log_dev(sig[1], d[1]), e2 = safe_log_dev(sig[2], d[2]);
+    float tr = e0 + e1 + e2;
+    float two_mu = 2.0f * mu;
+    float g[3] = {two_mu * e0 + lam * tr, two_mu * e1 + lam * tr, two_mu * e2 + lam * tr};
+    sym_from_diag(U, g, tau);
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// Return mappings on singular values: von Mises (kernels.py:63-72), Drucker-Prager after Klar et al. 2016
+// (kernels.py:75-89) and the snow clamp of Stomakhin et al. 2013 (kernels.py:258-262). Each returns the
+// change of the singular values, delta = new - old, computed without cancellation; the caller applies
+// F <- F + U diag(delta) V^T, which equals U diag(new) V^T exactly when the SVD is exact and leaves F
+// untouched (no reconstruction round-off) when nothing is projected. Returns false when delta == 0.
+// ---------------------------------------------------------------------------------------------------------
+MPM_HD bool project_von_mises(const float sig[3], const float d[3], float mu, float yield_stress, float delta[3]) {
+    float e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
+    float third = (e[0] + e[1] + e[2]) / 3.0f;
+    float dev[3] = {e[0] - third, e[1] - third, e[2] - third};
+    float n = sqrtf(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
+    float limit = yield_stress / (2.0f * mu);
+    if (!(n > limit)) return false;
+    float f = limit / n;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) delta[i] = expm1f(third + dev[i] * f) - d[i];
+    return true;
+}
+
+MPM_HD bool project_drucker_prager(const float sig[3], const float d[3], float mu, float lam, float alpha,
+                                   float delta[3]) {
+    float e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
+    float tr = e[0] + e[1] + e[2];
+    if (tr >= 0.0f) {  // separation: stress-free, singular values back to 1
+#pragma unroll
+        for (int i = 0; i < 3; ++i) delta[i] = -d[i];
+        return true;
+    }
+    float third = tr / 3.0f;
+    float dev[3] = {e[0] - third, e[1] - third, e[2] - third};
+    float n = sqrtf(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
+    if (n < 1.0e-10f) return false;
+    float dgamma = n + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * alpha;
+    if (dgamma <= 0.0f) return false;
+    float f = dgamma / n;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) delta[i] = expm1f(e[i] - dev[i] * f) - d[i];
+    return true;
+}
+
+MPM_HD bool project_snow(const float sig[3], const float d[3], float clamp_lo, float clamp_hi, float delta[3],
+                         float* jp_ratio) {
+    bool any = false;
+    float num = 1.0f, den = 1.0f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float ns = fminf(fmaxf(sig[i], clamp_lo), clamp_hi);
+        delta[i] = ns == sig[i] ? 0.0f : (ns - 1.0f) - d[i];
+        any |= delta[i] != 0.0f;
+        num *= sig[i];
+        den *= ns;
+    }
+    *jp_ratio = num / den;
+    return any;
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// Mesh queries: exact closest point on a triangle (Ericson, Real-Time Collision Detection 5.1.5) over a
+// BVH in the collider's local space; inside/outside from the angle-weighted pseudonormal of the closest
+// feature (Baerentzen & Aanaes 2005). Same meaning as Warp's mesh_query_point_sign_normal (colliders.py:50).
+// ---------------------------------------------------------------------------------------------------------
+// region: 0 face, 1..3 vertex a..c, 4 edge ab, 5 edge bc, 6 edge ca
+template <typename T>
+MPM_HD void closest_on_triangle(const T p[3], const T a[3], const T b[3], const T c[3], T bary[3], int* region) {
+    T ab[3], ac[3], ap[3], bp[3], cp[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        ab[i] = b[i] - a[i]; ac[i] = c[i] - a[i]; ap[i] = p[i] - a[i]; bp[i] = p[i] - b[i]; cp[i] = p[i] - c[i];
+    }
+    T d1 = ab[0] * ap[0] + ab[1] * ap[1] + ab[2] * ap[2];
+    T d2 = ac[0] * ap[0] + ac[1] * ap[1] + ac[2] * ap[2];
+    T d3 = ab[0] * bp[0] + ab[1] * bp[1] + ab[2] * bp[2];
+    T d4 = ac[0] * bp[0] + ac[1] * bp[1] + ac[2] * bp[2];
+    T d5 = ab[0] * cp[0] + ab[1] * cp[1] + ab[2] * cp[2];
+    T d6 = ac[0] * cp[0] + ac[1] * cp[1] + ac[2] * cp[2];
+    const T one(1), zero(0);
+    if (d1 <= zero && d2 <= zero) { bary[0] = one; bary[1] = zero; bary[2] = zero; *region = 1; return; }
+    if (d3 >= zero && d6 <= d5) { bary[0] = zero; bary[1] = one; bary[2] = zero; *region = 2; return; }
+    T vc = d1 * d4 - d3 * d2;
+    if (vc <= zero && d1 >= zero && d3 <= zero) {
+        T v = d1 / (d1 - d3);
+        bary[0] = one - v; bary[1] = v; bary[2] = zero; *region = 4; return;
+    }
+    if (d6 >= zero && d5 <= d6) { bary[0] = zero; bary[1] = zero; bary[2] = one; *region = 3; return; }
+    T vb = d5 * d2 - d1 * d6;
+    if (vb <= zero && d2 >= zero && d6 <= zero) {
+        T w = d2 / (d2 - d6);
+        bary[0] = one - w; bary[1] = zero; bary[2] = w; *region = 6; return;
+    }
+    T va = d3 * d6 - d5 * d4;
+    if (va <= zero && (d4 - d3) >= zero && (d5 - d6) >= zero) {
+        T w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+        bary[0] = zero; bary[1] = one - w; bary[2] = w; *region = 5; return;
+    }
+    T den = one / (va + vb + vc);
+    T v = vb * den, w = vc * den;
+    bary[0] = one - v - w; bary[1] = v; bary[2] = w; *region = 0;
+}
+
+template <typename T>
+MPM_HD T tri_dist2(const MeshTri& t, const T p[3], T bary[3], int* region) {
+    T a[3], b[3], c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { a[k] = t.a[k]; b[k] = t.b[k]; c[k] = t.c[k]; }
+    closest_on_triangle(p, a, b, c, bary, region);
+    T d2 = T(0);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        T e = bary[0] * a[k] + bary[1] * b[k] + bary[2] * c[k] - p[k];
+        d2 += e * e;
+    }
+    return d2;
+}
+
+struct MeshHit {
+    int tri;    // index into the leaf-ordered triangle array, -1 when the mesh is empty
+    float sign;
+    float cp[3];  // closest point, local space
+};
+
+MPM_HD float box_dist2(const BvhNode& nd, const float p[3]) {
+    float d = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float e = fmaxf(fmaxf(nd.lo[a] - p[a], p[a] - nd.hi[a]), 0.f);
+        d += e * e;
+    }
+    return d;
+}
+
+// Closest triangle by FP32 distance. Candidates whose distance is within `tol` (absolute, local units) of
+// the best so far are compared again in FP64, ties going to the lower face index: near the mesh's medial
+// axis two faces can be equidistant to FP32 rounding, and the FP64 comparison picks the same face as an
+// exact query would.
+MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris, const float p[3],
+                            float tol) {
+    MeshHit hit;
+    hit.tri = -1;
+    hit.sign = 1.f;
+    float best = 3.0e38f, lo2 = 3.0e38f, hi2 = 3.0e38f;
+    double best_d = -1.0;  // FP64 distance^2 of the best, once needed
+    const double pd[3] = {p[0], p[1], p[2]};
+    int best_region = 0;
+    float best_bary[3] = {0.f, 0.f, 0.f};
+    int stack[64];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const BvhNode nd = nodes[stack[--sp]];
+        if (box_dist2(nd, p) > hi2) continue;
+        if (nd.count > 0) {
+            for (int i = nd.start; i < nd.start + nd.count; ++i) {
+                const MeshTri& t = tris[i];
+                float bary[3];
+                int region;
+                float d2 = tri_dist2<float>(t, p, bary, &region);
+                if (d2 > hi2) continue;
+                bool take = hit.tri < 0 || d2 < lo2;
+                if (!take) {  // within tol of the best: decide in FP64
+                    double bd[3];
+                    int rd;
+                    if (best_d < 0.0) best_d = tri_dist2<double>(tris[hit.tri], pd, bd, &rd);
+                    double cd = tri_dist2<double>(t, pd, bd, &rd);
+                    take = cd < best_d || (cd == best_d && t.face < tris[hit.tri].face);
+                    if (take) best_d = cd;
+                } else {
+                    best_d = -1.0;
+                }
+                if (take) {
+                    best = d2;
+                    float r = sqrtf(best);
+                    lo2 = fmaxf(r - tol, 0.f);
+                    lo2 *= lo2;
+                    hi2 = (r + tol) * (r + tol);
+                    best_region = region;
+                    hit.tri = i;
+                    best_bary[0] = bary[0]; best_bary[1] = bary[1]; best_bary[2] = bary[2];
+                }
+            }
+        } else if (sp < 62) {
+            const BvhNode l = nodes[nd.start], r = nodes[nd.start + 1];
+            float dl = box_dist2(l, p), dr = box_dist2(r, p);
+            if (dl <= dr) { stack[sp++] = nd.start + 1; stack[sp++] = nd.start; }
+            else { stack[sp++] = nd.start; stack[sp++] = nd.start + 1; }
+        }
+    }
+    if (hit.tri < 0) return hit;
+    const MeshTri& t = tris[hit.tri];
+    if (best_d >= 0.0) {  // the winner was settled in FP64: take its region from the FP64 evaluation too
+        double bd[3];
+        tri_dist2<double>(t, pd, bd, &best_region);
+        best_bary[0] = (float)bd[0]; best_bary[1] = (float)bd[1]; best_bary[2] = (float)bd[2];
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) hit.cp[k] = best_bary[0] * t.a[k] + best_bary[1] * t.b[k] + best_bary[2] * t.c[k];
+    const float* pn = best_region == 0 ? t.fn : (best_region <= 3 ? t.vn[best_region - 1] : t.en[best_region - 4]);
+    float s = (p[0] - hit.cp[0]) * pn[0] + (p[1] - hit.cp[1]) * pn[1] + (p[2] - hit.cp[2]) * pn[2];
+    hit.sign = s >= 0.f ? 1.f : -1.f;
+    return hit;
+}
+
+// Absolute distance tolerance of the FP32 comparison at point p: a few FP32 ulps of the coordinates involved.
+MPM_HD float query_tol(const ColliderDev& c, const float p[3]) {
+    float m = fmaxf(fmaxf(fabsf(p[0]), fabsf(p[1])), fabsf(p[2]));
+    return 1.0e-6f * (m + c.mesh_scale);
+}
+
+// colliders.py:40-65 -> (outward normal, phi); phi = 1e30 when outside the margin box or behind an open mesh
+MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes,
+                                             const MeshTri* __restrict__ tris, const float p[3], float thickness,
+                                             float n[3], float* phi) {
+    n[0] = 0.f; n[1] = 0.f; n[2] = 1.f;
+    *phi = 1.0e30f;
+    if (c.n_tris == 0) return;
+    float pl[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) pl[r] = c.Minv[r][0] * p[0] + c.Minv[r][1] * p[1] + c.Minv[r][2] * p[2] + c.Minv[r][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+        if (pl[a] < c.aabb_lo[a] - c.margin || pl[a] > c.aabb_hi[a] + c.margin) return;
+    MeshHit h = mesh_closest(nodes + c.node_offset, tris + c.tri_offset, pl, query_tol(c, pl));
+    if (h.tri < 0) return;
+    float off[3] = {pl[0] - h.cp[0], pl[1] - h.cp[1], pl[2] - h.cp[2]};
+    float d[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) d[r] = c.M[r][0] * off[0] + c.M[r][1] * off[1] + c.M[r][2] * off[2];
+    float dist = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    if (dist > 1.0e-9f) {
+        float k = h.sign / dist;
+        n[0] = d[0] * k; n[1] = d[1] * k; n[2] = d[2] * k;
+    } else {  // on the surface: the face normal mapped by the inverse transpose
+        const float* fn = tris[c.tri_offset + h.tri].fn;
+        float tn[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) tn[r] = c.Minv[0][r] * fn[0] + c.Minv[1][r] * fn[1] + c.Minv[2][r] * fn[2];
+        float l = sqrtf(tn[0] * tn[0] + tn[1] * tn[1] + tn[2] * tn[2]);
+        float k = l > 0.f ? 1.f / l : 0.f;
+        n[0] = tn[0] * k; n[1] = tn[1] * k; n[2] = tn[2] * k;
+    }
+    if (!c.closed && h.sign < 0.f && dist > thickness) return;
+    *phi = h.sign * dist;
+}
+
+// colliders.py:68-74: velocity of the collider material point at p (central difference of the pose in s)
+MPM_HD void collider_velocity(const ColliderDev& c, const float p[3], float out[3]) {
+    float pl[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) pl[r] = c.Minv[r][0] * p[0] + c.Minv[r][1] * p[1] + c.Minv[r][2] * p[2] + c.Minv[r][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) out[r] = c.dM[r][0] * pl[0] + c.dM[r][1] * pl[1] + c.dM[r][2] * pl[2] + c.dM[r][3];
+}
+
+}  // namespace mpm

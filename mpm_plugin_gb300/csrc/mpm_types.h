@@ -1,0 +1,87 @@
+// Plain structs shared by the host library and the kernels. FP32 device-side copies of the host's float64
+// constants (the reference computes them in float64 and converts at launch, warp/solver.py:37-71).
+#pragma once
+
+#include <cstdint>
+
+namespace mpm {
+
+constexpr int kBlock = 4;       // grid block edge (nodes); a block is 64 nodes x 16 B = 1 KiB contiguous
+constexpr int kPad = 3;         // padding cells around the domain, warp/solver.py:18
+constexpr int kMaxMaterials = 64;
+
+// Grid: dense padded node box, stored as 4x4x4 blocks; each node is float4 {momentum|velocity xyz, mass}.
+struct GridDesc {
+    int dims[3];   // padded node counts, warp/solver.py:40
+    int nb[3];     // blocks per axis (dims rounded up to kBlock)
+    float origin[3];
+    float dx, inv_dx, p_vol;
+    float gravity[3];
+    int wall_lo_node[3], wall_hi_node[3], lo_on[3], hi_on[3];
+    float wall_friction;
+    float wall_lo[3], wall_hi[3], clamp_lo[3], clamp_hi[3];
+    float thickness, band;  // open-collider thickness 2 dx and contact band dx
+};
+
+__host__ __device__ inline int64_t node_index(const GridDesc& g, int i, int j, int k) {
+    int64_t b = ((int64_t)(i >> 2) * g.nb[1] + (j >> 2)) * g.nb[2] + (k >> 2);
+    return b * 64 + (((i & 3) * 4 + (j & 3)) * 4 + (k & 3));
+}
+
+struct Material {
+    int model;  // 0 elastic, 1 von Mises, 2 Drucker-Prager, 3 snow (kernels.py:8-13)
+    float mu, lam, yield_stress, alpha, hardening, max_hardening;
+    float clamp_lo, clamp_hi;  // snow: 1 - critical_compression, 1 + critical_stretch
+    float p_mass;              // density * p_vol in FP32 (warp/solver.py:91)
+};
+
+// Particle state, structure of arrays; every component is its own array of `cap` entries.
+struct Particles {
+    float* x[3];
+    float* v[3];
+    float* C[9];  // row-major APIC affine matrix
+    float* F[9];  // row-major deformation gradient
+    float* Jp;
+    int32_t* mat;
+    int32_t* emitter;
+    int32_t* id;  // insertion rank: the reference's particle order, restored on every download
+    int64_t n, cap;
+};
+
+struct BvhNode {  // 32 B; internal: children at start, start+1 (count == 0); leaf: count triangles at start
+    float lo[3];
+    int start;
+    float hi[3];
+    int count;
+};
+
+struct MeshTri {  // 128 B, leaf order
+    float a[3], b[3], c[3];
+    int face;       // index in the collider's own triangle list (tie-break of equal distances)
+    float fn[3];    // unit face normal
+    float en[3][3]; // edge pseudonormals ab, bc, ca
+    float vn[3][3]; // vertex pseudonormals a, b, c
+    float pad[1];
+};
+
+// Per collider: static data plus the pose of the current substep (written on the device each substep).
+struct ColliderDev {
+    float M[3][4], Minv[3][4], dM[3][4];
+    float aabb_lo[3], aabb_hi[3];
+    float margin, friction;
+    float mesh_scale;  // largest |coordinate| of the mesh's local bounding box
+    int closed;
+    int node_offset, tri_offset, n_tris;
+    // pose pair of the current advance: translation, quaternion (x, y, z, w), symmetric stretch
+    float t0[3], t1[3], q0[4], q1[4], S0[9], S1[9];
+};
+
+// Values a substep reads from device memory (so one captured substep graph serves every substep).
+struct StepParams {
+    float dt;
+    float s;            // fraction of the advance at the end of this substep, (k + 1) / steps
+    float inv_frame_dt; // 1 / duration of the current advance call
+    int k, steps;
+};
+
+}  // namespace mpm

@@ -214,12 +214,19 @@ static inline REAL bspline_w(REAL fx, int i) {
     return (REAL)0.5 * (fx - (REAL)0.5) * (fx - (REAL)0.5);
 }
 
-static void stencil(const OrcDomain *d, const REAL *xp_world, int base[3], REAL fx[3]) {
+/* Returns 0 when the stencil would leave the padded grid (also for NaN / inf positions); such a particle
+ * neither scatters nor gathers. The reference never meets this on valid input (positions are clamped). */
+static int stencil(const OrcDomain *d, const REAL *xp_world, int base[3], REAL fx[3]) {
+    int ok = 1;
     for (int a = 0; a < 3; ++a) {
         REAL xp = (xp_world[a] - (REAL)d->origin[a]) * (REAL)d->inv_dx;
-        base[a] = (int)RFLOOR(xp - (REAL)0.5);
-        fx[a] = xp - (REAL)base[a];
+        REAL b = RFLOOR(xp - (REAL)0.5);
+        int in = b >= (REAL)0 && b <= (REAL)(d->dims[a] - 3);
+        ok &= in;
+        base[a] = in ? (int)b : 0;
+        fx[a] = xp - b;
     }
+    return ok;
 }
 
 /* ---- p2g: kernels.py:92-140 ---- */
@@ -245,7 +252,7 @@ void orc_p2g(const OrcDomain *d, const OrcMaterial *mats, int n, const REAL *x, 
         for (int i = 0; i < 9; ++i) affine[i] = k_stress * tau[i] + pm * C[9 * p + i];
         int base[3];
         REAL fx[3], w0[3] = {0}, w1[3] = {0}, w2[3] = {0}, mv[3];
-        stencil(d, &x[3 * p], base, fx);
+        if (!stencil(d, &x[3 * p], base, fx)) continue;
         for (int a = 0; a < 3; ++a) mv[a] = pm * v[3 * p + a];
         for (int i = 0; i < 3; ++i) { w0[i] = bspline_w(fx[0], i); w1[i] = bspline_w(fx[1], i); w2[i] = bspline_w(fx[2], i); }
         for (int i = 0; i < 3; ++i)
@@ -313,10 +320,10 @@ void orc_g2p(const OrcDomain *d, const OrcMaterial *mats, int n, REAL *x, REAL *
     for (int p = 0; p < n; ++p) {
         int base[3];
         REAL fx[3], w0[3] = {0}, w1[3] = {0}, w2[3] = {0};
-        stencil(d, &x[3 * p], base, fx);
+        int inside = stencil(d, &x[3 * p], base, fx);
         for (int i = 0; i < 3; ++i) { w0[i] = bspline_w(fx[0], i); w1[i] = bspline_w(fx[1], i); w2[i] = bspline_w(fx[2], i); }
         REAL nv[3] = {0, 0, 0}, nC[9] = {0};
-        for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 3 * inside; ++i)
             for (int j = 0; j < 3; ++j)
                 for (int k = 0; k < 3; ++k) {
                     REAL w = w0[i] * w1[j] * w2[k];
@@ -379,7 +386,7 @@ void orc_scatter_volume(const OrcDomain *d, int n, const REAL *x, REAL *grid_vol
     for (int p = 0; p < n; ++p) {
         int base[3];
         REAL fx[3];
-        stencil(d, &x[3 * p], base, fx);
+        if (!stencil(d, &x[3 * p], base, fx)) continue;
         for (int i = 0; i < 3; ++i) {
             REAL wi = bspline_w(fx[0], i);
             for (int j = 0; j < 3; ++j) {
@@ -738,6 +745,17 @@ static void collider_velocity(const OrcCollider *c, const REAL *Minv, REAL s, co
     REAL k = inv_frame_dt / ((REAL)2.0 * h);
     for (int i = 0; i < 16; ++i) dM[i] = (Mp[i] - Mm[i]) * k;
     xform_point(dM, pl, out);
+}
+
+void orc_collider_pose(const OrcCollider *c, REAL s, REAL inv_frame_dt, REAL *M16, REAL *Minv16, REAL *dM16) {
+    REAL Mp[16], Mm[16];
+    collider_matrix(c, s, M16);
+    inverse44(M16, Minv16);
+    const REAL h = (REAL)1.0e-3;
+    collider_matrix(c, s + h, Mp);
+    collider_matrix(c, s - h, Mm);
+    REAL k = inv_frame_dt / ((REAL)2.0 * h);
+    for (int i = 0; i < 16; ++i) dM16[i] = (Mp[i] - Mm[i]) * k;
 }
 
 void orc_grid_colliders(const OrcDomain *d, int n_col, const OrcCollider *cols, REAL s, REAL inv_frame_dt,

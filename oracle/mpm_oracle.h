@@ -74,6 +74,8 @@ void orc_project_particles(const OrcDomain *d, int n_col, const OrcCollider *col
 void orc_substep(const OrcDomain *d, const OrcMaterial *mats, int n_col, const OrcCollider *cols, int n, REAL *x,
                  REAL *v, REAL *C, REAL *F, REAL *Jp, const int32_t *mat, REAL dt, REAL s, REAL inv_frame_dt,
                  REAL *grid, int threads);
+/* Collider pose at s as 4x4 row-major matrices: M, its inverse, and the central-difference dM/dt. */
+void orc_collider_pose(const OrcCollider *c, REAL s, REAL inv_frame_dt, REAL *M16, REAL *Minv16, REAL *dM16);
 REAL orc_max_speed(int n, const REAL *v);
 void orc_scatter_volume(const OrcDomain *d, int n, const REAL *x, REAL *grid_vol);
 void orc_query_fill(const OrcDomain *d, int m, const REAL *pts, const REAL *grid_vol, uint8_t *out);

@@ -67,6 +67,7 @@ def lib(precision: str = "f32") -> C.CDLL:
         L.orc_substep.argtypes = [P, P, C.c_int, P, C.c_int, P, P, P, P, P, P, R, R, R, P, C.c_int]
         L.orc_p2g.argtypes = [P, P, C.c_int, P, P, P, P, P, P, R, P, C.c_int]
         L.orc_grid_update.argtypes = [P, R, P, C.c_int]
+        L.orc_collider_pose.argtypes = [P, R, R, P, P, P]
         L.orc_max_speed.restype = R
         L.orc_max_speed.argtypes = [C.c_int, P]
         L.orc_scatter_volume.argtypes = [P, C.c_int, P, P]
@@ -315,6 +316,12 @@ class OracleSolver:
             s = self.save_state()
             self._set({k: v[~out] for k, v in s.items()})
         return removed
+
+    def collider_pose(self, c: int, s: float):
+        """(M, M^-1, dM/dt) of collider c at substep fraction s, each 3x4 (colliders.py:30-37, 68-74)."""
+        out = [np.zeros((4, 4), self.real) for _ in range(3)]
+        self.lib.orc_collider_pose(C.byref(self.cols[c]), s, 1.0 / self.frame_dt, *(_ptr(a) for a in out))
+        return tuple(a[:3] for a in out)
 
     def is_occupied(self, points) -> np.ndarray:
         pts = np.ascontiguousarray(np.asarray(points, self.real).reshape(-1, 3))

@@ -1,0 +1,85 @@
+"""The backend's device math built for the host (CPU only): SVD accuracy, stress accuracy, mesh queries."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+from device_math import HostMesh, stress, svd
+from scenes import icosphere, plane_mesh, unit_cube_mesh
+
+from oracle.oracle import OracleMesh
+
+
+def _rand_F(n, scale, seed):
+    rng = np.random.default_rng(seed)
+    return (np.eye(3) + scale * rng.normal(size=(n, 3, 3))).astype(np.float32)
+
+
+@pytest.mark.parametrize("scale", [1e-4, 1e-2, 0.3])
+def test_svd_convention_and_accuracy(scale):
+    F = _rand_F(20000, scale, 1)
+    U, s, d, V, fp64 = svd(F)
+    F64 = F.astype(np.float64)
+    rec = np.einsum("nij,nj,nkj->nik", U.astype(np.float64), s.astype(np.float64), V.astype(np.float64))
+    assert np.abs(rec - F64).max() < 4e-6
+    assert np.allclose(np.linalg.det(U), 1, atol=1e-5) and np.allclose(np.linalg.det(V), 1, atol=1e-5)
+    assert (s[:, 0] >= s[:, 1] - 1e-6).all() and (s[:, 1] >= np.abs(s[:, 2]) - 1e-6).all()
+    assert (np.sign(s[:, 2]) == np.sign(np.linalg.det(F64))).all()
+    # d = sigma - 1 keeps its relative accuracy for small strains
+    s_exact = np.linalg.svd(F64, compute_uv=False)
+    s_exact[:, 2] *= np.sign(np.linalg.det(F64))
+    err = np.abs(d.astype(np.float64) - (s_exact - 1.0))
+    assert (err <= 1e-6 * np.abs(s_exact - 1.0) + 1e-7 * scale).mean() > 0.99
+    assert fp64 <= 0.01 * len(F)
+
+
+def test_svd_inverted_and_degenerate():
+    F = np.array([np.eye(3), np.diag([1.1, 0.95, -0.9]), np.diag([1.2, 1.2, 0.9]), np.diag([1e-6, 1.0, 1.0]),
+                  [[0, 1, 0], [1, 0, 0], [0, 0, 1]], np.zeros((3, 3))], np.float32)
+    U, s, d, V, _ = svd(F)
+    rec = np.einsum("nij,nj,nkj->nik", U, s, V)
+    assert np.abs(rec - F).max() < 1e-5
+    assert s[1, 2] < 0 and s[4, 2] < 0  # det < 0: the last singular value carries the sign
+
+
+@pytest.mark.parametrize("model", [0, 1])
+def test_stress_small_strain_accuracy(model):
+    """Kirchhoff stress at strains of 1e-4 agrees with the float64 formula to 1e-5 relative."""
+    F = _rand_F(5000, 1e-4, 2)
+    mu, lam = 2e4, 3e4
+    tau = stress(F, model, mu, lam).astype(np.float64)
+    F64 = F.astype(np.float64)
+    U, s, Vt = np.linalg.svd(F64)
+    flip = np.linalg.det(U @ Vt) < 0
+    U[flip, :, 2] *= -1
+    s[flip, 2] *= -1
+    if model == 0:
+        R = U @ Vt
+        J = np.prod(s, axis=1)
+        ref = 2 * mu * (F64 - R) @ np.transpose(F64, (0, 2, 1)) + (lam * J * (J - 1))[:, None, None] * np.eye(3)
+    else:
+        e = np.log(np.maximum(s, 1e-4))
+        g = 2 * mu * e + lam * e.sum(1, keepdims=True)
+        ref = np.einsum("nij,nj,nkj->nik", U, g, U)
+    rel = np.linalg.norm(tau - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))
+    assert np.median(rel) < 1e-5 and rel.max() < 1e-3
+
+
+@pytest.mark.parametrize("mesh", ["sphere", "cube", "plane"])
+def test_mesh_query_matches_oracle(mesh):
+    if mesh == "sphere":
+        v, t = icosphere(1.0, 2)
+    elif mesh == "cube":
+        v, t = unit_cube_mesh(centered=True)
+    else:
+        v, t = plane_mesh(0.8)
+    hm, om = HostMesh(v, t), OracleMesh(v, t)
+    rng = np.random.default_rng(3)
+    pts = [rng.normal(size=(4000, 3)) * 0.7]
+    pts.append(np.concatenate([v * r for r in (0.3, 0.9, 1.02)]) + rng.normal(0, 1e-6, (3 * len(v), 3)))
+    pts = np.concatenate(pts).astype(np.float32)
+    cp, sg, fc = hm.query(pts)
+    for i, p in enumerate(pts):
+        f, s, _, _, d2 = om.query(p.astype(np.float64))
+        assert fc[i] == f and sg[i] == s, (i, p)
+        assert abs(np.linalg.norm(cp[i].astype(np.float64) - p) - np.sqrt(d2)) < 1e-5
