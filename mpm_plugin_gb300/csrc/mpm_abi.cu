@@ -15,14 +15,14 @@
 
 #include "../../include/mpm_gb300.h"
 #include "mpm_bvh.h"
+#include "mpm_host.h"
 #include "mpm_internal.h"
 
 using namespace mpm;
 
 namespace {
 
-constexpr double kCFL = 0.4;                // warp/solver.py:19
-constexpr double kColliderThickness = 2.0;  // warp/solver.py:20
+constexpr double kCFL = 0.4;  // warp/solver.py:19
 constexpr int kFields = 28;                 // x3 v3 C9 F9 Jp mat emitter id
 
 thread_local std::string g_last_error;
@@ -36,6 +36,7 @@ struct Handle {
     int device = 0;
     cudaStream_t stream = nullptr;
     MpmDomainDesc dom{};
+    HostDomain hd{};
     double dx = 0, inv_dx = 0, p_vol = 0;
     double origin[3] = {0, 0, 0};
     int dims[3] = {0, 0, 0};
@@ -186,91 +187,6 @@ Status ensure_stage(Handle* h, size_t bytes) {
     }
     h->stage_bytes = b;
     return {};
-}
-
-// ---- host pose math (mpm_core/geometry.py:30-50, warp/solver.py:154-172) ----------------------------
-
-void svd3_host(const double A[9], double U[9], double s[3], double V[9]) {  // one-sided Jacobi, float64
-    double B[9];
-    std::memcpy(B, A, sizeof B);
-    for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
-    const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-    for (int sweep = 0; sweep < 60; ++sweep) {
-        bool rotated = false;
-        for (auto& r : pq) {
-            int p = r[0], q = r[1];
-            double al = 0, be = 0, ga = 0;
-            for (int i = 0; i < 3; ++i) {
-                al += B[i * 3 + p] * B[i * 3 + p];
-                be += B[i * 3 + q] * B[i * 3 + q];
-                ga += B[i * 3 + p] * B[i * 3 + q];
-            }
-            if (ga == 0.0 || std::fabs(ga) <= 1e-17 * std::sqrt(al * be)) continue;
-            rotated = true;
-            double zeta = (be - al) / (2.0 * ga);
-            double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
-            double c = 1.0 / std::sqrt(1.0 + t * t), sn = c * t;
-            for (int i = 0; i < 3; ++i) {
-                double bp = B[i * 3 + p], bq = B[i * 3 + q];
-                B[i * 3 + p] = c * bp - sn * bq;
-                B[i * 3 + q] = sn * bp + c * bq;
-                double vp = V[i * 3 + p], vq = V[i * 3 + q];
-                V[i * 3 + p] = c * vp - sn * vq;
-                V[i * 3 + q] = sn * vp + c * vq;
-            }
-        }
-        if (!rotated) break;
-    }
-    double n[3];
-    for (int k = 0; k < 3; ++k) n[k] = std::sqrt(B[k] * B[k] + B[3 + k] * B[3 + k] + B[6 + k] * B[6 + k]);
-    int ord[3] = {0, 1, 2};
-    std::sort(ord, ord + 3, [&](int a, int b) { return n[a] > n[b]; });
-    double B2[9], V2[9];
-    for (int k = 0; k < 3; ++k) {
-        s[k] = n[ord[k]];
-        for (int i = 0; i < 3; ++i) {
-            B2[i * 3 + k] = B[i * 3 + ord[k]];
-            V2[i * 3 + k] = V[i * 3 + ord[k]];
-        }
-    }
-    std::memcpy(V, V2, sizeof V2);
-    for (int k = 0; k < 3; ++k)
-        for (int i = 0; i < 3; ++i) U[i * 3 + k] = s[k] > 0 ? B2[i * 3 + k] / s[k] : (i == k ? 1.0 : 0.0);
-}
-
-double det3(const double m[9]) {
-    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
-}
-
-// World matrix -> translation, rotation quaternion (x, y, z, w), symmetric stretch; M = [R S | t].
-void decompose(const float* m16, double t[3], double q[4], double S[9], double* min_sv) {
-    double A[9];
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) A[r * 3 + c] = m16[r * 4 + c];
-    for (int r = 0; r < 3; ++r) t[r] = m16[r * 4 + 3];
-    double U[9], s[3], V[9];
-    svd3_host(A, U, s, V);
-    *min_sv = s[2];
-    double R[9];
-    auto make_R = [&]() {
-        for (int r = 0; r < 3; ++r)
-            for (int c = 0; c < 3; ++c) R[r * 3 + c] = U[r * 3] * V[c * 3] + U[r * 3 + 1] * V[c * 3 + 1] + U[r * 3 + 2] * V[c * 3 + 2];
-    };
-    make_R();
-    if (det3(R) < 0) {  // mirrored: R stays a proper rotation, the flip goes into S
-        for (int r = 0; r < 3; ++r) U[r * 3 + 2] = -U[r * 3 + 2];
-        s[2] = -s[2];
-        make_R();
-    }
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 3; ++c) S[r * 3 + c] = V[r * 3] * s[0] * V[c * 3] + V[r * 3 + 1] * s[1] * V[c * 3 + 1] + V[r * 3 + 2] * s[2] * V[c * 3 + 2];
-    // quaternion: magnitudes from the diagonal, signs from the antisymmetric part (mpm_core/geometry.py:42-50)
-    double w = std::sqrt(std::max(0.0, 1 + R[0] + R[4] + R[8])) / 2;
-    double x = std::copysign(std::sqrt(std::max(0.0, 1 + R[0] - R[4] - R[8])) / 2, R[7] - R[5]);
-    double y = std::copysign(std::sqrt(std::max(0.0, 1 - R[0] + R[4] - R[8])) / 2, R[2] - R[6]);
-    double z = std::copysign(std::sqrt(std::max(0.0, 1 - R[0] - R[4] + R[8])) / 2, R[3] - R[1]);
-    double nq = std::sqrt(x * x + y * y + z * z + w * w);
-    q[0] = x / nq; q[1] = y / nq; q[2] = z / nq; q[3] = w / nq;
 }
 
 // ---- substep sequence ---------------------------------------------------------------------------------
@@ -540,61 +456,22 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     h->dom = *dom;
     h->ppc = ppc;
-    // domain constants (mpm_core/scene.py:60-67; warp/solver.py:37-53), float64
-    double size[3], longest = 0;
+    h->g = make_grid(*dom, gravity, ppc, &h->hd);
+    h->dx = h->hd.dx;
+    h->inv_dx = h->hd.inv_dx;
+    h->p_vol = h->hd.p_vol;
     for (int a = 0; a < 3; ++a) {
-        size[a] = dom->max[a] - dom->min[a];
-        longest = std::max(longest, size[a]);
+        h->origin[a] = h->hd.origin[a];
+        h->dims[a] = h->hd.dims[a];
     }
-    h->dx = longest / dom->resolution;
-    h->inv_dx = 1.0 / h->dx;
-    h->p_vol = std::pow(h->dx, 3.0) / ppc;
     GridDesc& g = h->g;
-    for (int a = 0; a < 3; ++a) {
-        int shape = std::max(1, (int)std::ceil(size[a] / h->dx - 1e-6));
-        h->dims[a] = shape + 2 * kPad;
-        h->origin[a] = dom->min[a] - kPad * h->dx;
-        g.dims[a] = h->dims[a];
-        g.nb[a] = (h->dims[a] + kBlock - 1) / kBlock;
-        g.origin[a] = (float)h->origin[a];
-        g.gravity[a] = (float)gravity[a];
-        g.lo_on[a] = dom->wall_lo[a] ? 1 : 0;
-        g.hi_on[a] = dom->wall_hi[a] ? 1 : 0;
-        g.wall_lo[a] = (float)dom->min[a];
-        g.wall_hi[a] = (float)dom->max[a];
-        g.clamp_lo[a] = (float)(h->origin[a] + h->dx);
-        g.clamp_hi[a] = (float)(h->origin[a] + (h->dims[a] - 2) * h->dx);
-        g.wall_lo_node[a] = (int)std::floor((dom->min[a] - h->origin[a]) / h->dx + 1e-3);
-        g.wall_hi_node[a] = (int)std::ceil((dom->max[a] - h->origin[a]) / h->dx - 1e-3);
-    }
-    g.dx = (float)h->dx;
-    g.inv_dx = (float)h->inv_dx;
-    g.p_vol = (float)h->p_vol;
-    g.wall_friction = (float)dom->wall_friction;
-    g.thickness = (float)(kColliderThickness * h->dx);
-    g.band = (float)h->dx;
-    // material tables (warp/solver.py:56-71; mpm_core/materials.py:48-51)
     std::vector<Material> table(std::max(1, (int)n_mat));
     h->mat_desc.assign(mats, mats + n_mat);
     h->mat_count.assign(n_mat, 0);
     for (int m = 0; m < n_mat; ++m) {
-        const MpmMaterialDesc& d = mats[m];
-        double e = d.youngs_modulus, nu = d.poisson_ratio;
-        double mu = e / (2 * (1 + nu)), lam = e * nu / ((1 + nu) * (1 - 2 * nu));
-        double sphi = std::sin(d.friction_angle_deg * (M_PI / 180.0));
-        double alpha = std::sqrt(2.0 / 3.0) * 2 * sphi / (3 - sphi);
-        Material& t = table[m];
-        t.model = d.model;
-        t.mu = (float)mu;
-        t.lam = (float)lam;
-        t.yield_stress = (float)d.yield_stress;
-        t.alpha = (float)alpha;
-        t.hardening = (float)d.hardening;
-        t.max_hardening = (float)d.max_hardening;
-        t.clamp_lo = 1.0f - (float)d.critical_compression;
-        t.clamp_hi = 1.0f + (float)d.critical_stretch;
-        t.p_mass = (float)d.density * (float)h->p_vol;
-        h->wave.push_back(std::sqrt((lam + 2 * mu) * (d.model == MPM_MODEL_SNOW ? d.max_hardening : 1.0) / d.density));
+        double wave;
+        table[m] = make_material(mats[m], h->p_vol, &wave);
+        h->wave.push_back(wave);
     }
     CK(cudaMalloc(&h->d_mats, sizeof(Material) * table.size()));
     CK(cudaMemcpy(h->d_mats, table.data(), sizeof(Material) * table.size(), cudaMemcpyHostToDevice));
@@ -641,20 +518,7 @@ Status set_transforms(Handle* h, int32_t n, const float* start16, const float* e
     if (n != h->n_col) return {MPM_ERR_VALUE, "expected " + std::to_string(h->n_col) + " collider transforms"};
     if (n == 0) return {};
     if (!start16 || !end16) return {MPM_ERR_ARGUMENT, "null transform array"};
-    for (int c = 0; c < n; ++c) {
-        double t0[3], q0[4], S0[9], t1[3], q1[4], S1[9], sv0, sv1;
-        decompose(start16 + 16 * c, t0, q0, S0, &sv0);
-        decompose(end16 + 16 * c, t1, q1, S1, &sv1);
-        if (q0[0] * q1[0] + q0[1] * q1[1] + q0[2] * q1[2] + q0[3] * q1[3] < 0)
-            for (double& v : q1) v = -v;  // slerp the short way round
-        ColliderDev& col = h->cols[c];
-        for (int k = 0; k < 3; ++k) { col.t0[k] = (float)t0[k]; col.t1[k] = (float)t1[k]; }
-        for (int k = 0; k < 4; ++k) { col.q0[k] = (float)q0[k]; col.q1[k] = (float)q1[k]; }
-        for (int k = 0; k < 9; ++k) { col.S0[k] = (float)S0[k]; col.S1[k] = (float)S1[k]; }
-        // AABB early-out margin: three cells in local units under the strongest shrink of either pose
-        double inv_scale = std::max(1.0 / std::max(sv0, 1e-12), 1.0 / std::max(sv1, 1e-12));
-        col.margin = (float)(3.0 * h->dx * inv_scale);
-    }
+    for (int c = 0; c < n; ++c) collider_set_pose(h->cols[c], start16 + 16 * c, end16 + 16 * c, h->dx);
     CK(cudaMemcpyAsync(h->d_cols, h->cols.data(), sizeof(ColliderDev) * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return {};
@@ -675,21 +539,7 @@ Status set_colliders(Handle* h, int32_t n, const MpmColliderDesc* cs) {
             return {MPM_ERR_VALUE, "bad collider mesh"};
         for (int i = 0; i < 3 * d.n_tris; ++i)
             if (d.tris[i] < 0 || d.tris[i] >= d.n_verts) return {MPM_ERR_VALUE, "collider triangle index out of range"};
-        ColliderDev& col = h->cols[c];
-        col.closed = d.closed ? 1 : 0;
-        col.friction = (float)d.friction;
-        col.node_offset = (int)all_nodes.size();
-        col.tri_offset = (int)all_tris.size();
-        col.n_tris = d.n_tris;
-        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-        for (int i = 0; i < d.n_verts; ++i)
-            for (int a = 0; a < 3; ++a) {
-                lo[a] = std::min(lo[a], d.verts[3 * i + a]);
-                hi[a] = std::max(hi[a], d.verts[3 * i + a]);
-            }
-        for (int a = 0; a < 3; ++a) { col.aabb_lo[a] = lo[a]; col.aabb_hi[a] = hi[a]; }
-        col.mesh_scale = 0.0f;
-        for (int a = 0; a < 3 && d.n_verts > 0; ++a) col.mesh_scale = std::max({col.mesh_scale, std::fabs(lo[a]), std::fabs(hi[a])});
+        collider_static(h->cols[c], d, (int)all_nodes.size(), (int)all_tris.size());
         std::vector<BvhNode> nodes;
         std::vector<MeshTri> tris;
         build_mesh(MeshInput{d.n_verts, d.n_tris, d.verts, d.tris}, nodes, tris);

@@ -14,6 +14,33 @@
 
 namespace mpm {
 
+#ifndef __CUDA_ARCH__
+using std::isfinite;
+#endif
+
+// Arithmetic with every operation rounded on its own (no fused multiply-add), for the few values whose
+// last bits decide a discrete choice (the collider pose, a grid node's position, the local query point,
+// FP64 distances that break near-ties between mesh faces): these follow the reference's operation order.
+#ifdef __CUDA_ARCH__
+MPM_HD float fadd(float a, float b) { return __fadd_rn(a, b); }
+MPM_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
+MPM_HD float fmul(float a, float b) { return __fmul_rn(a, b); }
+MPM_HD float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+MPM_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
+MPM_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
+MPM_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
+MPM_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+#else  // host: a volatile store keeps the compiler from fusing the operation into a multiply-add
+MPM_HD float fadd(float a, float b) { volatile float r = a + b; return r; }
+MPM_HD float fsub(float a, float b) { volatile float r = a - b; return r; }
+MPM_HD float fmul(float a, float b) { volatile float r = a * b; return r; }
+MPM_HD float fdiv(float a, float b) { volatile float r = a / b; return r; }
+MPM_HD double dadd(double a, double b) { volatile double r = a + b; return r; }
+MPM_HD double dsub(double a, double b) { volatile double r = a - b; return r; }
+MPM_HD double dmul(double a, double b) { volatile double r = a * b; return r; }
+MPM_HD double ddiv(double a, double b) { volatile double r = a / b; return r; }
+#endif
+
 // ---------------------------------------------------------------------------------------------------------
 // 3x3 SVD with the convention of Warp's svd3 (called at kernels.py:35,57,252): U and V proper rotations,
 // singular values in decreasing order, the sign of det(A) carried by the last one.
@@ -353,19 +380,60 @@ MPM_HD void closest_on_triangle(const T p[3], const T a[3], const T b[3], const 
     bary[0] = one - v - w; bary[1] = v; bary[2] = w; *region = 0;
 }
 
-template <typename T>
-MPM_HD T tri_dist2(const MeshTri& t, const T p[3], T bary[3], int* region) {
-    T a[3], b[3], c[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { a[k] = t.a[k]; b[k] = t.b[k]; c[k] = t.c[k]; }
-    closest_on_triangle(p, a, b, c, bary, region);
-    T d2 = T(0);
+MPM_HD float tri_dist2(const MeshTri& t, const float p[3], float bary[3], int* region) {
+    closest_on_triangle<float>(p, t.a, t.b, t.c, bary, region);
+    float d2 = 0.f;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-        T e = bary[0] * a[k] + bary[1] * b[k] + bary[2] * c[k] - p[k];
+        float e = bary[0] * t.a[k] + bary[1] * t.b[k] + bary[2] * t.c[k] - p[k];
         d2 += e * e;
     }
     return d2;
+}
+
+// FP64 distance^2 to a triangle with each operation rounded on its own, in the order of the closest-point
+// routine above, so near-ties between faces are decided the same way on every machine.
+MPM_HD double tri_dist2_exact(const MeshTri& t, const double p[3], double bary[3], int* region) {
+    double a[3], b[3], c[3], ab[3], ac[3], ap[3], bp[3], cp[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        a[k] = t.a[k]; b[k] = t.b[k]; c[k] = t.c[k];
+        ab[k] = dsub(b[k], a[k]); ac[k] = dsub(c[k], a[k]);
+        ap[k] = dsub(p[k], a[k]); bp[k] = dsub(p[k], b[k]); cp[k] = dsub(p[k], c[k]);
+    }
+    auto dot = [](const double* u, const double* v) { return dadd(dadd(dmul(u[0], v[0]), dmul(u[1], v[1])), dmul(u[2], v[2])); };
+    double d1 = dot(ab, ap), d2 = dot(ac, ap), d3 = dot(ab, bp), d4 = dot(ac, bp), d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d1 <= 0 && d2 <= 0) { bary[0] = 1; bary[1] = 0; bary[2] = 0; *region = 1; }
+    else if (d3 >= 0 && d6 <= d5) { bary[0] = 0; bary[1] = 1; bary[2] = 0; *region = 2; }
+    else {
+        double vc = dsub(dmul(d1, d4), dmul(d3, d2));
+        double vb = dsub(dmul(d5, d2), dmul(d1, d6));
+        double va = dsub(dmul(d3, d6), dmul(d5, d4));
+        if (vc <= 0 && d1 >= 0 && d3 <= 0) {
+            double v = ddiv(d1, dsub(d1, d3));
+            bary[0] = dsub(1.0, v); bary[1] = v; bary[2] = 0; *region = 4;
+        } else if (d6 >= 0 && d5 <= d6) {
+            bary[0] = 0; bary[1] = 0; bary[2] = 1; *region = 3;
+        } else if (vb <= 0 && d2 >= 0 && d6 <= 0) {
+            double w = ddiv(d2, dsub(d2, d6));
+            bary[0] = dsub(1.0, w); bary[1] = 0; bary[2] = w; *region = 6;
+        } else if (va <= 0 && dsub(d4, d3) >= 0 && dsub(d5, d6) >= 0) {
+            double w = ddiv(dsub(d4, d3), dadd(dsub(d4, d3), dsub(d5, d6)));
+            bary[0] = 0; bary[1] = dsub(1.0, w); bary[2] = w; *region = 5;
+        } else {
+            double den = ddiv(1.0, dadd(dadd(va, vb), vc));
+            double v = dmul(vb, den), w = dmul(vc, den);
+            bary[0] = dsub(dsub(1.0, v), w); bary[1] = v; bary[2] = w; *region = 0;
+        }
+    }
+    double dd = 0.0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        double q = dadd(dadd(dmul(bary[0], a[k]), dmul(bary[1], b[k])), dmul(bary[2], c[k]));
+        double e = dsub(q, p[k]);
+        dd = dadd(dd, dmul(e, e));
+    }
+    return dd;
 }
 
 struct MeshHit {
@@ -396,8 +464,8 @@ MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __
     float best = 3.0e38f, lo2 = 3.0e38f, hi2 = 3.0e38f;
     double best_d = -1.0;  // FP64 distance^2 of the best, once needed
     const double pd[3] = {p[0], p[1], p[2]};
-    int best_region = 0;
-    float best_bary[3] = {0.f, 0.f, 0.f};
+    int best_region = 0, best_face = 0x7fffffff;
+    float best_bary[3] = {0.f, 0.f, 0.f}, best_cp[3] = {0.f, 0.f, 0.f};
     int stack[64];
     int sp = 0;
     stack[sp++] = 0;
@@ -409,18 +477,29 @@ MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __
                 const MeshTri& t = tris[i];
                 float bary[3];
                 int region;
-                float d2 = tri_dist2<float>(t, p, bary, &region);
+                float d2 = tri_dist2(t, p, bary, &region);
                 if (d2 > hi2) continue;
-                bool take = hit.tri < 0 || d2 < lo2;
-                if (!take) {  // within tol of the best: decide in FP64
-                    double bd[3];
-                    int rd;
-                    if (best_d < 0.0) best_d = tri_dist2<double>(tris[hit.tri], pd, bd, &rd);
-                    double cd = tri_dist2<double>(t, pd, bd, &rd);
-                    take = cd < best_d || (cd == best_d && t.face < tris[hit.tri].face);
-                    if (take) best_d = cd;
-                } else {
+                float cp[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) cp[k] = bary[0] * t.a[k] + bary[1] * t.b[k] + bary[2] * t.c[k];
+                bool take;
+                if (hit.tri < 0 || d2 < lo2) {
+                    take = true;
                     best_d = -1.0;
+                } else {
+                    float sep = (cp[0] - best_cp[0]) * (cp[0] - best_cp[0]) + (cp[1] - best_cp[1]) * (cp[1] - best_cp[1]) +
+                                (cp[2] - best_cp[2]) * (cp[2] - best_cp[2]);
+                    if (sep <= tol * tol) {  // the same closest point (a shared edge or vertex): any face will do
+                        take = t.face < best_face;
+                        if (take) best_d = -1.0;
+                    } else {  // two different closest points within tol of each other: decide in FP64
+                        double bd[3];
+                        int rd;
+                        if (best_d < 0.0) best_d = tri_dist2_exact(tris[hit.tri], pd, bd, &rd);
+                        double cd = tri_dist2_exact(t, pd, bd, &rd);
+                        take = cd < best_d || (cd == best_d && t.face < best_face);
+                        if (take) best_d = cd;
+                    }
                 }
                 if (take) {
                     best = d2;
@@ -429,8 +508,10 @@ MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __
                     lo2 *= lo2;
                     hi2 = (r + tol) * (r + tol);
                     best_region = region;
+                    best_face = t.face;
                     hit.tri = i;
-                    best_bary[0] = bary[0]; best_bary[1] = bary[1]; best_bary[2] = bary[2];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) { best_bary[k] = bary[k]; best_cp[k] = cp[k]; }
                 }
             }
         } else if (sp < 62) {
@@ -444,7 +525,7 @@ MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __
     const MeshTri& t = tris[hit.tri];
     if (best_d >= 0.0) {  // the winner was settled in FP64: take its region from the FP64 evaluation too
         double bd[3];
-        tri_dist2<double>(t, pd, bd, &best_region);
+        tri_dist2_exact(t, pd, bd, &best_region);
         best_bary[0] = (float)bd[0]; best_bary[1] = (float)bd[1]; best_bary[2] = (float)bd[2];
     }
 #pragma unroll
@@ -461,6 +542,13 @@ MPM_HD float query_tol(const ColliderDev& c, const float p[3]) {
     return 1.0e-6f * (m + c.mesh_scale);
 }
 
+// World point -> collider local space, M^-1 p, rounded like the reference's transform_point.
+MPM_HD void to_local(const ColliderDev& c, const float p[3], float pl[3]) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+        pl[r] = fadd(fadd(fadd(fmul(c.Minv[r][0], p[0]), fmul(c.Minv[r][1], p[1])), fmul(c.Minv[r][2], p[2])), c.Minv[r][3]);
+}
+
 // colliders.py:40-65 -> (outward normal, phi); phi = 1e30 when outside the margin box or behind an open mesh
 MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes,
                                              const MeshTri* __restrict__ tris, const float p[3], float thickness,
@@ -469,8 +557,7 @@ MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes
     *phi = 1.0e30f;
     if (c.n_tris == 0) return;
     float pl[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) pl[r] = c.Minv[r][0] * p[0] + c.Minv[r][1] * p[1] + c.Minv[r][2] * p[2] + c.Minv[r][3];
+    to_local(c, p, pl);
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         if (pl[a] < c.aabb_lo[a] - c.margin || pl[a] > c.aabb_hi[a] + c.margin) return;
@@ -500,8 +587,7 @@ MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes
 // colliders.py:68-74: velocity of the collider material point at p (central difference of the pose in s)
 MPM_HD void collider_velocity(const ColliderDev& c, const float p[3], float out[3]) {
     float pl[3];
-#pragma unroll
-    for (int r = 0; r < 3; ++r) pl[r] = c.Minv[r][0] * p[0] + c.Minv[r][1] * p[1] + c.Minv[r][2] * p[2] + c.Minv[r][3];
+    to_local(c, p, pl);
 #pragma unroll
     for (int r = 0; r < 3; ++r) out[r] = c.dM[r][0] * pl[0] + c.dM[r][1] * pl[1] + c.dM[r][2] * pl[2] + c.dM[r][3];
 }

@@ -67,3 +67,104 @@ void mesh_query(void* mh, int n, const float* pts, float* cp, float* sign, int32
 }
 
 }  // extern "C"
+
+// ---- the whole substep of the CUDA backend, run on the host with the same per-item functions ----------
+#include "../../mpm_plugin_gb300/csrc/mpm_host.h"
+#include "../../mpm_plugin_gb300/csrc/mpm_substep.cuh"
+
+struct Emu {
+    GridDesc g;
+    HostDomain hd;
+    std::vector<Material> mats;
+    std::vector<float4> grid;
+    std::vector<ColliderDev> cols;
+    std::vector<BvhNode> nodes;
+    std::vector<MeshTri> tris;
+    unsigned int fp64 = 0;
+};
+
+extern "C" {
+
+void* emu_create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int n_mat, const double* gravity, int ppc) {
+    Emu* e = new Emu();
+    e->g = make_grid(*dom, gravity, ppc, &e->hd);
+    for (int m = 0; m < n_mat; ++m) {
+        double wave;
+        e->mats.push_back(make_material(mats[m], e->hd.p_vol, &wave));
+    }
+    e->grid.assign((size_t)e->g.nb[0] * e->g.nb[1] * e->g.nb[2] * 64, float4{0, 0, 0, 0});
+    return e;
+}
+
+void emu_destroy(void* e) { delete static_cast<Emu*>(e); }
+
+void emu_set_colliders(void* ev, int n, const MpmColliderDesc* cs) {
+    Emu* e = static_cast<Emu*>(ev);
+    e->cols.assign(n, ColliderDev{});
+    e->nodes.clear();
+    e->tris.clear();
+    for (int c = 0; c < n; ++c) {
+        collider_static(e->cols[c], cs[c], (int)e->nodes.size(), (int)e->tris.size());
+        std::vector<BvhNode> nd;
+        std::vector<MeshTri> tr;
+        build_mesh(MeshInput{cs[c].n_verts, cs[c].n_tris, cs[c].verts, cs[c].tris}, nd, tr);
+        e->nodes.insert(e->nodes.end(), nd.begin(), nd.end());
+        e->tris.insert(e->tris.end(), tr.begin(), tr.end());
+    }
+}
+
+void emu_set_transforms(void* ev, int n, const float* s16, const float* e16) {
+    Emu* e = static_cast<Emu*>(ev);
+    for (int c = 0; c < n; ++c) collider_set_pose(e->cols[c], s16 + 16 * c, e16 + 16 * c, e->hd.dx);
+}
+
+void emu_grid_dims(void* ev, int* dims) {
+    Emu* e = static_cast<Emu*>(ev);
+    for (int a = 0; a < 3; ++a) dims[a] = e->g.dims[a];
+}
+
+// x, v: (3, n) planar; C, F: (9, n) planar row-major components; Jp, mat: (n)
+unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, float* F, float* Jp, int32_t* mat,
+                         double dt, double s, double frame_dt) {
+    Emu* e = static_cast<Emu*>(ev);
+    Particles P{};
+    for (int a = 0; a < 3; ++a) { P.x[a] = x + a * n; P.v[a] = v + a * n; }
+    for (int k = 0; k < 9; ++k) { P.C[k] = C + k * n; P.F[k] = F + k * n; }
+    P.Jp = Jp;
+    P.mat = mat;
+    P.n = n;
+    P.cap = n;
+    const float dtf = (float)dt;
+    for (auto& c : e->cols) collider_pose_at(c, (float)s, (float)(1.0 / frame_dt));
+    std::fill(e->grid.begin(), e->grid.end(), float4{0, 0, 0, 0});
+    const ColliderDev* cols = e->cols.empty() ? nullptr : e->cols.data();
+    const int n_col = (int)e->cols.size();
+    for (int64_t p = 0; p < n; ++p) p2g_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data(), &e->fp64);
+    const int64_t nblk = (int64_t)e->g.nb[0] * e->g.nb[1] * e->g.nb[2];
+    for (int64_t blk = 0; blk < nblk; ++blk) {
+        const int bk = (int)(blk % e->g.nb[2]), bj = (int)((blk / e->g.nb[2]) % e->g.nb[1]);
+        const int bi = (int)(blk / ((int64_t)e->g.nb[2] * e->g.nb[1]));
+        for (int l = 0; l < 64; ++l) {
+            const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+            grid_update_node(e->g, &e->grid[blk * 64 + l], idx, dtf, cols, n_col, e->nodes.data(), e->tris.data());
+        }
+    }
+    for (int64_t p = 0; p < n; ++p)
+        g2p_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data(), cols, n_col, e->nodes.data(), e->tris.data(),
+                     &e->fp64);
+    return e->fp64;
+}
+
+void emu_read_grid(void* ev, float* out) {
+    Emu* e = static_cast<Emu*>(ev);
+    const GridDesc& g = e->g;
+    int64_t q = 0;
+    for (int i = 0; i < g.dims[0]; ++i)
+        for (int j = 0; j < g.dims[1]; ++j)
+            for (int k = 0; k < g.dims[2]; ++k, ++q) {
+                float4 v = e->grid[node_index(g, i, j, k)];
+                out[4 * q] = v.x; out[4 * q + 1] = v.y; out[4 * q + 2] = v.z; out[4 * q + 3] = v.w;
+            }
+}
+
+}  // extern "C"

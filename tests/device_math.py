@@ -11,8 +11,9 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent.parent
 SRC = ROOT / "tests" / "csrc" / "device_math_host.cpp"
-DEPS = [SRC, ROOT / "mpm_plugin_gb300" / "csrc" / "mpm_device.cuh", ROOT / "mpm_plugin_gb300" / "csrc" / "mpm_bvh.h",
-        ROOT / "mpm_plugin_gb300" / "csrc" / "mpm_types.h"]
+CSRC = ROOT / "mpm_plugin_gb300" / "csrc"
+DEPS = [SRC, *(CSRC / f for f in ("mpm_device.cuh", "mpm_bvh.h", "mpm_types.h", "mpm_host.h", "mpm_substep.cuh")),
+        ROOT / "include" / "mpm_gb300.h"]
 OUT = ROOT / "tests" / "_build" / "libdevice_math_host.so"
 _lib = None
 
@@ -28,8 +29,8 @@ def lib():
     if not OUT.exists() or OUT.stat().st_mtime < max(p.stat().st_mtime for p in DEPS):
         OUT.parent.mkdir(exist_ok=True)
         tmp = OUT.with_suffix(f".{os.getpid()}.tmp")
-        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", _cuda_include(), "-o", str(tmp),
-                        str(SRC)], check=True)
+        subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", _cuda_include(),
+                        "-o", str(tmp), str(SRC)], check=True)
         os.replace(tmp, OUT)
     L = C.CDLL(str(OUT))
     P = C.c_void_p
@@ -40,6 +41,15 @@ def lib():
     L.mesh_build.restype = P
     L.mesh_free.argtypes = [P]
     L.mesh_query.argtypes = [P, C.c_int, P, P, P, P]
+    L.emu_create.argtypes = [P, P, C.c_int, P, C.c_int]
+    L.emu_create.restype = P
+    L.emu_destroy.argtypes = [P]
+    L.emu_set_colliders.argtypes = [P, C.c_int, P]
+    L.emu_set_transforms.argtypes = [P, C.c_int, P, P]
+    L.emu_grid_dims.argtypes = [P, P]
+    L.emu_substep.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_double, C.c_double, C.c_double]
+    L.emu_substep.restype = C.c_uint
+    L.emu_read_grid.argtypes = [P, P]
     _lib = L
     return L
 
@@ -80,5 +90,81 @@ class HostMesh:
     def __del__(self):
         try:
             lib().mesh_free(self.h)
+        except Exception:
+            pass
+
+
+class SubstepEmulator:
+    """The CUDA backend's substep (mpm_substep.cuh) run on the CPU, one item after another."""
+
+    def __init__(self, domain, materials, gravity=(0.0, 0.0, -9.81), ppc=8):
+        from mpm_plugin_gb300 import _abi
+
+        d = _abi.MpmDomainDesc()
+        for a, ax in enumerate("xyz"):
+            d.min[a], d.max[a] = domain.min[a], domain.max[a]
+            d.wall_lo[a] = int(bool(domain.walls[f"{ax}-"]))
+            d.wall_hi[a] = int(bool(domain.walls[f"{ax}+"]))
+        d.resolution, d.wall_friction = domain.resolution, domain.wall_friction
+        mats = (_abi.MpmMaterialDesc * len(materials))()
+        for i, m in enumerate(materials):
+            mats[i] = _abi.MpmMaterialDesc(_abi.MODEL_IDS[m.model], m.youngs_modulus, m.poisson_ratio, m.density,
+                                           m.yield_stress, m.friction_angle_deg, m.hardening, m.critical_compression,
+                                           m.critical_stretch, m.max_hardening)
+        g = (C.c_double * 3)(*gravity)
+        self._abi = _abi
+        self.h = lib().emu_create(C.byref(d), mats, len(materials), g, ppc)
+        self.state = None
+
+    def set_colliders(self, colliders):
+        """colliders: [(verts, tris, closed, friction), ...]"""
+        self._keep = []
+        descs = (self._abi.MpmColliderDesc * max(1, len(colliders)))()
+        for i, (v, t, closed, fr) in enumerate(colliders):
+            v = np.ascontiguousarray(np.asarray(v, np.float32).reshape(-1, 3))
+            t = np.ascontiguousarray(np.asarray(t, np.int32).reshape(-1, 3))
+            self._keep += [v, t]
+            descs[i] = self._abi.MpmColliderDesc(len(v), len(t), v.ctypes.data, t.ctypes.data, int(closed), fr)
+        lib().emu_set_colliders(self.h, len(colliders), descs)
+        self.n_col = len(colliders)
+        eye = np.tile(np.eye(4, dtype=np.float32), (self.n_col, 1, 1))
+        self.set_collider_transforms(eye, eye)
+
+    def set_collider_transforms(self, start, end):
+        self._xf = [np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1, 4, 4)) for a in (start, end)]
+        lib().emu_set_transforms(self.h, self.n_col, _p(self._xf[0]), _p(self._xf[1]))
+
+    def load_state(self, s):
+        n = len(s["x"])
+        self.state = {"x": np.ascontiguousarray(np.asarray(s["x"], np.float32).reshape(n, 3).T),
+                      "v": np.ascontiguousarray(np.asarray(s["v"], np.float32).reshape(n, 3).T),
+                      "C": np.ascontiguousarray(np.asarray(s["C"], np.float32).reshape(n, 9).T),
+                      "F": np.ascontiguousarray(np.asarray(s["F"], np.float32).reshape(n, 9).T),
+                      "Jp": np.ascontiguousarray(np.asarray(s["Jp"], np.float32).reshape(n)),
+                      "mat": np.ascontiguousarray(np.asarray(s["mat"], np.int32).reshape(n)),
+                      "emitter": np.asarray(s["emitter"], np.int32).copy()}
+
+    def save_state(self):
+        s = self.state
+        n = len(s["Jp"])
+        return {"x": s["x"].T.copy(), "v": s["v"].T.copy(), "C": s["C"].T.reshape(n, 3, 3).copy(),
+                "F": s["F"].T.reshape(n, 3, 3).copy(), "Jp": s["Jp"].copy(), "mat": s["mat"].copy(),
+                "emitter": s["emitter"].copy()}
+
+    def substep(self, dt, s=1.0, frame_dt=1.0):
+        st = self.state
+        return lib().emu_substep(self.h, len(st["Jp"]), _p(st["x"]), _p(st["v"]), _p(st["C"]), _p(st["F"]),
+                                 _p(st["Jp"]), _p(st["mat"]), dt, s, frame_dt)
+
+    def read_grid(self):
+        dims = np.zeros(3, np.int32)
+        lib().emu_grid_dims(self.h, _p(dims))
+        out = np.zeros((*dims, 4), np.float32)
+        lib().emu_read_grid(self.h, _p(out))
+        return out
+
+    def __del__(self):
+        try:
+            lib().emu_destroy(self.h)
         except Exception:
             pass
