@@ -239,7 +239,7 @@ def run_gpu(args, world, rank, local):
     solver.set_option(_abi.OPT_KERNEL_TIMING, 0)
 
     # end to end through the solver API: one bake frame per step, host buffers
-    e2e_frames, frame_ms, substeps = max(2, min(args.steps, 6)), [], 0
+    e2e_frames, frame_ms, substeps = max(2, args.e2e_frames), [], 0
     h2d = 2 * 64  # the collider's start and end world matrices
     d2h = n * (12 + 12 + 4 + 4) + n * (12 + 12 + 36 + 36 + 4 + 4 + 4)  # get_particles + save_state
     solver.advance(FRAME_DT)  # warm the CFL path and the graph
@@ -312,6 +312,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--e2e-frames", type=int, default=4, help="24 fps frames timed through the solver API")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
