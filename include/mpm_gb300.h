@@ -138,6 +138,20 @@ int mpm_launch_count(void *handle, int64_t *launches);
 /* Number of SVD lanes that took the FP64 path since the handle was created. */
 int mpm_fp64_lanes(void *handle, int64_t *lanes);
 
+/* Occupancy query that allocates no device memory. It has no counterpart in the reference: it is for callers
+ * that cannot allocate device memory when they ask, such as a serving process whose device memory budget
+ * was handed out at start-up, or a host application whose own allocator owns the device (cudaFree would
+ * also synchronise the device). Same answer as mpm_is_occupied for particles at d_x: d_x (n,3), d_points (m,3)
+ * and d_out (m) are caller-owned device arrays; the work is queued on `stream` (NULL: the legacy default
+ * stream) and d_out is valid once that stream has reached it. Its volume grid lives in a static 16 MiB
+ * device array (4,194,304 grid nodes) that every GPU which loads this library keeps until the process exits;
+ * a domain whose padded grid needs more nodes is refused with MPM_ERR_VALUE. All calls share that array,
+ * so calls whose work overlaps on the GPU race. The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture. Errors: mpm_last_error(NULL). */
+int mpm_is_occupied_noalloc(const MpmDomainDesc *domain, int32_t particles_per_cell, int64_t n, const float *d_x,
+                            int64_t m, const float *d_points, uint8_t *d_out, int32_t device, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

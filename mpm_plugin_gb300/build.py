@@ -2,7 +2,7 @@
 
     python -m mpm_plugin_gb300.build [--force]
 
-Two translation units compiled in parallel with nvcc, then linked into one shared library with the CUDA
+Three translation units compiled in parallel with nvcc, then linked into one shared library with the CUDA
 runtime linked statically. No cmake, no torch extension machinery.
 """
 
@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = BUILD / "libmpm_gb300.so"
-SOURCES = ["mpm_kernels.cu", "mpm_abi.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_abi.cu", "mpm_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

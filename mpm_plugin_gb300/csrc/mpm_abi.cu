@@ -563,6 +563,8 @@ Status set_colliders(Handle* h, int32_t n, const MpmColliderDesc* cs) {
 
 }  // namespace
 
+void mpm::set_last_error(const std::string& msg) { g_last_error = msg; }
+
 // ============================================================================================================
 // C-ABI
 // ============================================================================================================

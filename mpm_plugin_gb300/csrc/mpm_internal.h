@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <string>
 
 #include "mpm_types.h"
 
@@ -13,6 +14,9 @@ struct EscapeBounds {  // particles past these planes on open sides are removed 
     int open_lo[3], open_hi[3];
     float lo[3], hi[3];
 };
+
+// Records the message mpm_last_error(NULL) returns on this thread.
+void set_last_error(const std::string& msg);
 
 void launch_step_begin(cudaStream_t st, StepParams* sp, ColliderDev* cols, int n_col);
 void launch_p2g(cudaStream_t st, const Particles& P, const Material* mats, const GridDesc& g, const StepParams* sp,
