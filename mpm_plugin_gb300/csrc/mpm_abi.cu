@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstddef>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -61,8 +62,14 @@ struct Handle {
 
     int n_col = 0;
     std::vector<ColliderDev> cols;
-    std::vector<std::vector<float>> col_verts;
     ColliderDev* d_cols = nullptr;
+    ColliderPose* d_poses = nullptr;  // poses of every substep of the current advance
+    int64_t pose_cap = 0;
+    WorkLists wl{};                   // active blocks and collider candidates, sized for the grid / particles
+    int64_t part_cand_cap = 0;
+    int2* d_sdf_cells = nullptr;      // narrow-band voxel grids of all colliders
+    int32_t* d_sdf_cand = nullptr;
+    bool sdf_dirty = true;
     BvhNode* d_nodes = nullptr;
     MeshTri* d_tris = nullptr;
     double frame_dt = 1.0;
@@ -80,7 +87,7 @@ struct Handle {
 
     bool use_graph = true;
     cudaGraphExec_t graph = nullptr;
-    int64_t graph_key[4] = {-1, -1, -1, -1};
+    int64_t graph_key[6] = {-1, -1, -1, -1, -1, -1};
 
     bool timing = false;
     std::vector<cudaEvent_t> ev_pool;
@@ -211,45 +218,69 @@ cudaEvent_t take_event(Handle* h) {
     return e;
 }
 
-constexpr int kSubstepKernels = 4;  // step_begin, p2g, grid_update, g2p
+SubstepArgs substep_args(Handle* h) {
+    SubstepArgs a{};
+    a.P = h->P;
+    a.mats = h->d_mats;
+    a.g = h->g;
+    a.sp = h->d_sp;
+    a.grid = h->grid;
+    a.fp64 = h->d_counters + 1;
+    a.wl = h->wl;
+    a.cd.cols = h->d_cols;
+    a.cd.poses = h->d_poses;
+    a.cd.n_col = h->n_col;
+    a.cd.nodes = h->d_nodes;
+    a.cd.tris = h->d_tris;
+    a.cd.cells = h->d_sdf_cells;
+    a.cd.cand = h->d_sdf_cand;
+    return a;
+}
 
-Status enqueue_substep(Handle* h, std::vector<cudaEvent_t>* ev) {
-    cudaStream_t st = h->stream;
-    launch_step_begin(st, h->d_sp, h->d_cols, h->n_col);
-    CK(cudaMemsetAsync(h->grid, 0, (size_t)h->grid_nodes * sizeof(float4), st));
-    if (ev) CK(cudaEventRecord((*ev)[0], st));
-    launch_p2g(st, h->P, h->d_mats, h->g, h->d_sp, h->grid, h->d_counters + 1);
-    if (ev) CK(cudaEventRecord((*ev)[1], st));
-    launch_grid_update(st, h->g, h->grid, h->d_sp, h->d_cols, h->n_col, h->d_nodes, h->d_tris);
-    if (ev) CK(cudaEventRecord((*ev)[2], st));
-    launch_g2p(st, h->P, h->d_mats, h->g, h->d_sp, h->grid, h->d_cols, h->n_col, h->d_nodes, h->d_tris,
-               h->d_counters + 1);
-    if (ev) CK(cudaEventRecord((*ev)[3], st));
-    CK(cudaGetLastError());
+Status ensure_part_cand(Handle* h) {
+    if (h->part_cand_cap >= h->P.cap) return {};
+    CK(cudaStreamSynchronize(h->stream));
+    if (h->wl.part_cand) cudaFree(h->wl.part_cand);
+    h->wl.part_cand = nullptr;
+    if (cudaMalloc(&h->wl.part_cand, sizeof(int32_t) * (size_t)h->P.cap) != cudaSuccess) {
+        cudaGetLastError();
+        h->part_cand_cap = 0;
+        return {MPM_ERR_MEMORY, "device allocation of the collider candidate list failed"};
+    }
+    h->part_cand_cap = h->P.cap;
+    invalidate_graph(h);
     return {};
 }
 
 Status run_substep(Handle* h) {
+    TRY(ensure_part_cand(h));
+    SubstepArgs a = substep_args(h);
+    const int kernels = substep_kernel_count(a);
     if (h->timing) {
-        std::vector<cudaEvent_t> ev(4);
+        std::vector<cudaEvent_t> ev(5);
         for (auto& e : ev) e = take_event(h);
-        TRY(enqueue_substep(h, &ev));
+        launch_substep(h->stream, a, ev.data());
+        CK(cudaGetLastError());
         h->ev_pending.push_back(ev);
-        h->launches += kSubstepKernels;
+        h->launches += kernels;
         return {};
     }
     if (!h->use_graph) {
-        h->launches += kSubstepKernels;
-        return enqueue_substep(h, nullptr);
+        launch_substep(h->stream, a, nullptr);
+        CK(cudaGetLastError());
+        h->launches += kernels;
+        return {};
     }
-    int64_t key[4] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena};
+    int64_t key[6] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena, (int64_t)(intptr_t)h->d_poses,
+                      (int64_t)(intptr_t)h->wl.part_cand};
     if (!h->graph || std::memcmp(key, h->graph_key, sizeof key) != 0) {
         invalidate_graph(h);
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        Status s = enqueue_substep(h, nullptr);
+        launch_substep(h->stream, a, nullptr);
+        cudaError_t e0 = cudaGetLastError();
         cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
-        if (s.code != MPM_OK) return s;
+        CK(e0);
         CK(e);
         e = cudaGraphInstantiate(&h->graph, graph, 0);
         cudaGraphDestroy(graph);
@@ -257,7 +288,98 @@ Status run_substep(Handle* h) {
         std::memcpy(h->graph_key, key, sizeof key);
     }
     CK(cudaGraphLaunch(h->graph, h->stream));
-    h->launches += kSubstepKernels;
+    h->launches += kernels;
+    return {};
+}
+
+// (Re)builds the colliders' narrow-band voxel grids when a mesh or the scale of its pose changed enough.
+Status ensure_sdf(Handle* h) {
+    if (!h->sdf_dirty || h->n_col == 0) return {};
+    CK(cudaStreamSynchronize(h->stream));
+    int64_t total = 0;
+    std::vector<int64_t> nvox(h->n_col);
+    for (int c = 0; c < h->n_col; ++c) {
+        ColliderDev& col = h->cols[c];
+        sdf_grid_params(col, total);
+        nvox[c] = (int64_t)col.sdf.dims[0] * col.sdf.dims[1] * col.sdf.dims[2];
+        total += col.n_tris > 0 ? nvox[c] : 0;
+    }
+    if (h->d_sdf_cells) cudaFree(h->d_sdf_cells);
+    if (h->d_sdf_cand) cudaFree(h->d_sdf_cand);
+    h->d_sdf_cells = nullptr;
+    h->d_sdf_cand = nullptr;
+    invalidate_graph(h);
+    if (total == 0) {
+        h->sdf_dirty = false;
+        return {};
+    }
+    int32_t *counts = nullptr, *starts = nullptr, *tmp = nullptr;
+    const int64_t tiles = scan_tile_count(total) + 2;
+    bool ok = cudaMalloc(&h->d_sdf_cells, sizeof(int2) * (size_t)total) == cudaSuccess &&
+              cudaMalloc(&counts, sizeof(int32_t) * (size_t)total) == cudaSuccess &&
+              cudaMalloc(&starts, sizeof(int32_t) * (size_t)total) == cudaSuccess &&
+              cudaMalloc(&tmp, sizeof(int32_t) * (size_t)(tiles + 1)) == cudaSuccess;
+    auto release = [&]() { cudaFree(counts); cudaFree(starts); cudaFree(tmp); };
+    if (!ok) {
+        cudaGetLastError();
+        release();
+        return {MPM_ERR_MEMORY, "device allocation of the collider voxel grids failed"};
+    }
+    for (int c = 0; c < h->n_col; ++c) {
+        const ColliderDev& col = h->cols[c];
+        if (col.n_tris == 0) continue;
+        launch_sdf_classify(h->stream, col, h->d_nodes + col.node_offset, h->d_tris + col.tri_offset, nvox[c],
+                            kSdfMaxCandidates, h->d_sdf_cells + col.sdf.cell_offset, counts + col.sdf.cell_offset);
+        h->launches += 1;
+    }
+    launch_exclusive_scan(h->stream, counts, total, starts, tmp, tmp + tiles);
+    h->launches += 3;
+    int32_t n_cand = 0;
+    cudaError_t e = cudaMemcpyAsync(&n_cand, tmp + tiles, sizeof n_cand, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess && cudaMalloc(&h->d_sdf_cand, sizeof(int32_t) * (size_t)std::max(n_cand, 1)) != cudaSuccess)
+        e = cudaErrorMemoryAllocation;
+    if (e == cudaSuccess) {
+        for (int c = 0; c < h->n_col; ++c) {
+            const ColliderDev& col = h->cols[c];
+            if (col.n_tris == 0) continue;
+            launch_sdf_fill(h->stream, col, h->d_nodes + col.node_offset, h->d_tris + col.tri_offset, nvox[c],
+                            kSdfMaxCandidates, h->d_sdf_cells + col.sdf.cell_offset, starts + col.sdf.cell_offset,
+                            h->d_sdf_cand);
+            h->launches += 1;
+        }
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    }
+    release();
+    if (e != cudaSuccess) return {MPM_ERR_CUDA, std::string("collider voxel grid build: ") + cudaGetErrorString(e)};
+    for (auto& col : h->cols) col.sdf.built = col.n_tris > 0 ? 1 : 0;
+    CK(cudaMemcpyAsync(h->d_cols, h->cols.data(), sizeof(ColliderDev) * h->n_col, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    h->sdf_dirty = false;
+    return {};
+}
+
+// Poses of the colliders for `steps` substeps (steps == 0: one substep ending at s).
+Status prepare_poses(Handle* h, int steps, double s, double frame_dt) {
+    if (h->n_col == 0) return {};
+    int64_t need = (int64_t)std::max(steps, 1) * h->n_col;
+    if (need > h->pose_cap) {
+        CK(cudaStreamSynchronize(h->stream));
+        if (h->d_poses) cudaFree(h->d_poses);
+        h->d_poses = nullptr;
+        int64_t cap = std::max<int64_t>(need, 2 * h->pose_cap);
+        if (cudaMalloc(&h->d_poses, sizeof(ColliderPose) * (size_t)cap) != cudaSuccess) {
+            cudaGetLastError();
+            h->pose_cap = 0;
+            return {MPM_ERR_MEMORY, "device allocation of collider poses failed"};
+        }
+        h->pose_cap = cap;
+        invalidate_graph(h);
+    }
+    launch_collider_poses(h->stream, h->d_cols, h->n_col, h->d_poses, steps, (float)s, (float)(1.0 / frame_dt));
+    CK(cudaGetLastError());
+    h->launches += 1;
     return {};
 }
 
@@ -268,8 +390,9 @@ Status set_step(Handle* h, double dt, double s, double frame_dt, int steps) {
     sp.inv_frame_dt = (float)(1.0 / frame_dt);
     sp.k = -1;
     sp.steps = steps;
-    // a pageable source is staged by the driver before this call returns, so `sp` may go out of scope
-    CK(cudaMemcpyAsync(h->d_sp, &sp, sizeof sp, cudaMemcpyHostToDevice, h->stream));
+    // only the fields before `seq`: the substep counter keeps running across calls. A pageable source is
+    // staged by the driver before this call returns, so `sp` may go out of scope.
+    CK(cudaMemcpyAsync(h->d_sp, &sp, offsetof(StepParams, seq), cudaMemcpyHostToDevice, h->stream));
     return {};
 }
 
@@ -364,6 +487,8 @@ Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
     int steps = (int)std::ceil(frame_dt / dt - 1e-9);
     dt = frame_dt / steps;
     TRY(set_step(h, dt, 0.0, frame_dt, steps));
+    TRY(ensure_sdf(h));
+    TRY(prepare_poses(h, steps, 0.0, frame_dt));
     for (int k = 0; k < steps; ++k) TRY(run_substep(h));
     int32_t removed = 0;
     TRY(remove_escaped(h, &removed));
@@ -483,6 +608,16 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     CK(cudaMemset(h->grid, 0, (size_t)h->grid_nodes * sizeof(float4)));
     CK(cudaMalloc(&h->d_sp, sizeof(StepParams)));
     CK(cudaMemset(h->d_sp, 0, sizeof(StepParams)));
+    {  // work lists: one flag and two list slots per grid block, one candidate slot per grid node
+        const int64_t nblk = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
+        CK(cudaMalloc(&h->wl.block_flag, sizeof(unsigned int) * (size_t)nblk));
+        CK(cudaMemset(h->wl.block_flag, 0, sizeof(unsigned int) * (size_t)nblk));
+        CK(cudaMalloc(&h->wl.blocks[0], sizeof(int32_t) * (size_t)nblk));
+        CK(cudaMalloc(&h->wl.blocks[1], sizeof(int32_t) * (size_t)nblk));
+        CK(cudaMalloc(&h->wl.counts, sizeof(unsigned int) * 4));
+        CK(cudaMemset(h->wl.counts, 0, sizeof(unsigned int) * 4));
+        CK(cudaMalloc(&h->wl.node_cand, sizeof(int32_t) * (size_t)h->grid_nodes));
+    }
     CK(cudaMalloc(&h->d_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
     CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * (2 + kMaxMaterials)));
     CK(cudaMallocHost(&h->h_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
@@ -508,6 +643,15 @@ void destroy(Handle* h) {
     cudaFree(h->d_counters);
     cudaFree(h->d_keep);
     cudaFree(h->d_scan_tmp);
+    cudaFree(h->d_poses);
+    cudaFree(h->d_sdf_cells);
+    cudaFree(h->d_sdf_cand);
+    cudaFree(h->wl.block_flag);
+    cudaFree(h->wl.blocks[0]);
+    cudaFree(h->wl.blocks[1]);
+    cudaFree(h->wl.counts);
+    cudaFree(h->wl.node_cand);
+    cudaFree(h->wl.part_cand);
     cudaFree(h->stage);
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -518,7 +662,11 @@ Status set_transforms(Handle* h, int32_t n, const float* start16, const float* e
     if (n != h->n_col) return {MPM_ERR_VALUE, "expected " + std::to_string(h->n_col) + " collider transforms"};
     if (n == 0) return {};
     if (!start16 || !end16) return {MPM_ERR_ARGUMENT, "null transform array"};
-    for (int c = 0; c < n; ++c) collider_set_pose(h->cols[c], start16 + 16 * c, end16 + 16 * c, h->dx);
+    for (int c = 0; c < n; ++c) {
+        collider_set_pose(h->cols[c], start16 + 16 * c, end16 + 16 * c, h->dx);
+        const SdfGridDev& g = h->cols[c].sdf;
+        if (!g.built || h->cols[c].margin > g.margin || h->cols[c].margin / 3.0f > g.cutoff) h->sdf_dirty = true;
+    }
     CK(cudaMemcpyAsync(h->d_cols, h->cols.data(), sizeof(ColliderDev) * n, cudaMemcpyHostToDevice, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     return {};
@@ -529,6 +677,7 @@ Status set_colliders(Handle* h, int32_t n, const MpmColliderDesc* cs) {
     CK(cudaStreamSynchronize(h->stream));
     free_colliders(h);
     invalidate_graph(h);
+    h->sdf_dirty = true;
     h->cols.assign(n, ColliderDev{});
     h->n_col = n;
     std::vector<BvhNode> all_nodes;
@@ -638,6 +787,8 @@ int mpm_substep(void* handle, double dt, double s, double frame_dt) {
         if (h->P.n == 0) return {};
         h->frame_dt = frame_dt;
         TRY(set_step(h, dt, s, frame_dt, 0));
+        TRY(ensure_sdf(h));
+        TRY(prepare_poses(h, 0, s, frame_dt));
         return run_substep(h);
     };
     return finish(h, run());
@@ -742,12 +893,13 @@ int mpm_kernel_times(void* handle, int32_t n_slots, float* ms, int64_t* launches
     HANDLE_OR_FAIL(handle);
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
-    for (auto& ev : h->ev_pending) {
-        for (int k = 0; k < 3; ++k) {
+    for (auto& ev : h->ev_pending) {  // ev: | clear | P2G | grid update + colliders | G2P + projection |
+        const int slot_of[4] = {3, 0, 1, 2};
+        for (int k = 0; k < 4; ++k) {
             float t = 0;
             cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
-            h->t_ms[k] += t;
-            h->t_launches[k] += 1;
+            h->t_ms[slot_of[k]] += t;
+            h->t_launches[slot_of[k]] += 1;
         }
         for (auto x : ev) h->ev_pool.push_back(x);
     }
@@ -787,12 +939,16 @@ int mpm_read_collider_pose(void* handle, int32_t c, float* M12, float* Minv12, f
     HANDLE_OR_FAIL(handle);
     if (c < 0 || c >= h->n_col) return finish(h, {MPM_ERR_VALUE, "collider index out of range"});
     auto run = [&]() -> Status {
-        ColliderDev col;
-        CK(cudaMemcpyAsync(&col, h->d_cols + c, sizeof col, cudaMemcpyDeviceToHost, h->stream));
+        if (!h->d_poses) return {MPM_ERR_VALUE, "no substep has run since the colliders were set"};
+        StepParams sp;
+        CK(cudaMemcpyAsync(&sp, h->d_sp, sizeof sp, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));
-        if (M12) std::memcpy(M12, col.M, sizeof col.M);
-        if (Minv12) std::memcpy(Minv12, col.Minv, sizeof col.Minv);
-        if (dM12) std::memcpy(dM12, col.dM, sizeof col.dM);
+        ColliderPose pose;
+        CK(cudaMemcpyAsync(&pose, h->d_poses + sp.pose_base + c, sizeof pose, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        if (M12) std::memcpy(M12, pose.M, sizeof pose.M);
+        if (Minv12) std::memcpy(Minv12, pose.Minv, sizeof pose.Minv);
+        if (dM12) std::memcpy(dM12, pose.dM, sizeof pose.dM);
         return {};
     };
     return finish(h, run());

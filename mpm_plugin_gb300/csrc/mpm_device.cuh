@@ -358,7 +358,7 @@ MPM_HD void closest_on_triangle(const T p[3], const T a[3], const T b[3], const 
     T d6 = ac[0] * cp[0] + ac[1] * cp[1] + ac[2] * cp[2];
     const T one(1), zero(0);
     if (d1 <= zero && d2 <= zero) { bary[0] = one; bary[1] = zero; bary[2] = zero; *region = 1; return; }
-    if (d3 >= zero && d6 <= d5) { bary[0] = zero; bary[1] = one; bary[2] = zero; *region = 2; return; }
+    if (d3 >= zero && d4 <= d3) { bary[0] = zero; bary[1] = one; bary[2] = zero; *region = 2; return; }
     T vc = d1 * d4 - d3 * d2;
     if (vc <= zero && d1 >= zero && d3 <= zero) {
         T v = d1 / (d1 - d3);
@@ -404,7 +404,7 @@ MPM_HD double tri_dist2_exact(const MeshTri& t, const double p[3], double bary[3
     auto dot = [](const double* u, const double* v) { return dadd(dadd(dmul(u[0], v[0]), dmul(u[1], v[1])), dmul(u[2], v[2])); };
     double d1 = dot(ab, ap), d2 = dot(ac, ap), d3 = dot(ab, bp), d4 = dot(ac, bp), d5 = dot(ab, cp), d6 = dot(ac, cp);
     if (d1 <= 0 && d2 <= 0) { bary[0] = 1; bary[1] = 0; bary[2] = 0; *region = 1; }
-    else if (d3 >= 0 && d6 <= d5) { bary[0] = 0; bary[1] = 1; bary[2] = 0; *region = 2; }
+    else if (d3 >= 0 && d4 <= d3) { bary[0] = 0; bary[1] = 1; bary[2] = 0; *region = 2; }
     else {
         double vc = dsub(dmul(d1, d4), dmul(d3, d2));
         double vb = dsub(dmul(d5, d2), dmul(d1, d6));
@@ -452,68 +452,102 @@ MPM_HD float box_dist2(const BvhNode& nd, const float p[3]) {
     return d;
 }
 
-// Closest triangle by FP32 distance. Candidates whose distance is within `tol` (absolute, local units) of
-// the best so far are compared again in FP64, ties going to the lower face index: near the mesh's medial
-// axis two faces can be equidistant to FP32 rounding, and the FP64 comparison picks the same face as an
-// exact query would.
+// Running closest-triangle selection. Candidates whose FP32 distance is within `tol` (absolute, local
+// units) of the best so far are compared again: if both give the same closest point (a shared edge or
+// vertex) the result does not depend on the face and the lower face index is kept; otherwise the two are
+// compared in FP64, ties going to the lower face index. Near the mesh's medial axis two faces can be
+// equidistant to FP32 rounding, and the FP64 comparison picks the same face as an exact query would.
+struct ClosestState {
+    float best, lo2, hi2;
+    double best_d;  // FP64 distance^2 of the best, once needed
+    int region, face, tri;
+    float bary[3], cp[3];
+
+    MPM_HD void init() {
+        best = lo2 = hi2 = 3.0e38f;
+        best_d = -1.0;
+        region = 0;
+        face = 0x7fffffff;
+        tri = -1;
+    }
+
+    MPM_HD void consider(const MeshTri* __restrict__ tris, int i, const float p[3], const double pd[3], float tol) {
+        const MeshTri& t = tris[i];
+        float b[3];
+        int rg;
+        float d2 = tri_dist2(t, p, b, &rg);
+        if (d2 > hi2) return;
+        float c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) c[k] = b[0] * t.a[k] + b[1] * t.b[k] + b[2] * t.c[k];
+        bool take;
+        if (tri < 0 || d2 < lo2) {
+            take = true;
+            best_d = -1.0;
+        } else {
+            float sep = (c[0] - cp[0]) * (c[0] - cp[0]) + (c[1] - cp[1]) * (c[1] - cp[1]) + (c[2] - cp[2]) * (c[2] - cp[2]);
+            if (sep <= tol * tol) {
+                take = t.face < face;
+                if (take) best_d = -1.0;
+            } else {
+                double bd[3];
+                int rd;
+                if (best_d < 0.0) best_d = tri_dist2_exact(tris[tri], pd, bd, &rd);
+                double cd = tri_dist2_exact(t, pd, bd, &rd);
+                take = cd < best_d || (cd == best_d && t.face < face);
+                if (take) best_d = cd;
+            }
+        }
+        if (take) {
+            best = d2;
+            float r = sqrtf(best);
+            lo2 = fmaxf(r - tol, 0.f);
+            lo2 *= lo2;
+            hi2 = (r + tol) * (r + tol);
+            region = rg;
+            face = t.face;
+            tri = i;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { bary[k] = b[k]; cp[k] = c[k]; }
+        }
+    }
+
+    MPM_HD MeshHit finish(const MeshTri* __restrict__ tris, const float p[3], const double pd[3]) {
+        MeshHit hit;
+        hit.tri = tri;
+        hit.sign = 1.f;
+        if (tri < 0) return hit;
+        const MeshTri& t = tris[tri];
+        float bb[3] = {bary[0], bary[1], bary[2]};
+        int rg = region;
+        if (best_d >= 0.0) {  // the winner was settled in FP64: take its region from the FP64 evaluation too
+            double bd[3];
+            tri_dist2_exact(t, pd, bd, &rg);
+            bb[0] = (float)bd[0]; bb[1] = (float)bd[1]; bb[2] = (float)bd[2];
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) hit.cp[k] = bb[0] * t.a[k] + bb[1] * t.b[k] + bb[2] * t.c[k];
+        const float* pn = rg == 0 ? t.fn : (rg <= 3 ? t.vn[rg - 1] : t.en[rg - 4]);
+        float s = (p[0] - hit.cp[0]) * pn[0] + (p[1] - hit.cp[1]) * pn[1] + (p[2] - hit.cp[2]) * pn[2];
+        hit.sign = s >= 0.f ? 1.f : -1.f;
+        return hit;
+    }
+};
+
+// Closest triangle through the BVH (nearer child first, subtrees farther than the best pruned).
 MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris, const float p[3],
                             float tol) {
-    MeshHit hit;
-    hit.tri = -1;
-    hit.sign = 1.f;
-    float best = 3.0e38f, lo2 = 3.0e38f, hi2 = 3.0e38f;
-    double best_d = -1.0;  // FP64 distance^2 of the best, once needed
+    ClosestState st;
+    st.init();
     const double pd[3] = {p[0], p[1], p[2]};
-    int best_region = 0, best_face = 0x7fffffff;
-    float best_bary[3] = {0.f, 0.f, 0.f}, best_cp[3] = {0.f, 0.f, 0.f};
     int stack[64];
     int sp = 0;
     stack[sp++] = 0;
     while (sp > 0) {
         const BvhNode nd = nodes[stack[--sp]];
-        if (box_dist2(nd, p) > hi2) continue;
+        if (box_dist2(nd, p) > st.hi2) continue;
         if (nd.count > 0) {
-            for (int i = nd.start; i < nd.start + nd.count; ++i) {
-                const MeshTri& t = tris[i];
-                float bary[3];
-                int region;
-                float d2 = tri_dist2(t, p, bary, &region);
-                if (d2 > hi2) continue;
-                float cp[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) cp[k] = bary[0] * t.a[k] + bary[1] * t.b[k] + bary[2] * t.c[k];
-                bool take;
-                if (hit.tri < 0 || d2 < lo2) {
-                    take = true;
-                    best_d = -1.0;
-                } else {
-                    float sep = (cp[0] - best_cp[0]) * (cp[0] - best_cp[0]) + (cp[1] - best_cp[1]) * (cp[1] - best_cp[1]) +
-                                (cp[2] - best_cp[2]) * (cp[2] - best_cp[2]);
-                    if (sep <= tol * tol) {  // the same closest point (a shared edge or vertex): any face will do
-                        take = t.face < best_face;
-                        if (take) best_d = -1.0;
-                    } else {  // two different closest points within tol of each other: decide in FP64
-                        double bd[3];
-                        int rd;
-                        if (best_d < 0.0) best_d = tri_dist2_exact(tris[hit.tri], pd, bd, &rd);
-                        double cd = tri_dist2_exact(t, pd, bd, &rd);
-                        take = cd < best_d || (cd == best_d && t.face < best_face);
-                        if (take) best_d = cd;
-                    }
-                }
-                if (take) {
-                    best = d2;
-                    float r = sqrtf(best);
-                    lo2 = fmaxf(r - tol, 0.f);
-                    lo2 *= lo2;
-                    hi2 = (r + tol) * (r + tol);
-                    best_region = region;
-                    best_face = t.face;
-                    hit.tri = i;
-#pragma unroll
-                    for (int k = 0; k < 3; ++k) { best_bary[k] = bary[k]; best_cp[k] = cp[k]; }
-                }
-            }
+            for (int i = nd.start; i < nd.start + nd.count; ++i) st.consider(tris, i, p, pd, tol);
         } else if (sp < 62) {
             const BvhNode l = nodes[nd.start], r = nodes[nd.start + 1];
             float dl = box_dist2(l, p), dr = box_dist2(r, p);
@@ -521,19 +555,105 @@ MPM_HD MeshHit mesh_closest(const BvhNode* __restrict__ nodes, const MeshTri* __
             else { stack[sp++] = nd.start; stack[sp++] = nd.start + 1; }
         }
     }
-    if (hit.tri < 0) return hit;
-    const MeshTri& t = tris[hit.tri];
-    if (best_d >= 0.0) {  // the winner was settled in FP64: take its region from the FP64 evaluation too
-        double bd[3];
-        tri_dist2_exact(t, pd, bd, &best_region);
-        best_bary[0] = (float)bd[0]; best_bary[1] = (float)bd[1]; best_bary[2] = (float)bd[2];
+    return st.finish(tris, p, pd);
+}
+
+// Leaf-ordered indices of the triangles within sqrt(R2) of c, in a fixed traversal order. Returns how many
+// there are; writes at most max_out of them to out (out may be null).
+MPM_HD int tris_within(const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris, const float c[3], float R2,
+                       int32_t* out, int max_out) {
+    int count = 0;
+    int stack[64];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp > 0) {
+        const BvhNode nd = nodes[stack[--sp]];
+        if (box_dist2(nd, c) > R2) continue;
+        if (nd.count > 0) {
+            for (int i = nd.start; i < nd.start + nd.count; ++i) {
+                float b[3];
+                int rg;
+                if (tri_dist2(tris[i], c, b, &rg) <= R2) {
+                    if (out && count < max_out) out[count] = i;
+                    ++count;
+                }
+            }
+        } else if (sp < 62) {
+            stack[sp++] = nd.start + 1;
+            stack[sp++] = nd.start;
+        }
     }
+    return count;
+}
+
+// ---------------------------------------------------------------------------------------------------------
+// Narrow-band voxel grid of a collider, in its local space over the bounding box grown by the margin.
+// A voxel is FAR when every point in it is provably outside beyond the contact cutoff (or, for an open mesh,
+// behind it beyond its thickness): collider_sdf's answer there cannot reach the band, so "far" is
+// returned at once. Otherwise the voxel lists every triangle within d_c + 2r of its centre (d_c: the
+// centre's distance to the mesh, r: the voxel's half diagonal), which contains the closest triangle and all
+// ties of any point in the voxel, so the query over the list gives the same answer as over the whole mesh.
+// Voxels whose list would exceed max_cand (deep inside a closed mesh) use the BVH.
+// ---------------------------------------------------------------------------------------------------------
+constexpr int kSdfFar = -1, kSdfUseBvh = -2;
+
+MPM_HD void sdf_voxel_center(const SdfGridDev& s, int64_t v, float c[3], float* r) {
+    const int i = (int)(v / ((int64_t)s.dims[1] * s.dims[2]));
+    const int j = (int)((v / s.dims[2]) % s.dims[1]);
+    const int k = (int)(v % s.dims[2]);
+    c[0] = s.lo[0] + ((float)i + 0.5f) * s.h;
+    c[1] = s.lo[1] + ((float)j + 0.5f) * s.h;
+    c[2] = s.lo[2] + ((float)k + 0.5f) * s.h;
+    *r = 0.8660254f * s.h * 1.0001f;  // half diagonal, rounded up
+}
+
+// Candidate count of voxel v, or kSdfFar / kSdfUseBvh; *R2 gets the candidate radius squared.
+MPM_HD int sdf_voxel_classify(const ColliderDev& col, const BvhNode* __restrict__ nodes,
+                              const MeshTri* __restrict__ tris, int64_t v, int max_cand, float* R2) {
+    const SdfGridDev& s = col.sdf;
+    float c[3], r;
+    sdf_voxel_center(s, v, c, &r);
+    const float tol = 1.0e-6f * (fmaxf(fmaxf(fabsf(c[0]), fabsf(c[1])), fabsf(c[2])) + col.mesh_scale);
+    MeshHit h = mesh_closest(nodes, tris, c, tol);
+    if (h.tri < 0) return kSdfFar;
+    const float dc = sqrtf((c[0] - h.cp[0]) * (c[0] - h.cp[0]) + (c[1] - h.cp[1]) * (c[1] - h.cp[1]) +
+                           (c[2] - h.cp[2]) * (c[2] - h.cp[2]));
+    const float slack = 4.0f * tol + 1.0e-5f * (dc + r);
+    if (dc - r > slack) {  // the voxel does not reach the surface: one sign for all its points
+        if (h.sign > 0.f && dc - r > s.cutoff + slack) return kSdfFar;
+        if (!col.closed && h.sign < 0.f && dc - r > s.thick + slack) return kSdfFar;
+    }
+    const float R = dc + 2.0f * r + slack;
+    *R2 = R * R;
+    const int n = tris_within(nodes, tris, c, *R2, nullptr, 0);
+    return n > max_cand ? kSdfUseBvh : n;
+}
+
+// Closest triangle of a local point inside the collider's margin box; hit.tri == -2 for "far".
+MPM_HD MeshHit mesh_closest_sdf(const ColliderDev& col, const BvhNode* __restrict__ nodes,
+                                const MeshTri* __restrict__ tris, const int2* __restrict__ cells,
+                                const int32_t* __restrict__ cand, const float p[3], float tol) {
+    const SdfGridDev& s = col.sdf;
+    if (!cells || !s.built) return mesh_closest(nodes, tris, p, tol);
+    int vi[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) hit.cp[k] = best_bary[0] * t.a[k] + best_bary[1] * t.b[k] + best_bary[2] * t.c[k];
-    const float* pn = best_region == 0 ? t.fn : (best_region <= 3 ? t.vn[best_region - 1] : t.en[best_region - 4]);
-    float s = (p[0] - hit.cp[0]) * pn[0] + (p[1] - hit.cp[1]) * pn[1] + (p[2] - hit.cp[2]) * pn[2];
-    hit.sign = s >= 0.f ? 1.f : -1.f;
-    return hit;
+    for (int a = 0; a < 3; ++a) {
+        int i = (int)floorf((p[a] - s.lo[a]) / s.h);
+        vi[a] = i < 0 ? 0 : (i >= s.dims[a] ? s.dims[a] - 1 : i);
+    }
+    const int2 cell = cells[s.cell_offset + ((int64_t)vi[0] * s.dims[1] + vi[1]) * s.dims[2] + vi[2]];
+    if (cell.y == kSdfFar) {
+        MeshHit far;
+        far.tri = -2;
+        far.sign = 1.f;
+        return far;
+    }
+    if (cell.y == kSdfUseBvh) return mesh_closest(nodes, tris, p, tol);
+    ClosestState st;
+    st.init();
+    const double pd[3] = {p[0], p[1], p[2]};
+    for (int i = 0; i < cell.y; ++i) st.consider(tris, cand[cell.x + i], p, pd, tol);
+    return st.finish(tris, p, pd);
 }
 
 // Absolute distance tolerance of the FP32 comparison at point p: a few FP32 ulps of the coordinates involved.
@@ -543,30 +663,42 @@ MPM_HD float query_tol(const ColliderDev& c, const float p[3]) {
 }
 
 // World point -> collider local space, M^-1 p, rounded like the reference's transform_point.
-MPM_HD void to_local(const ColliderDev& c, const float p[3], float pl[3]) {
+MPM_HD void to_local(const ColliderPose& c, const float p[3], float pl[3]) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
         pl[r] = fadd(fadd(fadd(fmul(c.Minv[r][0], p[0]), fmul(c.Minv[r][1], p[1])), fmul(c.Minv[r][2], p[2])), c.Minv[r][3]);
 }
 
+// True when p is inside the collider's local bounding box grown by its margin, the only region where
+// collider_sdf can return a finite distance (colliders.py:47-49).
+MPM_HD bool in_margin_box(const ColliderDev& c, const ColliderPose& pose, const float p[3]) {
+    if (c.n_tris == 0) return false;
+    float pl[3];
+    to_local(pose, p, pl);
+    bool in = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) in &= !(pl[a] < c.aabb_lo[a] - c.margin || pl[a] > c.aabb_hi[a] + c.margin);
+    return in;
+}
+
 // colliders.py:40-65 -> (outward normal, phi); phi = 1e30 when outside the margin box or behind an open mesh
-MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes,
-                                             const MeshTri* __restrict__ tris, const float p[3], float thickness,
-                                             float n[3], float* phi) {
+MPM_HD void collider_sdf(const ColliderDev& c, const ColliderPose& pose, const BvhNode* __restrict__ nodes,
+                         const MeshTri* __restrict__ tris, const int2* __restrict__ cells,
+                         const int32_t* __restrict__ cand, const float p[3], float thickness, float n[3], float* phi) {
     n[0] = 0.f; n[1] = 0.f; n[2] = 1.f;
     *phi = 1.0e30f;
     if (c.n_tris == 0) return;
     float pl[3];
-    to_local(c, p, pl);
+    to_local(pose, p, pl);
 #pragma unroll
     for (int a = 0; a < 3; ++a)
         if (pl[a] < c.aabb_lo[a] - c.margin || pl[a] > c.aabb_hi[a] + c.margin) return;
-    MeshHit h = mesh_closest(nodes + c.node_offset, tris + c.tri_offset, pl, query_tol(c, pl));
-    if (h.tri < 0) return;
+    MeshHit h = mesh_closest_sdf(c, nodes + c.node_offset, tris + c.tri_offset, cells, cand, pl, query_tol(c, pl));
+    if (h.tri < 0) return;  // empty mesh, or a far voxel
     float off[3] = {pl[0] - h.cp[0], pl[1] - h.cp[1], pl[2] - h.cp[2]};
     float d[3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) d[r] = c.M[r][0] * off[0] + c.M[r][1] * off[1] + c.M[r][2] * off[2];
+    for (int r = 0; r < 3; ++r) d[r] = pose.M[r][0] * off[0] + pose.M[r][1] * off[1] + pose.M[r][2] * off[2];
     float dist = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
     if (dist > 1.0e-9f) {
         float k = h.sign / dist;
@@ -575,7 +707,7 @@ MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes
         const float* fn = tris[c.tri_offset + h.tri].fn;
         float tn[3];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) tn[r] = c.Minv[0][r] * fn[0] + c.Minv[1][r] * fn[1] + c.Minv[2][r] * fn[2];
+        for (int r = 0; r < 3; ++r) tn[r] = pose.Minv[0][r] * fn[0] + pose.Minv[1][r] * fn[1] + pose.Minv[2][r] * fn[2];
         float l = sqrtf(tn[0] * tn[0] + tn[1] * tn[1] + tn[2] * tn[2]);
         float k = l > 0.f ? 1.f / l : 0.f;
         n[0] = tn[0] * k; n[1] = tn[1] * k; n[2] = tn[2] * k;
@@ -585,7 +717,7 @@ MPM_HD void collider_sdf(const ColliderDev& c, const BvhNode* __restrict__ nodes
 }
 
 // colliders.py:68-74: velocity of the collider material point at p (central difference of the pose in s)
-MPM_HD void collider_velocity(const ColliderDev& c, const float p[3], float out[3]) {
+MPM_HD void collider_velocity(const ColliderPose& c, const float p[3], float out[3]) {
     float pl[3];
     to_local(c, p, pl);
 #pragma unroll

@@ -205,4 +205,29 @@ inline void collider_set_pose(ColliderDev& col, const float* start16, const floa
     col.margin = (float)(3.0 * dx * inv_scale);
 }
 
+// Extent and resolution of a collider's narrow-band voxel grid. It covers the local bounding box grown by
+// 1.25 x the margin the current poses need, with a contact cutoff of 1.25 x one grid cell in local units,
+// so small changes of scale from frame to frame do not force a rebuild; at most about 97 voxels per axis.
+inline void sdf_grid_params(ColliderDev& col, int64_t cell_offset) {
+    SdfGridDev& g = col.sdf;
+    const double margin = 1.25 * col.margin;
+    const double cutoff = 1.25 * col.margin / 3.0;  // margin is three grid cells at the strongest shrink
+    double extent_max = 0.0, extent[3];
+    for (int a = 0; a < 3; ++a) {
+        extent[a] = (double)col.aabb_hi[a] - col.aabb_lo[a] + 2.0 * margin;
+        extent_max = std::max(extent_max, extent[a]);
+    }
+    const double hv = std::max(cutoff, extent_max / 96.0);
+    for (int a = 0; a < 3; ++a) {
+        g.lo[a] = (float)(col.aabb_lo[a] - margin);
+        g.dims[a] = std::max(1, (int)std::ceil(extent[a] / hv) + 1);
+    }
+    g.h = (float)hv;
+    g.cutoff = (float)cutoff;
+    g.thick = (float)(2.0 * cutoff);  // the open-mesh thickness is two grid cells
+    g.margin = (float)margin;
+    g.built = 0;
+    g.cell_offset = cell_offset;
+}
+
 }  // namespace mpm

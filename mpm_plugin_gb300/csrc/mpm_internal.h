@@ -18,14 +18,35 @@ struct EscapeBounds {  // particles past these planes on open sides are removed 
 // Records the message mpm_last_error(NULL) returns on this thread.
 void set_last_error(const std::string& msg);
 
-void launch_step_begin(cudaStream_t st, StepParams* sp, ColliderDev* cols, int n_col);
-void launch_p2g(cudaStream_t st, const Particles& P, const Material* mats, const GridDesc& g, const StepParams* sp,
-                float4* grid, unsigned int* fp64);
-void launch_grid_update(cudaStream_t st, const GridDesc& g, float4* grid, const StepParams* sp, const ColliderDev* cols,
-                        int n_col, const BvhNode* nodes, const MeshTri* tris);
-void launch_g2p(cudaStream_t st, const Particles& P, const Material* mats, const GridDesc& g, const StepParams* sp,
-                const float4* grid, const ColliderDev* cols, int n_col, const BvhNode* nodes, const MeshTri* tris,
-                unsigned int* fp64);
+constexpr unsigned int kListCtas = 152 * 8;  // CTAs of the kernels that walk device-sized work lists
+
+// Everything one substep's kernels read; the pointers stay fixed while a captured graph is replayed.
+struct SubstepArgs {
+    Particles P;
+    const Material* mats;
+    GridDesc g;
+    StepParams* sp;
+    float4* grid;
+    unsigned int* fp64;
+    WorkLists wl;
+    ColliderData cd;  // poses: the start of the pose array; kernels add the substep's pose_base
+};
+
+void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, ColliderPose* poses, int steps,
+                           float s_given, float inv_frame_dt);
+// One substep: step counters, clear of the previous blocks, P2G, grid update, collider contact, G2P,
+// particle projection. With ev (5 events), records ev[0..4] around: clear | P2G | grid | G2P.
+void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev);
+int substep_kernel_count(const SubstepArgs& a);
+
+constexpr int kSdfMaxCandidates = 128;
+// Narrow-band voxel grid of one collider: classify every voxel (cells[v].y: candidate count, kSdfFar or
+// kSdfUseBvh; counts[v]: the count, 0 otherwise), then, with starts = exclusive scan of counts plus the
+// collider's base, write the candidate lists (cells[v].x: first candidate).
+void launch_sdf_classify(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris,
+                         int64_t n_vox, int max_cand, int2* cells, int32_t* counts);
+void launch_sdf_fill(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris, int64_t n_vox,
+                     int max_cand, int2* cells, const int32_t* starts, int32_t* cand);
 void launch_max_speed(cudaStream_t st, const Particles& P, unsigned int* out);
 void launch_state_in(cudaStream_t st, const Particles& P, int64_t off, int64_t n, const float* x, const float* v,
                      const float* C, const float* F, const float* Jp, const int32_t* mat, const int32_t* emitter);

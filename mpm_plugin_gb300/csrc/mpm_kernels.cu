@@ -12,55 +12,129 @@
 namespace mpm {
 
 // ------------------------------------------------------------------------------------------------------
-// step_begin: advance the substep counter, set s = (k + 1) / steps (warp/solver.py:218-219), then the pose
-// of every collider at s.
+// Collider poses of every substep of an advance, one thread per (substep, collider): substep k ends at
+// s = (k + 1) / steps (warp/solver.py:218-219). steps == 0: one pose at the given s.
 // ------------------------------------------------------------------------------------------------------
-__global__ void k_step_begin(StepParams* sp, ColliderDev* cols, int n_col) {
-    __shared__ float s_sh;
-    if (threadIdx.x == 0) {
-        StepParams p = *sp;
-        if (p.steps > 0) {
-            p.k += 1;
-            p.s = (float)((double)(p.k + 1) / (double)p.steps);
-            *sp = p;
-        }
-        s_sh = p.s;
+__global__ void k_collider_poses(const ColliderDev* __restrict__ cols, int n_col, ColliderPose* __restrict__ poses,
+                                 int steps, float s_given, float inv_frame_dt) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t total = (int64_t)(steps > 0 ? steps : 1) * n_col;
+    if (t >= total) return;
+    int k = (int)(t / n_col), c = (int)(t % n_col);
+    float s = steps > 0 ? (float)((double)(k + 1) / (double)steps) : s_given;
+    collider_pose_at(cols[c], s, inv_frame_dt, poses[t]);
+}
+
+// ------------------------------------------------------------------------------------------------------
+// Start of a substep: counters, substep fraction, pose offset; the work lists of this substep start empty.
+// ------------------------------------------------------------------------------------------------------
+__global__ void k_step_begin(StepParams* sp, unsigned int* counts, int n_col) {
+    StepParams p = *sp;
+    p.seq += 1;
+    if (p.steps > 0) {
+        p.k += 1;
+        p.s = (float)((double)(p.k + 1) / (double)p.steps);
+        p.pose_base = p.k * n_col;
+    } else {
+        p.pose_base = 0;
     }
-    __syncthreads();
-    const float s = s_sh;
-    const float inv_frame_dt = sp->inv_frame_dt;
-    for (int c = threadIdx.x; c < n_col; c += blockDim.x) collider_pose_at(cols[c], s, inv_frame_dt);
+    *sp = p;
+    counts[p.seq & 1u] = 0u;
+    counts[2] = 0u;
+    counts[3] = 0u;
+}
+
+// Zeroes the grid blocks the previous substep used (and their flags), so the whole grid is zero again.
+__global__ void __launch_bounds__(256) k_clear_blocks(const StepParams* __restrict__ sp, WorkLists wl,
+                                                      float4* __restrict__ grid) {
+    const unsigned int prev = (sp->seq - 1u) & 1u;
+    const unsigned int n = wl.counts[prev];
+    const int32_t* __restrict__ list = wl.blocks[prev];
+    for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
+        const int64_t b = list[i];
+        grid[b * 64 + (threadIdx.x & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((threadIdx.x & 63) == 0) wl.block_flag[b] = 0u;
+    }
+}
+
+// Warp-aggregated append: one atomic per warp.
+__device__ __forceinline__ void warp_append(int32_t* __restrict__ list, unsigned int* __restrict__ count, int32_t v) {
+    const unsigned int mask = __activemask();
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    unsigned int base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    list[base + __popc(mask & ((1u << lane) - 1u))] = v;
 }
 
 __global__ void __launch_bounds__(256) k_p2g_scatter(Particles P, const Material* __restrict__ mats, GridDesc g,
                                                      const StepParams* __restrict__ sp, float4* __restrict__ grid,
-                                                     unsigned int* fp64_lanes) {
+                                                     unsigned int* fp64_lanes, WorkLists wl) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    p2g_particle(P, p, mats, g, sp->dt, grid, fp64_lanes);
+    const unsigned int cur = sp->seq & 1u;
+    p2g_particle(P, p, mats, g, sp->dt, grid, fp64_lanes, wl.block_flag, wl.blocks[cur], &wl.counts[cur]);
 }
 
-// One CTA of 64 threads per 4x4x4 block; nodes without mass return at once.
-__global__ void __launch_bounds__(64) k_grid_update(GridDesc g, float4* __restrict__ grid, const StepParams* __restrict__ sp,
-                                                    const ColliderDev* __restrict__ cols, int n_col,
-                                                    const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris) {
-    const int64_t blk = blockIdx.x;
-    const int l = threadIdx.x;
-    const int bk = (int)(blk % g.nb[2]);
-    const int bj = (int)((blk / g.nb[2]) % g.nb[1]);
-    const int bi = (int)(blk / ((int64_t)g.nb[2] * g.nb[1]));
-    const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-    grid_update_node(g, &grid[blk * 64 + l], idx, sp->dt, cols, n_col, nodes, tris);
+// Grid update over the active blocks, four 4x4x4 blocks per 256-thread CTA. Nodes inside a collider's
+// margin box are listed for k_grid_colliders.
+__global__ void __launch_bounds__(256) k_grid_update(GridDesc g, float4* __restrict__ grid,
+                                                     const StepParams* __restrict__ sp, WorkLists wl, ColliderData cd) {
+    const unsigned int cur = sp->seq & 1u;
+    const unsigned int n = wl.counts[cur];
+    const float dt = sp->dt;
+    cd.poses += sp->pose_base;
+    const int l = threadIdx.x & 63;
+    for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
+        const int64_t b = wl.blocks[cur][i];
+        const int bk = (int)(b % g.nb[2]);
+        const int bj = (int)((b / g.nb[2]) % g.nb[1]);
+        const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
+        const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+        bool has_mass = grid_node_walls(g, &grid[b * 64 + l], idx, dt);
+        if (has_mass && cd.n_col > 0) {
+            float pos[3];
+            node_position(g, idx, pos);
+            if (near_any_collider(pos, cd)) warp_append(wl.node_cand, &wl.counts[2], (int32_t)(b * 64 + l));
+        }
+    }
 }
 
+// Mesh-collider contact of the listed nodes (full warps of candidates; BVH queries).
+__global__ void __launch_bounds__(128) k_grid_colliders(GridDesc g, float4* __restrict__ grid,
+                                                        const StepParams* __restrict__ sp, WorkLists wl, ColliderData cd) {
+    const unsigned int n = wl.counts[2];
+    cd.poses += sp->pose_base;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int64_t q = wl.node_cand[i];
+        const int64_t b = q >> 6;
+        const int l = (int)(q & 63);
+        const int bk = (int)(b % g.nb[2]);
+        const int bj = (int)((b / g.nb[2]) % g.nb[1]);
+        const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
+        const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+        grid_node_colliders(g, &grid[q], idx, cd);
+    }
+}
+
+// G2P; particles that end inside a collider's margin box are listed for k_project_particles.
 __global__ void __launch_bounds__(256) k_g2p(Particles P, const Material* __restrict__ mats, GridDesc g,
                                              const StepParams* __restrict__ sp, const float4* __restrict__ grid,
-                                             const ColliderDev* __restrict__ cols, int n_col,
-                                             const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris,
-                                             unsigned int* fp64_lanes) {
+                                             unsigned int* fp64_lanes, WorkLists wl, ColliderData cd) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    g2p_particle(P, p, mats, g, sp->dt, grid, cols, n_col, nodes, tris, fp64_lanes);
+    float nx[3];
+    g2p_particle(P, p, mats, g, sp->dt, grid, fp64_lanes, nx);
+    cd.poses += sp->pose_base;
+    if (cd.n_col > 0 && near_any_collider(nx, cd)) warp_append(wl.part_cand, &wl.counts[3], (int32_t)p);
+}
+
+__global__ void __launch_bounds__(128) k_project_particles(Particles P, GridDesc g, const StepParams* __restrict__ sp,
+                                                           WorkLists wl, ColliderData cd) {
+    const unsigned int n = wl.counts[3];
+    cd.poses += sp->pose_base;
+    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        project_particle(P, wl.part_cand[i], g, cd);
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -280,32 +354,75 @@ __global__ void k_grid_unblock(GridDesc g, const float4* __restrict__ grid, floa
 }
 
 // ------------------------------------------------------------------------------------------------------
+// Narrow-band voxel grid of a collider: classify every voxel, then (after a scan) write candidate lists.
+// ------------------------------------------------------------------------------------------------------
+__global__ void k_sdf_classify(ColliderDev col, const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris,
+                               int64_t n_vox, int max_cand, int2* __restrict__ cells, int32_t* __restrict__ counts) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_vox) return;
+    float R2;
+    int c = sdf_voxel_classify(col, nodes, tris, v, max_cand, &R2);
+    cells[v] = make_int2(0, c);
+    counts[v] = c > 0 ? c : 0;
+}
+
+__global__ void k_sdf_fill(ColliderDev col, const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris,
+                           int64_t n_vox, int max_cand, int2* __restrict__ cells, const int32_t* __restrict__ starts,
+                           int32_t* __restrict__ cand) {
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n_vox) return;
+    const int2 cell = cells[v];
+    cells[v] = make_int2(starts[v], cell.y);
+    if (cell.y <= 0) return;
+    float R2, c[3], r;
+    sdf_voxel_classify(col, nodes, tris, v, max_cand, &R2);  // the same radius as the classify pass
+    sdf_voxel_center(col.sdf, v, c, &r);
+    tris_within(nodes, tris, c, R2, cand + starts[v], cell.y);
+}
+
+// ------------------------------------------------------------------------------------------------------
 // launchers
 // ------------------------------------------------------------------------------------------------------
 static inline unsigned int blocks_for(int64_t n, int t) { return (unsigned int)((n + t - 1) / t); }
 
-void launch_step_begin(cudaStream_t st, StepParams* sp, ColliderDev* cols, int n_col) {
-    k_step_begin<<<1, 32, 0, st>>>(sp, cols, n_col);
+void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, ColliderPose* poses, int steps,
+                           float s_given, float inv_frame_dt) {
+    if (n_col <= 0) return;
+    int64_t total = (int64_t)(steps > 0 ? steps : 1) * n_col;
+    k_collider_poses<<<blocks_for(total, 128), 128, 0, st>>>(cols, n_col, poses, steps, s_given, inv_frame_dt);
 }
 
-void launch_p2g(cudaStream_t st, const Particles& P, const Material* mats, const GridDesc& g, const StepParams* sp,
-                float4* grid, unsigned int* fp64) {
-    if (P.n == 0) return;
-    k_p2g_scatter<<<blocks_for(P.n, 256), 256, 0, st>>>(P, mats, g, sp, grid, fp64);
+void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev) {
+    const unsigned int list_ctas = kListCtas;
+    if (ev) cudaEventRecord(ev[0], st);
+    k_step_begin<<<1, 1, 0, st>>>(a.sp, a.wl.counts, a.cd.n_col);
+    k_clear_blocks<<<list_ctas, 256, 0, st>>>(a.sp, a.wl, a.grid);
+    if (ev) cudaEventRecord(ev[1], st);
+    if (a.P.n > 0) k_p2g_scatter<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.fp64, a.wl);
+    if (ev) cudaEventRecord(ev[2], st);
+    k_grid_update<<<list_ctas, 256, 0, st>>>(a.g, a.grid, a.sp, a.wl, a.cd);
+    if (a.cd.n_col > 0) k_grid_colliders<<<list_ctas, 128, 0, st>>>(a.g, a.grid, a.sp, a.wl, a.cd);
+    if (ev) cudaEventRecord(ev[3], st);
+    if (a.P.n > 0)
+        k_g2p<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.fp64, a.wl, a.cd);
+    if (a.cd.n_col > 0) k_project_particles<<<list_ctas, 128, 0, st>>>(a.P, a.g, a.sp, a.wl, a.cd);
+    if (ev) cudaEventRecord(ev[4], st);
 }
 
-void launch_grid_update(cudaStream_t st, const GridDesc& g, float4* grid, const StepParams* sp, const ColliderDev* cols,
-                        int n_col, const BvhNode* nodes, const MeshTri* tris) {
-    int64_t nblk = (int64_t)g.nb[0] * g.nb[1] * g.nb[2];
-    k_grid_update<<<(unsigned int)nblk, 64, 0, st>>>(g, grid, sp, cols, n_col, nodes, tris);
+void launch_sdf_classify(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris,
+                         int64_t n_vox, int max_cand, int2* cells, int32_t* counts) {
+    k_sdf_classify<<<blocks_for(n_vox, 128), 128, 0, st>>>(col, nodes, tris, n_vox, max_cand, cells, counts);
 }
 
-void launch_g2p(cudaStream_t st, const Particles& P, const Material* mats, const GridDesc& g, const StepParams* sp,
-                const float4* grid, const ColliderDev* cols, int n_col, const BvhNode* nodes, const MeshTri* tris,
-                unsigned int* fp64) {
-    if (P.n == 0) return;
-    k_g2p<<<blocks_for(P.n, 256), 256, 0, st>>>(P, mats, g, sp, grid, cols, n_col, nodes, tris, fp64);
+void launch_sdf_fill(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris, int64_t n_vox,
+                     int max_cand, int2* cells, const int32_t* starts, int32_t* cand) {
+    k_sdf_fill<<<blocks_for(n_vox, 128), 128, 0, st>>>(col, nodes, tris, n_vox, max_cand, cells, starts, cand);
 }
+
+int substep_kernel_count(const SubstepArgs& a) {
+    return 3 + (a.P.n > 0 ? 2 : 0) + (a.cd.n_col > 0 ? 2 : 0);
+}
+
 
 void launch_max_speed(cudaStream_t st, const Particles& P, unsigned int* out) {
     if (P.n == 0) return;

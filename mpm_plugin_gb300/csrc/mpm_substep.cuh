@@ -74,7 +74,7 @@ MPM_HD void inverse_affine(const float M[3][4], float out[3][4]) {  // float64 e
 
 // Collider pose at substep fraction s: M, its inverse, and dM/dt by a central difference in s with
 // h = 1e-3 scaled by 1 / frame_dt (colliders.py:30-37, 68-74).
-MPM_HD void collider_pose_at(ColliderDev& col, float s, float inv_frame_dt) {
+MPM_HD void collider_pose_at(const ColliderDev& col, float s, float inv_frame_dt, ColliderPose& out) {
     float M[3][4], Mp[3][4], Mm[3][4], Mi[3][4];
     const float h = 1.0e-3f;
     collider_matrix(col, s, M);
@@ -84,9 +84,9 @@ MPM_HD void collider_pose_at(ColliderDev& col, float s, float inv_frame_dt) {
     float k = fdiv(inv_frame_dt, fmul(2.0f, h));
     for (int r = 0; r < 3; ++r)
         for (int j = 0; j < 4; ++j) {
-            col.M[r][j] = M[r][j];
-            col.Minv[r][j] = Mi[r][j];
-            col.dM[r][j] = fmul(fsub(Mp[r][j], Mm[r][j]), k);
+            out.M[r][j] = M[r][j];
+            out.Minv[r][j] = Mi[r][j];
+            out.dM[r][j] = fmul(fsub(Mp[r][j], Mm[r][j]), k);
         }
 }
 
@@ -117,8 +117,23 @@ MPM_HD void store_mat3(float* const* dst, int64_t p, const float M[3][3]) {
         for (int j = 0; j < 3; ++j) dst[i * 3 + j][p] = M[i][j];
 }
 
+// Adds grid block b to the active list of this substep unless it is there already.
+MPM_HD void mark_block(int64_t b, unsigned int* __restrict__ flags, int32_t* __restrict__ list,
+                       unsigned int* __restrict__ count) {
+#ifdef __CUDA_ARCH__
+    if (flags[b] == 0u && atomicExch(&flags[b], 1u) == 0u) list[atomicAdd(count, 1u)] = (int32_t)b;
+#else
+    if (flags[b] == 0u) {
+        flags[b] = 1u;
+        list[(*count)++] = (int32_t)b;
+    }
+#endif
+}
+
+// flags / list / count may be null (no active-block bookkeeping).
 MPM_HD void p2g_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         float4* __restrict__ grid, unsigned int* fp64) {
+                         float4* __restrict__ grid, unsigned int* fp64, unsigned int* __restrict__ flags = nullptr,
+                         int32_t* __restrict__ list = nullptr, unsigned int* __restrict__ count = nullptr) {
     const Material m = mats[P.mat[p]];
     float F[3][3], tau[3][3];
     load_mat3(P.F, p, F);
@@ -148,6 +163,14 @@ MPM_HD void p2g_particle(const Particles& P, int64_t p, const Material* __restri
         mv[a] = pm * P.v[a][p];
     }
     if (!inside) return;
+    if (flags) {  // the 1 to 8 grid blocks this particle's 3x3x3 stencil touches
+        const int b0[3] = {base[0] >> 2, base[1] >> 2, base[2] >> 2};
+        const int b1[3] = {(base[0] + 2) >> 2, (base[1] + 2) >> 2, (base[2] + 2) >> 2};
+        for (int bi = b0[0]; bi <= b1[0]; ++bi)
+            for (int bj = b0[1]; bj <= b1[1]; ++bj)
+                for (int bk = b0[2]; bk <= b1[2]; ++bk)
+                    mark_block(((int64_t)bi * g.nb[1] + bj) * g.nb[2] + bk, flags, list, count);
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -176,49 +199,66 @@ MPM_HD void wall_contact(float vel[3], int axis, float friction) {
     }
 }
 
-MPM_HD void grid_update_node(const GridDesc& g, float4* node, const int idx[3], float dt,
-                             const ColliderDev* __restrict__ cols, int n_col, const BvhNode* __restrict__ nodes,
-                             const MeshTri* __restrict__ tris) {
+// Normalise, gravity and wall contact of one node (kernels.py:155-180); false for a node without mass.
+MPM_HD bool grid_node_walls(const GridDesc& g, float4* node, const int idx[3], float dt) {
     float4 nv = *node;
     const float m = nv.w;
-    if (!(m > 0.0f)) return;  // the reference skips m <= 0 (kernels.py:171-172)
+    if (!(m > 0.0f)) return false;  // the reference skips m <= 0 (kernels.py:171-172)
     float vel[3] = {nv.x / m + dt * g.gravity[0], nv.y / m + dt * g.gravity[1], nv.z / m + dt * g.gravity[2]};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         if (g.lo_on[a] && idx[a] <= g.wall_lo_node[a] && vel[a] < 0.0f) wall_contact(vel, a, g.wall_friction);
         if (g.hi_on[a] && idx[a] >= g.wall_hi_node[a] && vel[a] > 0.0f) wall_contact(vel, a, g.wall_friction);
     }
-    if (n_col > 0) {
-        const float pos[3] = {fadd(g.origin[0], fmul((float)idx[0], g.dx)), fadd(g.origin[1], fmul((float)idx[1], g.dx)),
-                              fadd(g.origin[2], fmul((float)idx[2], g.dx))};
-        for (int c = 0; c < n_col; ++c) {
-            const ColliderDev& col = cols[c];
-            float n[3], phi;
-            collider_sdf(col, nodes, tris, pos, g.thickness, n, &phi);
-            if (phi < g.band) {
-                float vcol[3];
-                collider_velocity(col, pos, vcol);
-                float rel[3] = {vel[0] - vcol[0], vel[1] - vcol[1], vel[2] - vcol[2]};
-                float vn = rel[0] * n[0] + rel[1] * n[1] + rel[2] * n[2];
-                if (vn < 0.0f) {
-                    float rt[3] = {rel[0] - vn * n[0], rel[1] - vn * n[1], rel[2] - vn * n[2]};
-                    float rt_len = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2]);
-                    if (rt_len > 0.0f) {
-                        float f = fmaxf(0.0f, 1.0f - col.friction * (-vn) / rt_len);
-                        rt[0] *= f; rt[1] *= f; rt[2] *= f;
-                    }
-                    if (phi < 0.0f) {  // behind the surface: no penetration
+    *node = make_float4(vel[0], vel[1], vel[2], m);
+    return true;
+}
+
+// World position of a grid node, rounded like the reference's origin + (i, j, k) * dx (colliders.py:101).
+MPM_HD void node_position(const GridDesc& g, const int idx[3], float pos[3]) {
 #pragma unroll
-                        for (int a = 0; a < 3; ++a) vel[a] = vcol[a] + rt[a];
-                    } else {  // in the band: friction only
+    for (int a = 0; a < 3; ++a) pos[a] = fadd(g.origin[a], fmul((float)idx[a], g.dx));
+}
+
+MPM_HD bool near_any_collider(const float pos[3], const ColliderData& cd) {
+    for (int c = 0; c < cd.n_col; ++c)
+        if (in_margin_box(cd.cols[c], cd.poses[c], pos)) return true;
+    return false;
+}
+
+// Mesh-collider contact of one node after the wall pass (colliders.py:77-117).
+MPM_HD void grid_node_colliders(const GridDesc& g, float4* node, const int idx[3], const ColliderData& cd) {
+    float4 nv = *node;
+    float vel[3] = {nv.x, nv.y, nv.z};
+    float pos[3];
+    node_position(g, idx, pos);
+    for (int c = 0; c < cd.n_col; ++c) {
+        const ColliderDev& col = cd.cols[c];
+        float n[3], phi;
+        collider_sdf(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, pos, g.thickness, n, &phi);
+        if (phi < g.band) {
+            float vcol[3];
+            collider_velocity(cd.poses[c], pos, vcol);
+            float rel[3] = {vel[0] - vcol[0], vel[1] - vcol[1], vel[2] - vcol[2]};
+            float vn = rel[0] * n[0] + rel[1] * n[1] + rel[2] * n[2];
+            if (vn < 0.0f) {
+                float rt[3] = {rel[0] - vn * n[0], rel[1] - vn * n[1], rel[2] - vn * n[2]};
+                float rt_len = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2]);
+                if (rt_len > 0.0f) {
+                    float f = fmaxf(0.0f, 1.0f - col.friction * (-vn) / rt_len);
+                    rt[0] *= f; rt[1] *= f; rt[2] *= f;
+                }
+                if (phi < 0.0f) {  // behind the surface: no penetration
 #pragma unroll
-                        for (int a = 0; a < 3; ++a) vel[a] = vcol[a] + rt[a] + vn * n[a];
-                    }
+                    for (int a = 0; a < 3; ++a) vel[a] = vcol[a] + rt[a];
+                } else {  // in the band: friction only
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) vel[a] = vcol[a] + rt[a] + vn * n[a];
                 }
             }
         }
     }
-    *node = make_float4(vel[0], vel[1], vel[2], m);
+    *node = make_float4(vel[0], vel[1], vel[2], nv.w);
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -232,9 +272,9 @@ MPM_HD float4 load_node(const float4* p) {
 #endif
 }
 
+// Returns the new position in nx_out.
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         const float4* __restrict__ grid, const ColliderDev* __restrict__ cols, int n_col,
-                         const BvhNode* __restrict__ nodes, const MeshTri* __restrict__ tris, unsigned int* fp64) {
+                         const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3]) {
     float xo[3];
     int base[3];
     float fx[3], w[3][3];
@@ -313,15 +353,27 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
     }
     store_mat3(P.F, p, Fn);
 
-    for (int c = 0; c < n_col; ++c) {  // push particles that ended up inside a collider onto its surface
-        const ColliderDev& col = cols[c];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        P.x[a][p] = nx[a];
+        P.v[a][p] = nv[a];
+        nx_out[a] = nx[a];
+    }
+}
+
+// Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity
+// relative to the collider (colliders.py:120-148).
+MPM_HD void project_particle(const Particles& P, int64_t p, const GridDesc& g, const ColliderData& cd) {
+    float nx[3] = {P.x[0][p], P.x[1][p], P.x[2][p]}, nv[3] = {P.v[0][p], P.v[1][p], P.v[2][p]};
+    for (int c = 0; c < cd.n_col; ++c) {
+        const ColliderDev& col = cd.cols[c];
         float n[3], phi;
-        collider_sdf(col, nodes, tris, nx, g.thickness, n, &phi);
+        collider_sdf(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, nx, g.thickness, n, &phi);
         if (phi < 0.0f) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) nx[a] = nx[a] - phi * n[a];
             float vcol[3];
-            collider_velocity(col, nx, vcol);
+            collider_velocity(cd.poses[c], nx, vcol);
             float vn = (nv[0] - vcol[0]) * n[0] + (nv[1] - vcol[1]) * n[1] + (nv[2] - vcol[2]) * n[2];
             if (vn < 0.0f) {
 #pragma unroll

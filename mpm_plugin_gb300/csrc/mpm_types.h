@@ -64,9 +64,20 @@ struct MeshTri {  // 128 B, leaf order
     float pad[1];
 };
 
-// Per collider: static data plus the pose of the current substep (written on the device each substep).
+// Narrow-band voxel grid of one collider in its local space (see mpm_device.cuh).
+struct SdfGridDev {
+    float lo[3], h;       // corner and voxel edge, local units
+    int dims[3];
+    int built;            // 0: not built, queries use the BVH
+    int64_t cell_offset;  // first cell of this collider in the shared cell array
+    float cutoff;         // local distance beyond which an outside point cannot reach the contact band
+    float thick;          // local distance beyond which a point behind an open mesh is outside it
+    float margin;         // margin of the bounding box the grid covers
+};
+
+// Per collider: static data and the pose pair of the current advance.
 struct ColliderDev {
-    float M[3][4], Minv[3][4], dM[3][4];
+    SdfGridDev sdf;
     float aabb_lo[3], aabb_hi[3];
     float margin, friction;
     float mesh_scale;  // largest |coordinate| of the mesh's local bounding box
@@ -76,12 +87,41 @@ struct ColliderDev {
     float t0[3], t1[3], q0[4], q1[4], S0[9], S1[9];
 };
 
-// Values a substep reads from device memory (so one captured substep graph serves every substep).
+// A collider's pose at one substep: world transform, its inverse, and d(transform)/dt for the velocity.
+struct ColliderPose {
+    float M[3][4], Minv[3][4], dM[3][4];
+};
+
+// Everything a collider query needs, as device pointers.
+struct ColliderData {
+    const ColliderDev* cols;
+    const ColliderPose* poses;  // of the current substep (already offset)
+    int n_col;
+    const BvhNode* nodes;
+    const MeshTri* tris;
+    const int2* cells;      // narrow-band voxel grids (may be null)
+    const int32_t* cand;    // their candidate lists
+};
+
+// Values a substep reads from device memory, so one captured graph of a substep replays for all of them.
 struct StepParams {
     float dt;
-    float s;            // fraction of the advance at the end of this substep, (k + 1) / steps
-    float inv_frame_dt; // 1 / duration of the current advance call
-    int k, steps;
+    float s;             // fraction of the advance at the end of this substep, (k + 1) / steps
+    float inv_frame_dt;  // 1 / duration of the current advance call
+    int k, steps;        // substep index within the advance; steps == 0 for a single explicit substep
+    unsigned int seq;    // substeps run so far on this handle (selects the active-block list in use)
+    int pose_base;       // first pose of this substep in the pose array
+};
+
+// Work lists the substep builds on the device. Active blocks are the 4x4x4 grid blocks P2G touched;
+// there are two lists, used by alternate substeps, so a substep can clear the blocks of the one before.
+struct WorkLists {
+    unsigned int* block_flag;   // one per grid block: 1 while the block is in the current list
+    int32_t* blocks[2];         // active block ids
+    unsigned int* counts;       // [0], [1]: active block counts; [2]: collider node candidates;
+                                // [3]: collider particle candidates
+    int32_t* node_cand;         // grid nodes (blocked index) inside some collider's margin box
+    int32_t* part_cand;         // particles inside some collider's margin box after G2P
 };
 
 }  // namespace mpm

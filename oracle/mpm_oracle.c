@@ -552,7 +552,7 @@ static void closest_on_triangle(const double *p, const double *a, const double *
     double d1 = D3(ab, ap), d2 = D3(ac, ap), d3 = D3(ab, bp), d4 = D3(ac, bp), d5 = D3(ab, cp), d6 = D3(ac, cp);
 #undef D3
     if (d1 <= 0 && d2 <= 0) { bary[0] = 1; bary[1] = 0; bary[2] = 0; *region = 1; return; }
-    if (d3 >= 0 && d6 <= d5) { bary[0] = 0; bary[1] = 1; bary[2] = 0; *region = 2; return; }
+    if (d3 >= 0 && d4 <= d3) { bary[0] = 0; bary[1] = 1; bary[2] = 0; *region = 2; return; }
     double vc = d1 * d4 - d3 * d2;
     if (vc <= 0 && d1 >= 0 && d3 <= 0) { double v = d1 / (d1 - d3); bary[0] = 1 - v; bary[1] = v; bary[2] = 0; *region = 4; return; }
     if (d6 >= 0 && d5 <= d6) { bary[0] = 0; bary[1] = 0; bary[2] = 1; *region = 3; return; }

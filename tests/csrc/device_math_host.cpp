@@ -80,8 +80,39 @@ struct Emu {
     std::vector<ColliderDev> cols;
     std::vector<BvhNode> nodes;
     std::vector<MeshTri> tris;
+    std::vector<int2> cells;
+    std::vector<int32_t> cand;
+    bool use_sdf = true;
     unsigned int fp64 = 0;
 };
+
+// Narrow-band voxel grids, built with the same per-voxel functions the GPU build runs.
+static void emu_build_sdf(Emu* e) {
+    e->cells.clear();
+    e->cand.clear();
+    int64_t total = 0;
+    for (auto& col : e->cols) {
+        sdf_grid_params(col, total);
+        if (col.n_tris == 0) continue;
+        const int64_t nv = (int64_t)col.sdf.dims[0] * col.sdf.dims[1] * col.sdf.dims[2];
+        total += nv;
+        const BvhNode* nodes = e->nodes.data() + col.node_offset;
+        const MeshTri* tris = e->tris.data() + col.tri_offset;
+        for (int64_t v = 0; v < nv; ++v) {
+            float R2;
+            int c = sdf_voxel_classify(col, nodes, tris, v, 128, &R2);
+            int start = (int)e->cand.size();
+            e->cells.push_back(int2{start, c});
+            if (c > 0) {
+                float ctr[3], r;
+                sdf_voxel_center(col.sdf, v, ctr, &r);
+                e->cand.resize(start + c);
+                tris_within(nodes, tris, ctr, R2, e->cand.data() + start, c);
+            }
+        }
+        col.sdf.built = 1;
+    }
+}
 
 extern "C" {
 
@@ -116,7 +147,10 @@ void emu_set_colliders(void* ev, int n, const MpmColliderDesc* cs) {
 void emu_set_transforms(void* ev, int n, const float* s16, const float* e16) {
     Emu* e = static_cast<Emu*>(ev);
     for (int c = 0; c < n; ++c) collider_set_pose(e->cols[c], s16 + 16 * c, e16 + 16 * c, e->hd.dx);
+    if (e->use_sdf) emu_build_sdf(e);
 }
+
+void emu_use_sdf(void* ev, int on) { static_cast<Emu*>(ev)->use_sdf = on != 0; }
 
 void emu_grid_dims(void* ev, int* dims) {
     Emu* e = static_cast<Emu*>(ev);
@@ -135,10 +169,18 @@ unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, floa
     P.n = n;
     P.cap = n;
     const float dtf = (float)dt;
-    for (auto& c : e->cols) collider_pose_at(c, (float)s, (float)(1.0 / frame_dt));
+    std::vector<ColliderPose> poses(e->cols.size());
+    for (size_t c = 0; c < e->cols.size(); ++c) collider_pose_at(e->cols[c], (float)s, (float)(1.0 / frame_dt), poses[c]);
     std::fill(e->grid.begin(), e->grid.end(), float4{0, 0, 0, 0});
-    const ColliderDev* cols = e->cols.empty() ? nullptr : e->cols.data();
-    const int n_col = (int)e->cols.size();
+    ColliderData cd{};
+    cd.cols = e->cols.empty() ? nullptr : e->cols.data();
+    cd.poses = poses.empty() ? nullptr : poses.data();
+    cd.n_col = (int)e->cols.size();
+    cd.nodes = e->nodes.data();
+    cd.tris = e->tris.data();
+    cd.cells = e->use_sdf && !e->cells.empty() ? e->cells.data() : nullptr;
+    cd.cand = e->cand.empty() ? nullptr : e->cand.data();
+    const int n_col = cd.n_col;
     for (int64_t p = 0; p < n; ++p) p2g_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data(), &e->fp64);
     const int64_t nblk = (int64_t)e->g.nb[0] * e->g.nb[1] * e->g.nb[2];
     for (int64_t blk = 0; blk < nblk; ++blk) {
@@ -146,13 +188,37 @@ unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, floa
         const int bi = (int)(blk / ((int64_t)e->g.nb[2] * e->g.nb[1]));
         for (int l = 0; l < 64; ++l) {
             const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-            grid_update_node(e->g, &e->grid[blk * 64 + l], idx, dtf, cols, n_col, e->nodes.data(), e->tris.data());
+            float4* node = &e->grid[blk * 64 + l];
+            if (!grid_node_walls(e->g, node, idx, dtf) || n_col == 0) continue;
+            float pos[3];
+            node_position(e->g, idx, pos);
+            if (near_any_collider(pos, cd)) grid_node_colliders(e->g, node, idx, cd);
         }
     }
-    for (int64_t p = 0; p < n; ++p)
-        g2p_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data(), cols, n_col, e->nodes.data(), e->tris.data(),
-                     &e->fp64);
+    for (int64_t p = 0; p < n; ++p) {
+        float nx[3];
+        g2p_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data(), &e->fp64, nx);
+        if (n_col > 0 && near_any_collider(nx, cd)) project_particle(P, p, e->g, cd);
+    }
     return e->fp64;
+}
+
+// collider_sdf of collider c at substep fraction s for n world points: out (n, 4) = normal, phi
+void emu_collider_sdf(void* ev, int c, float s, int use_sdf, int n, const float* pts, float* out) {
+    Emu* e = static_cast<Emu*>(ev);
+    ColliderPose pose;
+    collider_pose_at(e->cols[c], s, 1.0f, pose);
+    const int2* cells = use_sdf && !e->cells.empty() ? e->cells.data() : nullptr;
+    const int32_t* cand = e->cand.empty() ? nullptr : e->cand.data();
+    for (int k = 0; k < n; ++k) {
+        float nn[3], phi = 1.0e30f;
+        if (in_margin_box(e->cols[c], pose, &pts[3 * k]))
+            collider_sdf(e->cols[c], pose, e->nodes.data(), e->tris.data(), cells, cand, &pts[3 * k], e->g.thickness, nn,
+                         &phi);
+        else
+            nn[0] = nn[1] = 0.f, nn[2] = 1.f;
+        out[4 * k] = nn[0]; out[4 * k + 1] = nn[1]; out[4 * k + 2] = nn[2]; out[4 * k + 3] = phi;
+    }
 }
 
 void emu_read_grid(void* ev, float* out) {

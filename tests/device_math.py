@@ -50,6 +50,8 @@ def lib():
     L.emu_substep.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_double, C.c_double, C.c_double]
     L.emu_substep.restype = C.c_uint
     L.emu_read_grid.argtypes = [P, P]
+    L.emu_use_sdf.argtypes = [P, C.c_int]
+    L.emu_collider_sdf.argtypes = [P, C.c_int, C.c_float, C.c_int, C.c_int, P, P]
     _lib = L
     return L
 
@@ -97,7 +99,7 @@ class HostMesh:
 class SubstepEmulator:
     """The CUDA backend's substep (mpm_substep.cuh) run on the CPU, one item after another."""
 
-    def __init__(self, domain, materials, gravity=(0.0, 0.0, -9.81), ppc=8):
+    def __init__(self, domain, materials, gravity=(0.0, 0.0, -9.81), ppc=8, use_sdf=True):
         from mpm_plugin_gb300 import _abi
 
         d = _abi.MpmDomainDesc()
@@ -114,6 +116,7 @@ class SubstepEmulator:
         g = (C.c_double * 3)(*gravity)
         self._abi = _abi
         self.h = lib().emu_create(C.byref(d), mats, len(materials), g, ppc)
+        lib().emu_use_sdf(self.h, int(use_sdf))
         self.state = None
 
     def set_colliders(self, colliders):
@@ -155,6 +158,13 @@ class SubstepEmulator:
         st = self.state
         return lib().emu_substep(self.h, len(st["Jp"]), _p(st["x"]), _p(st["v"]), _p(st["C"]), _p(st["F"]),
                                  _p(st["Jp"]), _p(st["mat"]), dt, s, frame_dt)
+
+    def collider_sdf(self, c, s, pts, use_sdf=True):
+        """(normal xyz, phi) of collider c at substep fraction s for world points (phi 1e30: far)."""
+        pts = np.ascontiguousarray(np.asarray(pts, np.float32).reshape(-1, 3))
+        out = np.zeros((len(pts), 4), np.float32)
+        lib().emu_collider_sdf(self.h, c, s, int(use_sdf), len(pts), _p(pts), _p(out))
+        return out
 
     def read_grid(self):
         dims = np.zeros(3, np.int32)

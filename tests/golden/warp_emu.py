@@ -532,7 +532,7 @@ def closest_point_triangles(p, a, b, c):
     one = np.ones(T)
     zero = np.zeros(T)
     put((d1 <= 0) & (d2 <= 0), np.stack([one, zero, zero], 1), 1)
-    put((d3 >= 0) & (d6 <= d5), np.stack([zero, one, zero], 1), 2)
+    put((d3 >= 0) & (d4 <= d3), np.stack([zero, one, zero], 1), 2)
     with np.errstate(divide="ignore", invalid="ignore"):
         v_ab = d1 / (d1 - d3)
         put((vc <= 0) & (d1 >= 0) & (d3 <= 0), np.stack([1 - v_ab, v_ab, zero], 1), 4)

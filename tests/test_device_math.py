@@ -88,3 +88,81 @@ def test_mesh_query_matches_oracle(mesh):
         assert abs(np.linalg.norm(cp[i].astype(np.float64) - p) - np.sqrt(d2)) < 1e-5
         # the same face, or another face through the same closest point (a shared edge or vertex)
         assert fc[i] == f or np.linalg.norm(cp[i] - ocp) < 1e-5, (i, p, fc[i], f)
+
+
+@pytest.mark.parametrize("mesh,closed", [("sphere", True), ("cube", True), ("plane", False)])
+def test_narrow_band_grid_matches_full_query(mesh, closed):
+    """Collider SDF through the narrow-band voxel grid against the full BVH query.
+
+    Where the grid answers "far", the exact distance must be outside and beyond the contact band (or behind
+    an open mesh beyond its thickness), so neither grid contact nor particle projection would act; elsewhere
+    the two answers are identical.
+    """
+    from device_math import SubstepEmulator
+    from scenes import domain, preset, rot_x, scale, translate
+
+    if mesh == "sphere":
+        v, t = icosphere(1.0, 3)
+        xf0 = translate(0.5, 0.5, 0.3) @ scale(0.15)
+        xf1 = translate(0.5, 0.52, 0.3) @ rot_x(30) @ scale(0.15)
+    elif mesh == "cube":
+        v, t = unit_cube_mesh(centered=True)
+        xf0 = translate(0.5, 0.5, 0.2) @ scale(0.4, 0.3, 0.2)
+        xf1 = translate(0.51, 0.5, 0.2) @ rot_x(5) @ scale(0.4, 0.3, 0.2)
+    else:
+        v, t = plane_mesh(0.8)
+        xf0 = translate(0.5, 0.5, 0.3) @ rot_x(10)
+        xf1 = xf0
+    d = domain(res=64)
+    e = SubstepEmulator(d, [preset("jelly")])
+    e.set_colliders([(v, t, closed, 0.5)])
+    e.set_collider_transforms(xf0[None], xf1[None])
+    rng = np.random.default_rng(7)
+    pts = rng.uniform(0.0, 1.0, (20000, 3)).astype(np.float32)
+    for s in (0.0, 0.5, 1.0):
+        a = e.collider_sdf(0, s, pts, use_sdf=True)
+        b = e.collider_sdf(0, s, pts, use_sdf=False)
+        far = a[:, 3] >= 1e29
+        band, thick = d.dx, 2 * d.dx
+        # far in the grid: the exact answer is far too, or outside beyond the band
+        ok_far = (b[far, 3] >= 1e29) | (b[far, 3] >= band)
+        assert ok_far.all()
+        np.testing.assert_array_equal(a[~far], b[~far])
+        assert (~far).sum() > 100
+
+
+def _closest_point_independent(p, a, b, c):
+    """Closest point on a triangle without region tests: the plane projection if it falls inside, else the
+    nearest of the closest points on the three edges."""
+    n = np.cross(b - a, c - a)
+    n2 = n @ n
+    q = p - ((p - a) @ n) / n2 * n
+    u = np.cross(c - b, q - b) @ n / n2
+    v = np.cross(a - c, q - c) @ n / n2
+    w = 1 - u - v
+    if u >= 0 and v >= 0 and w >= 0:
+        return q
+    best = None
+    for s, e in ((a, b), (b, c), (c, a)):
+        t = np.clip((p - s) @ (e - s) / ((e - s) @ (e - s)), 0.0, 1.0)
+        x = s + t * (e - s)
+        if best is None or (x - p) @ (x - p) < (best - p) @ (best - p):
+            best = x
+    return best
+
+
+@pytest.mark.parametrize("mesh", ["sphere", "cube", "plane"])
+def test_closest_point_against_independent_method(mesh):
+    """Distances of the device query and of the oracle against a closest-point routine with no region logic."""
+    v, t = {"sphere": lambda: icosphere(1.0, 1), "cube": lambda: unit_cube_mesh(centered=True),
+            "plane": lambda: plane_mesh(0.8)}[mesh]()
+    hm, om = HostMesh(v, t), OracleMesh(v, t)
+    rng = np.random.default_rng(11)
+    pts = (rng.normal(size=(3000, 3)) * 0.8).astype(np.float32)
+    tri = np.asarray(v, np.float64)[np.asarray(t)]
+    cp, _, _ = hm.query(pts)
+    for i, p in enumerate(pts.astype(np.float64)):
+        exact = min(np.linalg.norm(_closest_point_independent(p, *tr) - p) for tr in tri)
+        assert abs(np.linalg.norm(cp[i] - p) - exact) < 2e-6 * (1 + exact), i
+        _, _, _, _, d2 = om.query(p)
+        assert abs(np.sqrt(d2) - exact) < 1e-9 * (1 + exact), i
