@@ -110,7 +110,10 @@ int mpm_load_state(void *handle, int64_t n, const float *x, const float *v, cons
 /* Runtime options (no reference counterpart; tuning and measurement of this backend). */
 enum {
     MPM_OPT_USE_GRAPH = 1,     /* 1 (default): replay a captured CUDA graph per substep */
-    MPM_OPT_KERNEL_TIMING = 2  /* 1: record CUDA events around each kernel of every substep */
+    MPM_OPT_KERNEL_TIMING = 2, /* 1: record CUDA events between the kernel groups of every substep (event nodes
+                                  in the captured graph); each substep then waits for its own completion */
+    MPM_OPT_SORT_INTERVAL = 3  /* N (default 4): after every N substeps the particle storage is reordered into
+                                  grid-block order (ids travel along, so host order is unchanged); 0: never */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

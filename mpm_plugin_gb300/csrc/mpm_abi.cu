@@ -24,13 +24,43 @@ using namespace mpm;
 namespace {
 
 constexpr double kCFL = 0.4;  // warp/solver.py:19
-constexpr int kFields = 28;                 // x3 v3 C9 F9 Jp mat emitter id
+constexpr int kFields = 34;                 // x3 v3 C9 F9 Jp tau6 mat emitter id
 
 thread_local std::string g_last_error;
 
 struct Status {
     int code = MPM_OK;
     std::string msg;
+};
+
+// Instantiated substep graphs keyed by what the kernels' arguments depend on; two entries, so the two
+// particle arenas that the reorder alternates between both keep their graph.
+struct GraphCache {
+    static constexpr int kKey = 6;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int64_t key[2][kKey] = {};
+    int last = 0;
+    cudaGraphExec_t find(const int64_t* k) {
+        for (int i = 0; i < 2; ++i)
+            if (exec[i] && std::memcmp(key[i], k, sizeof(int64_t) * kKey) == 0) {
+                last = i;
+                return exec[i];
+            }
+        return nullptr;
+    }
+    int victim() const { return exec[0] == nullptr ? 0 : exec[1] == nullptr ? 1 : 1 - last; }
+    void put(int i, const int64_t* k, cudaGraphExec_t g) {
+        if (exec[i]) cudaGraphExecDestroy(exec[i]);
+        exec[i] = g;
+        std::memcpy(key[i], k, sizeof(int64_t) * kKey);
+        last = i;
+    }
+    void clear() {
+        for (auto& e : exec) {
+            if (e) cudaGraphExecDestroy(e);
+            e = nullptr;
+        }
+    }
 };
 
 struct Handle {
@@ -85,11 +115,20 @@ struct Handle {
     int64_t launches = 0;       // kernels of this library launched so far (graph replays count their kernels)
     int64_t graph_kernels = 0;  // kernels in the captured substep graph
 
+    SortScratch ss{};            // counting sort of the particles by grid node
+    int64_t ss_cap = 0;          // particle capacity the per-particle sort arrays were sized for
+    int32_t* ss_scan = nullptr;  // scan scratch over the grid's node counts
+    int64_t ss_scan_cap = 0;
+    int sort_interval = 4;       // reorder the particles by grid node after every this many substeps (0: never)
+    int64_t since_sort = 0;
+
     bool use_graph = true;
-    cudaGraphExec_t graph = nullptr;
-    int64_t graph_key[6] = {-1, -1, -1, -1, -1, -1};
+    GraphCache graphs;           // the substep graph, one per particle arena (the reorder alternates two)
 
     bool timing = false;
+    cudaEvent_t tev[5] = {};     // event nodes of the timed graph
+    GraphCache tgraphs;          // the substep graph with timing events
+    cudaEvent_t perm_ev[2] = {};
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::vector<cudaEvent_t>> ev_pending;  // per substep: 4 events around p2g / grid / g2p
     double t_ms[4] = {0, 0, 0, 0};
@@ -140,18 +179,18 @@ Particles bind_arena(void* base, int64_t cap, int64_t n) {
     for (int e = 0; e < 9; ++e) P.C[e] = f + (int64_t)(6 + e) * cap;
     for (int e = 0; e < 9; ++e) P.F[e] = f + (int64_t)(15 + e) * cap;
     P.Jp = f + (int64_t)24 * cap;
-    P.mat = reinterpret_cast<int32_t*>(f + (int64_t)25 * cap);
-    P.emitter = reinterpret_cast<int32_t*>(f + (int64_t)26 * cap);
-    P.id = reinterpret_cast<int32_t*>(f + (int64_t)27 * cap);
+    for (int e = 0; e < 6; ++e) P.tau[e] = f + (int64_t)(25 + e) * cap;
+    P.mat = reinterpret_cast<int32_t*>(f + (int64_t)31 * cap);
+    P.emitter = reinterpret_cast<int32_t*>(f + (int64_t)32 * cap);
+    P.id = reinterpret_cast<int32_t*>(f + (int64_t)33 * cap);
     P.n = n;
     P.cap = cap;
     return P;
 }
 
 void invalidate_graph(Handle* h) {
-    if (h->graph) cudaGraphExecDestroy(h->graph);
-    h->graph = nullptr;
-    h->graph_key[0] = -1;
+    h->graphs.clear();
+    h->tgraphs.clear();
 }
 
 Status ensure_capacity(Handle* h, int64_t need) {
@@ -252,43 +291,132 @@ Status ensure_part_cand(Handle* h) {
     return {};
 }
 
+// Per-particle sort arrays (key, rank, order), sized for the particle capacity.
+Status ensure_sort_scratch(Handle* h) {
+    if (h->ss_cap >= h->P.cap) return {};
+    CK(cudaStreamSynchronize(h->stream));
+    cudaFree(h->ss.key);
+    h->ss.key = h->ss.rank = h->ss.order = nullptr;
+    h->ss_cap = 0;
+    const int64_t cap = h->P.cap;
+    if (cudaMalloc(&h->ss.key, sizeof(int32_t) * 3 * (size_t)cap) != cudaSuccess) {
+        cudaGetLastError();
+        h->ss.key = nullptr;
+        return {MPM_ERR_MEMORY, "device allocation of the particle sort arrays failed"};
+    }
+    h->ss.rank = h->ss.key + cap;
+    h->ss.order = h->ss.key + 2 * cap;
+    h->ss_cap = cap;
+    return {};
+}
+
+// Reorders the particle arena by the grid node of each particle's stencil base (counting sort, then
+// dst[i] = src[order[i]] for every field), so that neighbouring threads of the next substeps' P2G and G2P
+// touch neighbouring grid nodes. Particle ids travel with the particles, so host order is unchanged.
+Status reorder_particles(Handle* h) {
+    if (h->P.n == 0) return {};
+    TRY(ensure_sort_scratch(h));
+    if (!h->spare_arena) {
+        if (cudaMalloc(&h->spare_arena, (size_t)h->P.cap * kFields * 4) != cudaSuccess) {
+            cudaGetLastError();
+            h->spare_arena = nullptr;
+            return {MPM_ERR_MEMORY, "device allocation of particle storage failed"};
+        }
+    }
+    Particles dst = bind_arena(h->spare_arena, h->P.cap, h->P.n);
+    if (h->timing) {
+        if (!h->perm_ev[0])
+            for (auto& e : h->perm_ev) CK(cudaEventCreate(&e));
+        CK(cudaEventRecord(h->perm_ev[0], h->stream));
+    }
+    launch_sort(h->stream, h->P, h->g, h->ss, h->grid_nodes, h->ss_scan, h->ss_scan_cap);
+    launch_permute(h->stream, h->P, dst, h->ss.order);
+    CK(cudaGetLastError());
+    h->launches += 6;  // keys, three-pass scan, order, permutation
+    if (h->timing) {
+        CK(cudaEventRecord(h->perm_ev[1], h->stream));
+        CK(cudaEventSynchronize(h->perm_ev[1]));
+        float t = 0;
+        cudaEventElapsedTime(&t, h->perm_ev[0], h->perm_ev[1]);
+        h->t_ms[3] += t;
+    }
+    std::swap(h->arena, h->spare_arena);
+    h->P = dst;
+    return {};
+}
+
+void accumulate_times(Handle* h, const cudaEvent_t* ev) {  // ev: | clear | P2G | grid + colliders | G2P + projection |
+    const int slot_of[4] = {3, 0, 1, 2};
+    for (int k = 0; k < 4; ++k) {
+        float t = 0;
+        cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
+        h->t_ms[slot_of[k]] += t;
+        h->t_launches[slot_of[k]] += 1;
+    }
+}
+
+Status capture_graph(Handle* h, const SubstepArgs& a, cudaEvent_t* ev, cudaGraphExec_t* out) {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    launch_substep(h->stream, a, ev, true);
+    cudaError_t e0 = cudaGetLastError();
+    cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+    CK(e0);
+    CK(e);
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(e);
+    return {};
+}
+
 Status run_substep(Handle* h) {
     TRY(ensure_part_cand(h));
     SubstepArgs a = substep_args(h);
     const int kernels = substep_kernel_count(a);
-    if (h->timing) {
-        std::vector<cudaEvent_t> ev(5);
-        for (auto& e : ev) e = take_event(h);
-        launch_substep(h->stream, a, ev.data());
-        CK(cudaGetLastError());
-        h->ev_pending.push_back(ev);
-        h->launches += kernels;
-        return {};
-    }
-    if (!h->use_graph) {
-        launch_substep(h->stream, a, nullptr);
-        CK(cudaGetLastError());
-        h->launches += kernels;
-        return {};
-    }
+    h->launches += kernels;
     int64_t key[6] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena, (int64_t)(intptr_t)h->d_poses,
                       (int64_t)(intptr_t)h->wl.part_cand};
-    if (!h->graph || std::memcmp(key, h->graph_key, sizeof key) != 0) {
-        invalidate_graph(h);
-        cudaGraph_t graph;
-        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-        launch_substep(h->stream, a, nullptr);
-        cudaError_t e0 = cudaGetLastError();
-        cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
-        CK(e0);
-        CK(e);
-        e = cudaGraphInstantiate(&h->graph, graph, 0);
-        cudaGraphDestroy(graph);
-        CK(e);
-        std::memcpy(h->graph_key, key, sizeof key);
+    if (!h->use_graph) {
+        if (h->timing) {
+            std::vector<cudaEvent_t> ev(5);
+            for (auto& e : ev) e = take_event(h);
+            launch_substep(h->stream, a, ev.data(), false);
+            h->ev_pending.push_back(ev);
+        } else {
+            launch_substep(h->stream, a, nullptr, false);
+        }
+        CK(cudaGetLastError());
+        return {};
     }
-    CK(cudaGraphLaunch(h->graph, h->stream));
-    h->launches += kernels;
+    if (h->timing) {  // the same graph with event nodes; read them before the next replay overwrites them
+        if (!h->tev[0])
+            for (auto& e : h->tev) CK(cudaEventCreate(&e));
+        cudaGraphExec_t g = h->tgraphs.find(key);
+        if (!g) {
+            TRY(capture_graph(h, a, h->tev, &g));
+            h->tgraphs.put(h->tgraphs.victim(), key, g);
+        }
+        CK(cudaGraphLaunch(g, h->stream));
+        CK(cudaEventSynchronize(h->tev[4]));
+        accumulate_times(h, h->tev);
+        return {};
+    }
+    cudaGraphExec_t g = h->graphs.find(key);
+    if (!g) {
+        TRY(capture_graph(h, a, nullptr, &g));
+        h->graphs.put(h->graphs.victim(), key, g);
+    }
+    CK(cudaGraphLaunch(g, h->stream));
+    return {};
+}
+
+// One substep, then the reorder into bin order when it is due.
+Status substep_and_sort(Handle* h) {
+    TRY(run_substep(h));
+    if (h->sort_interval > 0 && ++h->since_sort >= h->sort_interval) {
+        TRY(reorder_particles(h));
+        h->since_sort = 0;
+    }
     return {};
 }
 
@@ -489,7 +617,7 @@ Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
     TRY(set_step(h, dt, 0.0, frame_dt, steps));
     TRY(ensure_sdf(h));
     TRY(prepare_poses(h, steps, 0.0, frame_dt));
-    for (int k = 0; k < steps; ++k) TRY(run_substep(h));
+    for (int k = 0; k < steps; ++k) TRY(substep_and_sort(h));
     int32_t removed = 0;
     TRY(remove_escaped(h, &removed));
     CK(cudaStreamSynchronize(h->stream));
@@ -524,7 +652,8 @@ Status upload_particles(Handle* h, int64_t off, int64_t n, const float* x, const
     const int32_t* de = (const int32_t*)put(emitter, (size_t)n * 4);
     CK(cudaGetLastError());
     launch_state_in(h->stream, h->P, off, n, dx_, dv, dC, dF, dJ, dm, de);
-    h->launches += 1;
+    launch_particle_stress(h->stream, h->P, off, n, h->d_mats, h->d_counters + 1);
+    h->launches += 2;
     CK(cudaGetLastError());
     return {};
 }
@@ -617,6 +746,11 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
         CK(cudaMalloc(&h->wl.counts, sizeof(unsigned int) * 4));
         CK(cudaMemset(h->wl.counts, 0, sizeof(unsigned int) * 4));
         CK(cudaMalloc(&h->wl.node_cand, sizeof(int32_t) * (size_t)h->grid_nodes));
+        // sort by grid node: one count and start per node, plus the key of stencils outside the grid
+        CK(cudaMalloc(&h->ss.count, sizeof(unsigned int) * (size_t)(h->grid_nodes + 1)));
+        CK(cudaMalloc(&h->ss.start, sizeof(int32_t) * (size_t)(h->grid_nodes + 1)));
+        h->ss_scan_cap = scan_tile_count(h->grid_nodes + 1) + 1;
+        CK(cudaMalloc(&h->ss_scan, sizeof(int32_t) * (size_t)(h->ss_scan_cap + 2)));
     }
     CK(cudaMalloc(&h->d_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
     CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * (2 + kMaxMaterials)));
@@ -633,6 +767,10 @@ void destroy(Handle* h) {
     for (auto& v : h->ev_pending)
         for (auto e : v) cudaEventDestroy(e);
     for (auto e : h->ev_pool) cudaEventDestroy(e);
+    for (auto e : h->tev)
+        if (e) cudaEventDestroy(e);
+    for (auto e : h->perm_ev)
+        if (e) cudaEventDestroy(e);
     free_colliders(h);
     cudaFree(h->arena);
     cudaFree(h->spare_arena);
@@ -652,6 +790,10 @@ void destroy(Handle* h) {
     cudaFree(h->wl.counts);
     cudaFree(h->wl.node_cand);
     cudaFree(h->wl.part_cand);
+    cudaFree(h->ss.key);
+    cudaFree(h->ss.count);
+    cudaFree(h->ss.start);
+    cudaFree(h->ss_scan);
     cudaFree(h->stage);
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->stream) cudaStreamDestroy(h->stream);
@@ -789,7 +931,7 @@ int mpm_substep(void* handle, double dt, double s, double frame_dt) {
         TRY(set_step(h, dt, s, frame_dt, 0));
         TRY(ensure_sdf(h));
         TRY(prepare_poses(h, 0, s, frame_dt));
-        return run_substep(h);
+        return substep_and_sort(h);
     };
     return finish(h, run());
 }
@@ -870,6 +1012,11 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
         case MPM_OPT_KERNEL_TIMING:
             h->timing = value != 0;
             return MPM_OK;
+        case MPM_OPT_SORT_INTERVAL:
+            if (value < 0 || value > (1 << 30)) return finish(h, {MPM_ERR_VALUE, "sort interval out of range"});
+            h->sort_interval = (int)value;
+            h->since_sort = 0;
+            return MPM_OK;
         default:
             return finish(h, {MPM_ERR_VALUE, "unknown option"});
     }
@@ -893,14 +1040,8 @@ int mpm_kernel_times(void* handle, int32_t n_slots, float* ms, int64_t* launches
     HANDLE_OR_FAIL(handle);
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
-    for (auto& ev : h->ev_pending) {  // ev: | clear | P2G | grid update + colliders | G2P + projection |
-        const int slot_of[4] = {3, 0, 1, 2};
-        for (int k = 0; k < 4; ++k) {
-            float t = 0;
-            cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
-            h->t_ms[slot_of[k]] += t;
-            h->t_launches[slot_of[k]] += 1;
-        }
+    for (auto& ev : h->ev_pending) {
+        accumulate_times(h, ev.data());
         for (auto x : ev) h->ev_pool.push_back(x);
     }
     h->ev_pending.clear();

@@ -257,26 +257,40 @@ MPM_HD void sym_from_diag(const float U[3][3], const float g[3], float tau[3][3]
         for (int j = 0; j < 3; ++j) tau[i][j] = U[i][0] * g[0] * U[j][0] + U[i][1] * g[1] * U[j][1] + U[i][2] * g[2] * U[j][2];
 }
 
-MPM_HD void fixed_corotated_tau(const float F[3][3], float mu, float lam, float tau[3][3], unsigned int* fp64) {
-    float U[3][3], sig[3], d[3], V[3][3];
-    svd3(F, U, sig, d, V, fp64);
+// Principal Kirchhoff stresses of the fixed-corotated energy (kernels.py:30-38) from the singular values sig
+// and their deviations d = sig - 1: 2 mu (sig - 1) sig + lam (J - 1) J.
+MPM_HD void corotated_principal(float mu, float lam, const float sig[3], const float d[3], float g[3]) {
     float Jm1 = jm1(d);
     float iso = lam * (1.0f + Jm1) * Jm1;
-    float g[3] = {2.0f * mu * d[0] * sig[0] + iso, 2.0f * mu * d[1] * sig[1] + iso, 2.0f * mu * d[2] * sig[2] + iso};
-    sym_from_diag(U, g, tau);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] = 2.0f * mu * d[i] * sig[i] + iso;
 }
 
 MPM_HD float safe_log_dev(float s, float d) {  // log(max(s, 1e-4)) from d = s - 1 (kernels.py:41-43)
     return s > 1.0e-4f ? log1pf(d) : logf(1.0e-4f);
 }
 
-MPM_HD void hencky_tau(const float F[3][3], float mu, float lam, float tau[3][3], unsigned int* fp64) {
-    float U[3][3], sig[3], d[3], V[3][3];
-    svd3(F, U, sig, d, V, fp64);
+// Principal Kirchhoff stresses of the Hencky (logarithmic) energy (kernels.py:51-60): 2 mu e + lam tr(e).
+MPM_HD void hencky_principal(float mu, float lam, const float sig[3], const float d[3], float g[3]) {
     float e0 = safe_log_dev(sig[0], d[0]), e1 = safe_log_dev(sig[1], d[1]), e2 = safe_log_dev(sig[2], d[2]);
     float tr = e0 + e1 + e2;
     float two_mu = 2.0f * mu;
-    float g[3] = {two_mu * e0 + lam * tr, two_mu * e1 + lam * tr, two_mu * e2 + lam * tr};
+    g[0] = two_mu * e0 + lam * tr;
+    g[1] = two_mu * e1 + lam * tr;
+    g[2] = two_mu * e2 + lam * tr;
+}
+
+MPM_HD void fixed_corotated_tau(const float F[3][3], float mu, float lam, float tau[3][3], unsigned int* fp64) {
+    float U[3][3], sig[3], d[3], V[3][3], g[3];
+    svd3(F, U, sig, d, V, fp64);
+    corotated_principal(mu, lam, sig, d, g);
+    sym_from_diag(U, g, tau);
+}
+
+MPM_HD void hencky_tau(const float F[3][3], float mu, float lam, float tau[3][3], unsigned int* fp64) {
+    float U[3][3], sig[3], d[3], V[3][3], g[3];
+    svd3(F, U, sig, d, V, fp64);
+    hencky_principal(mu, lam, sig, d, g);
     sym_from_diag(U, g, tau);
 }
 

@@ -35,9 +35,19 @@ struct SubstepArgs {
 void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, ColliderPose* poses, int steps,
                            float s_given, float inv_frame_dt);
 // One substep: step counters, clear of the previous blocks, P2G, grid update, collider contact, G2P,
-// particle projection. With ev (5 events), records ev[0..4] around: clear | P2G | grid | G2P.
-void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev);
+// particle projection. With ev (5 events), records ev[0..4] around: clear | P2G | grid | G2P (as event
+// nodes when `capturing`).
+void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool capturing);
 int substep_kernel_count(const SubstepArgs& a);
+// Counting sort of the particles by the grid node of their stencil base: fills ss.order (scan_tmp: scan
+// scratch of scan_cap + 2 entries, at least scan_tile_count(n_nodes + 1) + 1).
+void launch_sort(cudaStream_t st, const Particles& P, const GridDesc& g, const SortScratch& ss, int64_t n_nodes,
+                 int32_t* scan_tmp, int64_t scan_cap);
+// Kirchhoff stress of the particles [off, off + n) from their F and Jp.
+void launch_particle_stress(cudaStream_t st, const Particles& P, int64_t off, int64_t n, const Material* mats,
+                            unsigned int* fp64);
+// dst[i] = src[order[i]] for every particle field (reorder into bin order).
+void launch_permute(cudaStream_t st, const Particles& src, const Particles& dst, const int32_t* order);
 
 constexpr int kSdfMaxCandidates = 128;
 // Narrow-band voxel grid of one collider: classify every voxel (cells[v].y: candidate count, kSdfFar or

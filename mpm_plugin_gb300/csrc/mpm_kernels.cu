@@ -6,8 +6,10 @@
 // for every substep of an advance.
 #include <cuda_runtime.h>
 
-#include "mpm_substep.cuh"
+#include <algorithm>
+
 #include "mpm_internal.h"
+#include "mpm_substep.cuh"
 
 namespace mpm {
 
@@ -49,7 +51,7 @@ __global__ void __launch_bounds__(256) k_clear_blocks(const StepParams* __restri
                                                       float4* __restrict__ grid) {
     const unsigned int prev = (sp->seq - 1u) & 1u;
     const unsigned int n = wl.counts[prev];
-    const int32_t* __restrict__ list = wl.blocks[prev];
+    const int32_t* __restrict__ list = active_blocks(wl, prev);
     for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
         const int64_t b = list[i];
         grid[b * 64 + (threadIdx.x & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -67,13 +69,136 @@ __device__ __forceinline__ void warp_append(int32_t* __restrict__ list, unsigned
     list[base + __popc(mask & ((1u << lane) - 1u))] = v;
 }
 
+// P2G with warp-level aggregation: lanes whose stencils start at the same grid node (neighbours in the
+// particle order after the reorder by grid node) form a segment; each of the 27 x 4 contributions is summed
+// over the segment with shuffles (after round r a lane holds the sum of the next 2^r lanes of its segment)
+// and only the segment's first lane issues the 16-byte reduction, so a cell of ~8 particles costs one
+// reduction per node instead of eight. Lanes past the end or with a stencil outside the grid are
+// single-lane segments that add nothing.
 __global__ void __launch_bounds__(256) k_p2g_scatter(Particles P, const Material* __restrict__ mats, GridDesc g,
                                                      const StepParams* __restrict__ sp, float4* __restrict__ grid,
-                                                     unsigned int* fp64_lanes, WorkLists wl) {
+                                                     WorkLists wl) {
+    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = (int)(threadIdx.x & 31u);
+    if ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= P.n) return;  // whole warp past the end
+    P2gTerms t;
+    const bool valid = p < P.n && p2g_terms(P, p, mats, g, sp->dt, t);
+    const int64_t key = valid ? node_index(g, t.base[0], t.base[1], t.base[2]) : -1 - (int64_t)lane;
+    const int64_t key_prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const int64_t key_next = __shfl_down_sync(0xffffffffu, key, 1);
+    const bool first = lane == 0 || key_prev != key;
+    const bool last = lane == 31 || key_next != key;
+    const unsigned int ends = __ballot_sync(0xffffffffu, last);
+    const int tail = __ffs(ends >> lane) - 1;  // lanes after this one in its segment
+    const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned int)tail);
+    const bool leader = valid && first;
+    if (leader) {
+        const unsigned int cur = sp->seq & 1u;
+        mark_stencil_blocks(g, t.base, wl.block_flag, active_blocks(wl, cur), &wl.counts[cur]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float val[4] = {0.f, 0.f, 0.f, 0.f};
+                if (valid) p2g_node(t, g, i, j, k, val);
+#pragma unroll
+                for (int s = 1; s < 32; s <<= 1) {
+                    if (s <= span) {  // warp-uniform
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) {
+                            const float o = __shfl_down_sync(0xffffffffu, val[c], s);
+                            if (s <= tail) val[c] += o;
+                        }
+                    }
+                }
+                if (leader) grid_add(&grid[node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k)], val[0], val[1],
+                                     val[2], val[3]);
+            }
+}
+
+// exclusive scan of int32 in three passes: per-CTA sums, one CTA over the sums, per-CTA scan + offset
+constexpr int kScanTile = 1024;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int* sh_warp, int* total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh_warp[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int s = lane < (int)(blockDim.x >> 5) ? sh_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sh_warp[lane] = s;
+    }
+    __syncthreads();
+    int incl = x + (wid > 0 ? sh_warp[wid - 1] : 0);
+    if (total) *total = sh_warp[(blockDim.x >> 5) - 1];
+    return incl - v;
+}
+
+// ------------------------------------------------------------------------------------------------------
+// Periodic reorder by grid node: keys and ranks, (exclusive scan of the counts), order, permutation.
+// ------------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_sort_keys(Particles P, GridDesc g, SortScratch ss, int64_t n_nodes) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P.n) return;
-    const unsigned int cur = sp->seq & 1u;
-    p2g_particle(P, p, mats, g, sp->dt, grid, fp64_lanes, wl.block_flag, wl.blocks[cur], &wl.counts[cur]);
+    int base[3];
+    float fx;
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) inside &= stencil_axis((P.x[a][p] - g.origin[a]) * g.inv_dx, g.dims[a], &base[a], &fx);
+    const int32_t key = (int32_t)(inside ? node_index(g, base[0], base[1], base[2]) : n_nodes);
+    ss.key[p] = key;
+    ss.rank[p] = (int32_t)atomicAdd(&ss.count[key], 1u);
+}
+
+__global__ void __launch_bounds__(256) k_sort_scatter(int64_t n, SortScratch ss) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    ss.order[ss.start[ss.key[p]] + ss.rank[p]] = (int32_t)p;
+}
+
+// dst[i] = src[order[i]] for every field: neighbouring threads of P2G and G2P then touch neighbouring grid
+// nodes, so their reductions and gathers hit the same cache lines.
+__global__ void k_permute(Particles src, Particles dst, const int32_t* __restrict__ order) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= src.n) return;
+    const int64_t q = order[i];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        dst.x[a][i] = src.x[a][q];
+        dst.v[a][i] = src.v[a][q];
+    }
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+        dst.C[e][i] = src.C[e][q];
+        dst.F[e][i] = src.F[e][q];
+    }
+    dst.Jp[i] = src.Jp[q];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) dst.tau[e][i] = src.tau[e][q];
+    dst.mat[i] = src.mat[q];
+    dst.emitter[i] = src.emitter[q];
+    dst.id[i] = src.id[q];
+}
+
+// Stress of the particles [off, off + n) from their F and Jp (particles entering the arena).
+__global__ void k_particle_stress(Particles P, int64_t off, int64_t n, const Material* __restrict__ mats,
+                                  unsigned int* fp64_lanes) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    particle_stress(P, off + i, mats, fp64_lanes);
 }
 
 // Grid update over the active blocks, four 4x4x4 blocks per 256-thread CTA. Nodes inside a collider's
@@ -86,7 +211,7 @@ __global__ void __launch_bounds__(256) k_grid_update(GridDesc g, float4* __restr
     cd.poses += sp->pose_base;
     const int l = threadIdx.x & 63;
     for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
-        const int64_t b = wl.blocks[cur][i];
+        const int64_t b = active_blocks(wl, cur)[i];
         const int bk = (int)(b % g.nb[2]);
         const int bj = (int)((b / g.nb[2]) % g.nb[1]);
         const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
@@ -233,38 +358,13 @@ __global__ void k_compact(Particles src, Particles dst, const int32_t* __restric
         dst.F[e][q] = src.F[e][p];
     }
     dst.Jp[q] = src.Jp[p];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) dst.tau[e][q] = src.tau[e][p];
     dst.mat[q] = src.mat[p];
     dst.emitter[q] = src.emitter[p];
     dst.id[q] = new_id[src.id[p]];
 }
 
-// exclusive scan of int32 in three passes: per-CTA sums, one CTA over the sums, per-CTA scan + offset
-constexpr int kScanTile = 1024;
-
-__device__ __forceinline__ int block_exclusive_scan(int v, int* sh_warp, int* total) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) sh_warp[wid] = x;
-    __syncthreads();
-    if (wid == 0) {
-        int s = lane < (int)(blockDim.x >> 5) ? sh_warp[lane] : 0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        sh_warp[lane] = s;
-    }
-    __syncthreads();
-    int incl = x + (wid > 0 ? sh_warp[wid - 1] : 0);
-    if (total) *total = sh_warp[(blockDim.x >> 5) - 1];
-    return incl - v;
-}
 
 __global__ void k_scan_tiles(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ tile_sums) {
     __shared__ int sh[32];
@@ -392,21 +492,45 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
     k_collider_poses<<<blocks_for(total, 128), 128, 0, st>>>(cols, n_col, poses, steps, s_given, inv_frame_dt);
 }
 
-void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev) {
+void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool capturing) {
     const unsigned int list_ctas = kListCtas;
-    if (ev) cudaEventRecord(ev[0], st);
+    // while a graph is being captured the records become event nodes that fire on every replay
+    auto mark = [&](int i) {
+        if (ev) cudaEventRecordWithFlags(ev[i], st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+    };
+    mark(0);
     k_step_begin<<<1, 1, 0, st>>>(a.sp, a.wl.counts, a.cd.n_col);
     k_clear_blocks<<<list_ctas, 256, 0, st>>>(a.sp, a.wl, a.grid);
-    if (ev) cudaEventRecord(ev[1], st);
-    if (a.P.n > 0) k_p2g_scatter<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.fp64, a.wl);
-    if (ev) cudaEventRecord(ev[2], st);
+    mark(1);
+    if (a.P.n > 0) k_p2g_scatter<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.wl);
+    mark(2);
     k_grid_update<<<list_ctas, 256, 0, st>>>(a.g, a.grid, a.sp, a.wl, a.cd);
     if (a.cd.n_col > 0) k_grid_colliders<<<list_ctas, 128, 0, st>>>(a.g, a.grid, a.sp, a.wl, a.cd);
-    if (ev) cudaEventRecord(ev[3], st);
-    if (a.P.n > 0)
-        k_g2p<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.fp64, a.wl, a.cd);
+    mark(3);
+    if (a.P.n > 0) k_g2p<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.fp64, a.wl, a.cd);
     if (a.cd.n_col > 0) k_project_particles<<<list_ctas, 128, 0, st>>>(a.P, a.g, a.sp, a.wl, a.cd);
-    if (ev) cudaEventRecord(ev[4], st);
+    mark(4);
+}
+
+void launch_sort(cudaStream_t st, const Particles& P, const GridDesc& g, const SortScratch& ss, int64_t n_nodes,
+                 int32_t* scan_tmp, int64_t scan_cap) {
+    if (P.n == 0) return;
+    cudaMemsetAsync(ss.count, 0, sizeof(unsigned int) * (size_t)(n_nodes + 1), st);
+    k_sort_keys<<<blocks_for(P.n, 256), 256, 0, st>>>(P, g, ss, n_nodes);
+    launch_exclusive_scan(st, reinterpret_cast<const int32_t*>(ss.count), n_nodes + 1, ss.start, scan_tmp,
+                          scan_tmp + scan_cap);
+    k_sort_scatter<<<blocks_for(P.n, 256), 256, 0, st>>>(P.n, ss);
+}
+
+void launch_particle_stress(cudaStream_t st, const Particles& P, int64_t off, int64_t n, const Material* mats,
+                            unsigned int* fp64) {
+    if (n <= 0) return;
+    k_particle_stress<<<blocks_for(n, 128), 128, 0, st>>>(P, off, n, mats, fp64);
+}
+
+void launch_permute(cudaStream_t st, const Particles& src, const Particles& dst, const int32_t* order) {
+    if (src.n == 0) return;
+    k_permute<<<blocks_for(src.n, 256), 256, 0, st>>>(src, dst, order);
 }
 
 void launch_sdf_classify(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris,

@@ -130,60 +130,136 @@ MPM_HD void mark_block(int64_t b, unsigned int* __restrict__ flags, int32_t* __r
 #endif
 }
 
-// flags / list / count may be null (no active-block bookkeeping).
-MPM_HD void p2g_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         float4* __restrict__ grid, unsigned int* fp64, unsigned int* __restrict__ flags = nullptr,
-                         int32_t* __restrict__ list = nullptr, unsigned int* __restrict__ count = nullptr) {
-    const Material m = mats[P.mat[p]];
-    float F[3][3], tau[3][3];
-    load_mat3(P.F, p, F);
+// P2G of one particle into `sink` (sink.begin(base) once, then sink.add(i, j, k, mv x, y, z, m) per node);
+// false for a particle whose stencil leaves the padded grid (it scatters nothing).
+// Kirchhoff stress of one particle from the SVD of its deformation gradient, F = U diag(sig) V^T with
+// d = sig - 1 (kernels.py:117-124): Hencky for von Mises and Drucker-Prager, fixed-corotated with snow
+// hardening exp(xi (1 - Jp)) capped at max_hardening, plain fixed-corotated otherwise. Stored as the six
+// entries xx, yy, zz, xy, xz, yz of the symmetric tensor.
+MPM_HD void tau_from_svd(const Material& m, float jp, const float U[3][3], const float sig[3], const float d[3],
+                         float tau6[6]) {
+    float g[3], tau[3][3];
     if (m.model == 1 || m.model == 2) {
-        hencky_tau(F, m.mu, m.lam, tau, fp64);
+        hencky_principal(m.mu, m.lam, sig, d, g);
     } else if (m.model == 3) {
-        float h = fminf(expf(m.hardening * (1.0f - P.Jp[p])), m.max_hardening);
-        fixed_corotated_tau(F, m.mu * h, m.lam * h, tau, fp64);
+        float h = fminf(expf(m.hardening * (1.0f - jp)), m.max_hardening);
+        corotated_principal(m.mu * h, m.lam * h, sig, d, g);
     } else {
-        fixed_corotated_tau(F, m.mu, m.lam, tau, fp64);
+        corotated_principal(m.mu, m.lam, sig, d, g);
     }
-    const float pm = m.p_mass;
+    sym_from_diag(U, g, tau);
+    tau6[0] = tau[0][0];
+    tau6[1] = tau[1][1];
+    tau6[2] = tau[2][2];
+    tau6[3] = tau[0][1];
+    tau6[4] = tau[0][2];
+    tau6[5] = tau[1][2];
+}
+
+// The stress of particle p from its stored F and Jp, for particles that enter the arena (added or loaded).
+MPM_HD void particle_stress(const Particles& P, int64_t p, const Material* __restrict__ mats, unsigned int* fp64) {
+    const Material m = mats[P.mat[p]];
+    float F[3][3], U[3][3], sig[3], d[3], V[3][3], t[6];
+    load_mat3(P.F, p, F);
+    svd3(F, U, sig, d, V, fp64);
+    tau_from_svd(m, P.Jp[p], U, sig, d, t);
+#pragma unroll
+    for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
+}
+
+// Per-particle terms of P2G (kernels.py:93-140): stencil base and weights, p_mass v and the affine matrix
+// A = -dt p_vol 4 inv_dx^2 tau + p_mass C. tau is the particle's stored Kirchhoff stress, computed from F at
+// the end of the previous G2P (or when the particle entered), so P2G itself decomposes nothing.
+struct P2gTerms {
+    int base[3];
+    float fx[3], w[3][3], mv[3], A[3][3], pm;
+};
+
+// False when the stencil leaves the grid (the particle scatters nothing).
+MPM_HD bool p2g_terms(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
+                      P2gTerms& t) {
+    const float t0 = P.tau[0][p], t1 = P.tau[1][p], t2 = P.tau[2][p], t3 = P.tau[3][p], t4 = P.tau[4][p],
+                t5 = P.tau[5][p];
+    const float tau[3][3] = {{t0, t3, t4}, {t3, t1, t5}, {t4, t5, t2}};
+    t.pm = mats[P.mat[p]].p_mass;
     const float k_stress = -dt * g.p_vol * 4.0f * g.inv_dx * g.inv_dx;
-    float A[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) A[i][j] = k_stress * tau[i][j] + pm * P.C[i * 3 + j][p];
-    int base[3];
-    float fx[3], w[3][3], mv[3];
+        for (int j = 0; j < 3; ++j) t.A[i][j] = k_stress * tau[i][j] + t.pm * P.C[i * 3 + j][p];
     bool inside = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         float xp = (P.x[a][p] - g.origin[a]) * g.inv_dx;
-        inside &= stencil_axis(xp, g.dims[a], &base[a], &fx[a]);
-        bspline_weights(fx[a], w[a]);
-        mv[a] = pm * P.v[a][p];
+        inside &= stencil_axis(xp, g.dims[a], &t.base[a], &t.fx[a]);
+        bspline_weights(t.fx[a], t.w[a]);
+        t.mv[a] = t.pm * P.v[a][p];
     }
-    if (!inside) return;
-    if (flags) {  // the 1 to 8 grid blocks this particle's 3x3x3 stencil touches
-        const int b0[3] = {base[0] >> 2, base[1] >> 2, base[2] >> 2};
-        const int b1[3] = {(base[0] + 2) >> 2, (base[1] + 2) >> 2, (base[2] + 2) >> 2};
-        for (int bi = b0[0]; bi <= b1[0]; ++bi)
-            for (int bj = b0[1]; bj <= b1[1]; ++bj)
-                for (int bk = b0[2]; bk <= b1[2]; ++bk)
-                    mark_block(((int64_t)bi * g.nb[1] + bj) * g.nb[2] + bk, flags, list, count);
-    }
+    return inside;
+}
+
+// Momentum (x, y, z) and mass the particle adds to stencil node (i, j, k), i, j, k in 0..2:
+// w (p_mass v + A (x_i - x_p)) and w p_mass.
+MPM_HD void p2g_node(const P2gTerms& t, const GridDesc& g, int i, int j, int k, float out[4]) {
+    float wt = t.w[0][i] * t.w[1][j] * t.w[2][k];
+    float dpos[3] = {((float)i - t.fx[0]) * g.dx, ((float)j - t.fx[1]) * g.dx, ((float)k - t.fx[2]) * g.dx};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) out[a] = wt * (t.mv[a] + (t.A[a][0] * dpos[0] + t.A[a][1] * dpos[1] + t.A[a][2] * dpos[2]));
+    out[3] = wt * t.pm;
+}
+
+// Lists the grid blocks a stencil at `base` touches (one to eight 4x4x4 blocks).
+MPM_HD void mark_stencil_blocks(const GridDesc& g, const int base[3], unsigned int* flags, int32_t* list,
+                                unsigned int* count) {
+    const int b0[3] = {base[0] >> 2, base[1] >> 2, base[2] >> 2};
+    const int b1[3] = {(base[0] + 2) >> 2, (base[1] + 2) >> 2, (base[2] + 2) >> 2};
+    for (int bi = b0[0]; bi <= b1[0]; ++bi)
+        for (int bj = b0[1]; bj <= b1[1]; ++bj)
+            for (int bk = b0[2]; bk <= b1[2]; ++bk)
+                mark_block(((int64_t)bi * g.nb[1] + bj) * g.nb[2] + bk, flags, list, count);
+}
+
+// P2G of one particle into `sink` (sink.begin(base), then sink.add(i, j, k, ...) per stencil node).
+template <class Sink>
+MPM_HD bool p2g_particle_into(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
+                              float dt, Sink& sink) {
+    P2gTerms t;
+    if (!p2g_terms(P, p, mats, g, dt, t)) return false;
+    sink.begin(t.base);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                float wt = w[0][i] * w[1][j] * w[2][k];
-                float dpos[3] = {((float)i - fx[0]) * g.dx, ((float)j - fx[1]) * g.dx, ((float)k - fx[2]) * g.dx};
-                float val[3];
-#pragma unroll
-                for (int a = 0; a < 3; ++a) val[a] = wt * (mv[a] + (A[a][0] * dpos[0] + A[a][1] * dpos[1] + A[a][2] * dpos[2]));
-                grid_add(&grid[node_index(g, base[0] + i, base[1] + j, base[2] + k)], val[0], val[1], val[2], wt * pm);
+                float val[4];
+                p2g_node(t, g, i, j, k, val);
+                sink.add(t.base[0] + i, t.base[1] + j, t.base[2] + k, val[0], val[1], val[2], val[3]);
             }
+    return true;
+}
+
+// Scatter straight into the global grid, optionally listing the grid blocks the stencil touches.
+struct GlobalSink {
+    const GridDesc* g;
+    float4* grid;
+    unsigned int* flags;
+    int32_t* list;
+    unsigned int* count;
+    MPM_HD void begin(const int base[3]) {
+        if (flags) mark_stencil_blocks(*g, base, flags, list, count);
+    }
+    MPM_HD void add(int i, int j, int k, float a, float b, float c, float d) {
+        grid_add(&grid[node_index(*g, i, j, k)], a, b, c, d);
+    }
+};
+
+// flags / list / count may be null (no active-block bookkeeping).
+MPM_HD void p2g_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
+                         float4* __restrict__ grid, unsigned int* __restrict__ flags = nullptr,
+                         int32_t* __restrict__ list = nullptr, unsigned int* __restrict__ count = nullptr) {
+    GlobalSink sink{&g, grid, flags, list, count};
+    p2g_particle_into(P, p, mats, g, dt, sink);
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -272,9 +348,11 @@ MPM_HD float4 load_node(const float4* p) {
 #endif
 }
 
-// Returns the new position in nx_out.
-MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3]) {
+// G2P of one particle gathering node velocities from `src` (src(i, j, k) -> float4); the new position goes
+// to nx_out.
+template <class Source>
+MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
+                              float dt, const Source& src, unsigned int* fp64, float nx_out[3]) {
     float xo[3];
     int base[3];
     float fx[3], w[3][3];
@@ -297,7 +375,7 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
             for (int k = 0; k < 3; ++k) {
                 float wt = w[0][i] * w[1][j] * w[2][k];
                 float dpos[3] = {((float)i - fx[0]) * g.dx, ((float)j - fx[1]) * g.dx, ((float)k - fx[2]) * g.dx};
-                float4 gv = load_node(&grid[node_index(g, base[0] + i, base[1] + j, base[2] + k)]);
+                float4 gv = src(base[0] + i, base[1] + j, base[2] + k);
                 float gva[3] = {gv.x, gv.y, gv.z};
                 float cw = cscale * wt;
 #pragma unroll
@@ -329,10 +407,15 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
         for (int j = 0; j < 3; ++j)
             Fn[i][j] = ((i == 0 ? 1.0f : 0.0f) + dt * nC[i][0]) * F[0][j] + ((i == 1 ? 1.0f : 0.0f) + dt * nC[i][1]) * F[1][j] +
                        ((i == 2 ? 1.0f : 0.0f) + dt * nC[i][2]) * F[2][j];  // (I + dt C) F
+    // SVD of the trial F: the plastic models project its singular values (kernels.py:241-262); all models then
+    // take the next substep's stress from the same decomposition (F = U diag(sig + delta) V^T), which is what
+    // P2G would get from decomposing the stored F again.
     const Material m = mats[P.mat[p]];
-    if (m.model != 0) {  // plastic models: SVD of the trial F and a return mapping on its singular values
-        float U[3][3], sig[3], d[3], V[3][3], delta[3];
-        svd3(Fn, U, sig, d, V, fp64);
+    float U[3][3], sig[3], d[3], V[3][3];
+    svd3(Fn, U, sig, d, V, fp64);
+    float jp = P.Jp[p];
+    if (m.model != 0) {
+        float delta[3];
         bool moved;
         if (m.model == 1) {
             moved = project_von_mises(sig, d, m.mu, m.yield_stress, delta);
@@ -341,7 +424,8 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
         } else {
             float ratio;
             moved = project_snow(sig, d, m.clamp_lo, m.clamp_hi, delta, &ratio);
-            P.Jp[p] = P.Jp[p] * ratio;
+            jp = jp * ratio;
+            P.Jp[p] = jp;
         }
         if (moved) {  // F = U diag(new) V^T, applied as F + U diag(new - old) V^T
 #pragma unroll
@@ -349,9 +433,18 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
 #pragma unroll
                 for (int j = 0; j < 3; ++j)
                     Fn[i][j] += U[i][0] * delta[0] * V[j][0] + U[i][1] * delta[1] * V[j][1] + U[i][2] * delta[2] * V[j][2];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                sig[i] += delta[i];
+                d[i] += delta[i];
+            }
         }
     }
     store_mat3(P.F, p, Fn);
+    float t[6];
+    tau_from_svd(m, jp, U, sig, d, t);
+#pragma unroll
+    for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
 
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -359,6 +452,18 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
         P.v[a][p] = nv[a];
         nx_out[a] = nx[a];
     }
+}
+
+struct GlobalSource {
+    const GridDesc* g;
+    const float4* grid;
+    MPM_HD float4 operator()(int i, int j, int k) const { return load_node(&grid[node_index(*g, i, j, k)]); }
+};
+
+MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
+                         const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3]) {
+    GlobalSource src{&g, grid};
+    g2p_particle_from(P, p, mats, g, dt, src, fp64, nx_out);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

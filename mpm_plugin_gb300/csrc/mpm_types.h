@@ -42,6 +42,7 @@ struct Particles {
     float* C[9];  // row-major APIC affine matrix
     float* F[9];  // row-major deformation gradient
     float* Jp;
+    float* tau[6];  // Kirchhoff stress xx yy zz xy xz yz, from F and Jp (set by G2P and when particles enter)
     int32_t* mat;
     int32_t* emitter;
     int32_t* id;  // insertion rank: the reference's particle order, restored on every download
@@ -122,6 +123,22 @@ struct WorkLists {
                                 // [3]: collider particle candidates
     int32_t* node_cand;         // grid nodes (blocked index) inside some collider's margin box
     int32_t* part_cand;         // particles inside some collider's margin box after G2P
+};
+
+// The active-block list of parity `cur`, selected without indexing the struct's array (a dynamic index into
+// a kernel parameter's array makes the compiler copy the whole struct to local memory).
+__host__ __device__ __forceinline__ int32_t* active_blocks(const WorkLists& wl, unsigned int cur) {
+    return cur ? wl.blocks[1] : wl.blocks[0];
+}
+
+// Periodic reorder of the particle arena by grid node: key = blocked index of the stencil's base node (or
+// the node count for stencils outside the grid), a counting sort by key, then a permutation of every field.
+struct SortScratch {
+    int32_t* key;        // per particle
+    int32_t* rank;       // per particle: arrival order within its key
+    int32_t* order;      // per particle: the particle that goes to position i
+    unsigned int* count; // per key (grid nodes + 1)
+    int32_t* start;      // per key: exclusive prefix sum of count
 };
 
 }  // namespace mpm

@@ -2,6 +2,10 @@
 // suite can check the SVD's accuracy and the BVH closest-point query against the oracle without a GPU.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "../../mpm_plugin_gb300/csrc/mpm_bvh.h"
@@ -86,6 +90,7 @@ struct Emu {
     unsigned int fp64 = 0;
 };
 
+
 // Narrow-band voxel grids, built with the same per-voxel functions the GPU build runs.
 static void emu_build_sdf(Emu* e) {
     e->cells.clear();
@@ -151,23 +156,38 @@ void emu_set_transforms(void* ev, int n, const float* s16, const float* e16) {
 }
 
 void emu_use_sdf(void* ev, int on) { static_cast<Emu*>(ev)->use_sdf = on != 0; }
-
 void emu_grid_dims(void* ev, int* dims) {
     Emu* e = static_cast<Emu*>(ev);
     for (int a = 0; a < 3; ++a) dims[a] = e->g.dims[a];
 }
 
-// x, v: (3, n) planar; C, F: (9, n) planar row-major components; Jp, mat: (n)
-unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, float* F, float* Jp, int32_t* mat,
-                         double dt, double s, double frame_dt) {
+// Stored-stress form of particles from F (9, n) planar, Jp and mat: tau (6, n) planar.
+void emu_particle_stress(void* ev, int64_t n, float* F, float* Jp, int32_t* mat, float* tau) {
+    Emu* e = static_cast<Emu*>(ev);
+    Particles P{};
+    for (int k = 0; k < 9; ++k) P.F[k] = F + k * n;
+    for (int k = 0; k < 6; ++k) P.tau[k] = tau + k * n;
+    P.Jp = Jp;
+    P.mat = mat;
+    P.n = P.cap = n;
+    for (int64_t p = 0; p < n; ++p) particle_stress(P, p, e->mats.data(), &e->fp64);
+}
+
+// x, v: (3, n) planar; C, F: (9, n) planar row-major components; tau: (6, n) stored stress, computed from
+// F and Jp first when stress_valid is 0 (particles that just entered); Jp, mat: (n)
+unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, float* F, float* Jp, float* tau,
+                         int stress_valid, int32_t* mat, double dt, double s, double frame_dt) {
     Emu* e = static_cast<Emu*>(ev);
     Particles P{};
     for (int a = 0; a < 3; ++a) { P.x[a] = x + a * n; P.v[a] = v + a * n; }
     for (int k = 0; k < 9; ++k) { P.C[k] = C + k * n; P.F[k] = F + k * n; }
     P.Jp = Jp;
+    for (int k = 0; k < 6; ++k) P.tau[k] = tau + k * n;
     P.mat = mat;
     P.n = n;
     P.cap = n;
+    if (!stress_valid)
+        for (int64_t p = 0; p < n; ++p) particle_stress(P, p, e->mats.data(), &e->fp64);
     const float dtf = (float)dt;
     std::vector<ColliderPose> poses(e->cols.size());
     for (size_t c = 0; c < e->cols.size(); ++c) collider_pose_at(e->cols[c], (float)s, (float)(1.0 / frame_dt), poses[c]);
@@ -181,7 +201,7 @@ unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, floa
     cd.cells = e->use_sdf && !e->cells.empty() ? e->cells.data() : nullptr;
     cd.cand = e->cand.empty() ? nullptr : e->cand.data();
     const int n_col = cd.n_col;
-    for (int64_t p = 0; p < n; ++p) p2g_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data(), &e->fp64);
+    for (int64_t p = 0; p < n; ++p) p2g_particle(P, p, e->mats.data(), e->g, dtf, e->grid.data());
     const int64_t nblk = (int64_t)e->g.nb[0] * e->g.nb[1] * e->g.nb[2];
     for (int64_t blk = 0; blk < nblk; ++blk) {
         const int bk = (int)(blk % e->g.nb[2]), bj = (int)((blk / e->g.nb[2]) % e->g.nb[1]);

@@ -47,10 +47,11 @@ def lib():
     L.emu_set_colliders.argtypes = [P, C.c_int, P]
     L.emu_set_transforms.argtypes = [P, C.c_int, P, P]
     L.emu_grid_dims.argtypes = [P, P]
-    L.emu_substep.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_double, C.c_double, C.c_double]
+    L.emu_substep.argtypes = [P, C.c_int64, P, P, P, P, P, P, C.c_int, P, C.c_double, C.c_double, C.c_double]
     L.emu_substep.restype = C.c_uint
     L.emu_read_grid.argtypes = [P, P]
     L.emu_use_sdf.argtypes = [P, C.c_int]
+    L.emu_particle_stress.argtypes = [P, C.c_int64, P, P, P, P]
     L.emu_collider_sdf.argtypes = [P, C.c_int, C.c_float, C.c_int, C.c_int, P, P]
     _lib = L
     return L
@@ -145,7 +146,9 @@ class SubstepEmulator:
                       "F": np.ascontiguousarray(np.asarray(s["F"], np.float32).reshape(n, 9).T),
                       "Jp": np.ascontiguousarray(np.asarray(s["Jp"], np.float32).reshape(n)),
                       "mat": np.ascontiguousarray(np.asarray(s["mat"], np.int32).reshape(n)),
-                      "emitter": np.asarray(s["emitter"], np.int32).copy()}
+                      "emitter": np.asarray(s["emitter"], np.int32).copy(),
+                      "tau": np.zeros((6, n), np.float32)}
+        self.stress_valid = False
 
     def save_state(self):
         s = self.state
@@ -156,8 +159,18 @@ class SubstepEmulator:
 
     def substep(self, dt, s=1.0, frame_dt=1.0):
         st = self.state
-        return lib().emu_substep(self.h, len(st["Jp"]), _p(st["x"]), _p(st["v"]), _p(st["C"]), _p(st["F"]),
-                                 _p(st["Jp"]), _p(st["mat"]), dt, s, frame_dt)
+        r = lib().emu_substep(self.h, len(st["Jp"]), _p(st["x"]), _p(st["v"]), _p(st["C"]), _p(st["F"]),
+                              _p(st["Jp"]), _p(st["tau"]), int(self.stress_valid), _p(st["mat"]), dt, s, frame_dt)
+        self.stress_valid = True
+        return r
+
+    def stress_of_state(self):
+        """(6, n) stress computed from the current F and Jp alone (what a fresh particle would get)."""
+        st = self.state
+        n = len(st["Jp"])
+        tau = np.zeros((6, n), np.float32)
+        lib().emu_particle_stress(self.h, n, _p(st["F"]), _p(st["Jp"]), _p(st["mat"]), _p(tau))
+        return tau
 
     def collider_sdf(self, c, s, pts, use_sdf=True):
         """(normal xyz, phi) of collider c at substep fraction s for world points (phi 1e30: far)."""

@@ -30,6 +30,21 @@ def test_emulated_substep_matches_reference(name):
         assert rel_err(out[k], ref[k]) <= 1e-5, (k, rel_err(out[k], ref[k]))
 
 
+def test_stored_stress_matches_stress_of_stored_f():
+    """The stress G2P stores (from the trial F's SVD after the return mapping) equals the stress of the
+    stored F decomposed again, which is what the reference's next P2G computes."""
+    case = Case("models_substep")
+    a = case.action
+    e = SubstepEmulator(case.domain, case.materials, case.gravity, case.ppc)
+    e.load_state(case.state("in"))
+    for _ in range(3):
+        e.substep(a["dt"], a["s"], a["frame_dt"])
+    kept, fresh = e.state["tau"], e.stress_of_state()
+    scale = np.abs(fresh).max()
+    assert scale > 0
+    assert np.abs(kept - fresh).max() <= 1e-5 * scale, np.abs(kept - fresh).max() / scale
+
+
 def test_emulated_grid_matches_oracle_grid():
     """Node by node: mass and velocity after the grid update and collider contact."""
     from oracle.oracle import OracleSolver
