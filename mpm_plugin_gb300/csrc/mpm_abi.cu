@@ -24,7 +24,7 @@ using namespace mpm;
 namespace {
 
 constexpr double kCFL = 0.4;  // warp/solver.py:19
-constexpr int kFields = 34;                 // x3 v3 C9 F9 Jp tau6 mat emitter id
+constexpr int kFields = kParticleFields;    // x3 v3 C9 F9 Jp tau6 mat emitter id
 
 thread_local std::string g_last_error;
 
@@ -330,7 +330,7 @@ Status reorder_particles(Handle* h) {
         CK(cudaEventRecord(h->perm_ev[0], h->stream));
     }
     launch_sort(h->stream, h->P, h->g, h->ss, h->grid_nodes, h->ss_scan, h->ss_scan_cap);
-    launch_permute(h->stream, h->P, dst, h->ss.order);
+    launch_permute(h->stream, h->arena, h->spare_arena, h->P.cap, h->P.n, h->ss.order);
     CK(cudaGetLastError());
     h->launches += 6;  // keys, three-pass scan, order, permutation
     if (h->timing) {

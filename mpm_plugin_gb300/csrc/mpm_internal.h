@@ -46,8 +46,9 @@ void launch_sort(cudaStream_t st, const Particles& P, const GridDesc& g, const S
 // Kirchhoff stress of the particles [off, off + n) from their F and Jp.
 void launch_particle_stress(cudaStream_t st, const Particles& P, int64_t off, int64_t n, const Material* mats,
                             unsigned int* fp64);
-// dst[i] = src[order[i]] for every particle field (reorder into bin order).
-void launch_permute(cudaStream_t st, const Particles& src, const Particles& dst, const int32_t* order);
+// dst[i] = src[order[i]] for every field of a particle arena (kParticleFields planes of cap words each).
+void launch_permute(cudaStream_t st, const void* src_arena, void* dst_arena, int64_t cap, int64_t n,
+                    const int32_t* order);
 
 constexpr int kSdfMaxCandidates = 128;
 // Narrow-band voxel grid of one collider: classify every voxel (cells[v].y: candidate count, kSdfFar or

@@ -119,8 +119,11 @@ __global__ void __launch_bounds__(256) k_p2g_scatter(Particles P, const Material
             }
 }
 
-// exclusive scan of int32 in three passes: per-CTA sums, one CTA over the sums, per-CTA scan + offset
-constexpr int kScanTile = 1024;
+// exclusive scan of int32 in three passes: per-CTA sums, one CTA over the sums, per-CTA scan + offset.
+// A CTA of kScanThreads threads covers kScanItems consecutive values per thread.
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
 
 __device__ __forceinline__ int block_exclusive_scan(int v, int* sh_warp, int* total) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -171,26 +174,20 @@ __global__ void __launch_bounds__(256) k_sort_scatter(int64_t n, SortScratch ss)
 
 // dst[i] = src[order[i]] for every field: neighbouring threads of P2G and G2P then touch neighbouring grid
 // nodes, so their reductions and gathers hit the same cache lines.
-__global__ void k_permute(Particles src, Particles dst, const int32_t* __restrict__ order) {
+// The arena's fields are kParticleFields planes of `cap` words each, so the permutation is one gather per
+// plane; all loads of a thread are issued before its stores, which the compiler could not reorder on its own
+// (source and destination planes are plain pointers).
+
+__global__ void __launch_bounds__(256) k_permute(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst,
+                                                 int64_t cap, int64_t n, const int32_t* __restrict__ order) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= src.n) return;
+    if (i >= n) return;
     const int64_t q = order[i];
+    uint32_t w[kParticleFields];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        dst.x[a][i] = src.x[a][q];
-        dst.v[a][i] = src.v[a][q];
-    }
+    for (int f = 0; f < kParticleFields; ++f) w[f] = __ldg(&src[f * cap + q]);
 #pragma unroll
-    for (int e = 0; e < 9; ++e) {
-        dst.C[e][i] = src.C[e][q];
-        dst.F[e][i] = src.F[e][q];
-    }
-    dst.Jp[i] = src.Jp[q];
-#pragma unroll
-    for (int e = 0; e < 6; ++e) dst.tau[e][i] = src.tau[e][q];
-    dst.mat[i] = src.mat[q];
-    dst.emitter[i] = src.emitter[q];
-    dst.id[i] = src.id[q];
+    for (int f = 0; f < kParticleFields; ++f) dst[f * cap + i] = w[f];
 }
 
 // Stress of the particles [off, off + n) from their F and Jp (particles entering the arena).
@@ -242,8 +239,10 @@ __global__ void __launch_bounds__(128) k_grid_colliders(GridDesc g, float4* __re
     }
 }
 
-// G2P; particles that end inside a collider's margin box are listed for k_project_particles.
-__global__ void __launch_bounds__(256) k_g2p(Particles P, const Material* __restrict__ mats, GridDesc g,
+// G2P; particles that end inside a collider's margin box are listed for k_project_particles. Capped at 80
+// registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra resident warps
+// outweigh the few spilled values (measured 10 % faster than the uncapped 120 registers).
+__global__ void __launch_bounds__(256, 3) k_g2p(Particles P, const Material* __restrict__ mats, GridDesc g,
                                              const StepParams* __restrict__ sp, const float4* __restrict__ grid,
                                              unsigned int* fp64_lanes, WorkLists wl, ColliderData cd) {
     int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,10 +365,16 @@ __global__ void k_compact(Particles src, Particles dst, const int32_t* __restric
 }
 
 
-__global__ void k_scan_tiles(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ tile_sums) {
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const int32_t* __restrict__ in, int64_t n,
+                                                              int32_t* __restrict__ tile_sums) {
     __shared__ int sh[32];
-    int64_t i = (int64_t)blockIdx.x * kScanTile + threadIdx.x;
-    int v = i < n ? in[i] : 0;
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int v = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + k * kScanThreads + threadIdx.x;
+        v += i < n ? in[i] : 0;
+    }
     int total;
     block_exclusive_scan(v, sh, &total);
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
@@ -393,13 +398,39 @@ __global__ void k_scan_sums(int32_t* __restrict__ sums, int64_t m, int32_t* __re
     if (threadIdx.x == 0 && grand_total) *grand_total = carry;
 }
 
-__global__ void k_scan_apply(const int32_t* __restrict__ in, int64_t n, const int32_t* __restrict__ tile_offsets,
-                             int32_t* __restrict__ out) {
+// Shared tile index with one pad word per 32, so thread t reading its values t * kScanItems + k hits 32
+// different banks across a warp.
+__device__ __forceinline__ int scan_pad(int i) { return i + (i >> 5); }
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t* __restrict__ in, int64_t n,
+                                                              const int32_t* __restrict__ tile_offsets,
+                                                              int32_t* __restrict__ out) {
     __shared__ int sh[32];
-    int64_t i = (int64_t)blockIdx.x * kScanTile + threadIdx.x;
-    int v = i < n ? in[i] : 0;
-    int ex = block_exclusive_scan(v, sh, nullptr);
-    if (i < n) out[i] = ex + tile_offsets[blockIdx.x];
+    __shared__ int tile[kScanTile + kScanTile / 32];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int l = k * kScanThreads + threadIdx.x;
+        tile[scan_pad(l)] = base + l < n ? in[base + l] : 0;
+    }
+    __syncthreads();
+    int sum = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) sum += tile[scan_pad(threadIdx.x * kScanItems + k)];
+    int run = block_exclusive_scan(sum, sh, nullptr) + tile_offsets[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int l = scan_pad(threadIdx.x * kScanItems + k);
+        const int x = tile[l];
+        tile[l] = run;
+        run += x;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int l = k * kScanThreads + threadIdx.x;
+        if (base + l < n) out[base + l] = tile[scan_pad(l)];
+    }
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -528,9 +559,11 @@ void launch_particle_stress(cudaStream_t st, const Particles& P, int64_t off, in
     k_particle_stress<<<blocks_for(n, 128), 128, 0, st>>>(P, off, n, mats, fp64);
 }
 
-void launch_permute(cudaStream_t st, const Particles& src, const Particles& dst, const int32_t* order) {
-    if (src.n == 0) return;
-    k_permute<<<blocks_for(src.n, 256), 256, 0, st>>>(src, dst, order);
+void launch_permute(cudaStream_t st, const void* src_arena, void* dst_arena, int64_t cap, int64_t n,
+                    const int32_t* order) {
+    if (n == 0) return;
+    k_permute<<<blocks_for(n, 256), 256, 0, st>>>(static_cast<const uint32_t*>(src_arena),
+                                                 static_cast<uint32_t*>(dst_arena), cap, n, order);
 }
 
 void launch_sdf_classify(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris,
@@ -585,9 +618,9 @@ void launch_exclusive_scan(cudaStream_t st, const int32_t* in, int64_t n, int32_
                            int32_t* total) {
     if (n == 0) return;
     int64_t tiles = scan_tile_count(n);
-    k_scan_tiles<<<(unsigned int)tiles, kScanTile, 0, st>>>(in, n, tile_tmp);
+    k_scan_tiles<<<(unsigned int)tiles, kScanThreads, 0, st>>>(in, n, tile_tmp);
     k_scan_sums<<<1, 1024, 0, st>>>(tile_tmp, tiles, total);
-    k_scan_apply<<<(unsigned int)tiles, kScanTile, 0, st>>>(in, n, tile_tmp, out);
+    k_scan_apply<<<(unsigned int)tiles, kScanThreads, 0, st>>>(in, n, tile_tmp, out);
 }
 
 void launch_scatter_volume(cudaStream_t st, const Particles& P, const GridDesc& g, float* vol) {

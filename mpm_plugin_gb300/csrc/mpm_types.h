@@ -36,6 +36,9 @@ struct Material {
 };
 
 // Particle state, structure of arrays; every component is its own array of `cap` entries.
+// Words per particle in the arena: x3 v3 C9 F9 Jp tau6 mat emitter id, one plane of `cap` words each.
+constexpr int kParticleFields = 34;
+
 struct Particles {
     float* x[3];
     float* v[3];
