@@ -155,6 +155,27 @@ int mpm_fp64_lanes(void *handle, int64_t *lanes);
 int mpm_is_occupied_noalloc(const MpmDomainDesc *domain, int32_t particles_per_cell, int64_t n, const float *d_x,
                             int64_t m, const float *d_points, uint8_t *d_out, int32_t device, void *stream);
 
+/* Batches. No counterpart in the reference, whose solver advances one scene per call: a batch advances many
+ * independent scenes (handles created on one device) together. Every kernel of a substep is launched once for
+ * all scenes of the batch from a device table of the scenes, and the launch sequence of one batched substep is
+ * a CUDA graph replayed as often as the scene with the most substeps in the frame needs; each scene keeps its
+ * own CFL time step, materials, colliders and particle order, and scenes whose frame is done sit idle. A
+ * handle belongs to at most one batch; while it does, all of its work (including its own mpm_* calls) runs on
+ * the batch's stream. Destroying a handle removes it from its batch. Errors: mpm_batch_last_error(batch). */
+int mpm_batch_create(void **batch);
+int mpm_batch_destroy(void *batch); /* member handles stay valid and leave the batch */
+const char *mpm_batch_last_error(void *batch);
+int mpm_batch_add(void *batch, void *handle);
+int mpm_batch_remove(void *batch, void *handle);
+int mpm_batch_size(void *batch, int32_t *n);
+/* One frame of every scene, in the order they were added: frame_dt[i] for scene i (its advance(frame_dt),
+ * mpm_core/solver.py:67-68), stats[i] as mpm_advance returns them. */
+int mpm_batch_advance(void *batch, const double *frame_dt, MpmAdvanceStats *stats);
+int mpm_batch_set_option(void *batch, int32_t option, int64_t value); /* MPM_OPT_SORT_INTERVAL */
+int mpm_batch_get_stream(void *batch, void **stream);
+/* Kernels launched by the batch and its scenes so far. */
+int mpm_batch_launch_count(void *batch, int64_t *launches);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,7 +23,9 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_set_collider_transforms", "mpm_advance", "mpm_substep", "mpm_particle_count", "mpm_get_particles",
            "mpm_is_occupied", "mpm_save_state", "mpm_load_state", "mpm_set_option", "mpm_get_stream",
            "mpm_synchronize", "mpm_kernel_times", "mpm_grid_dims", "mpm_read_grid", "mpm_read_collider_pose",
-           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc")
+           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_batch_create", "mpm_batch_destroy",
+           "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
+           "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count")
 
 
 class MpmDomainDesc(C.Structure):
@@ -83,6 +85,15 @@ def lib() -> C.CDLL:
         "mpm_launch_count": [P, C.POINTER(I64)],
         "mpm_fp64_lanes": [P, C.POINTER(I64)],
         "mpm_is_occupied_noalloc": [C.POINTER(MpmDomainDesc), I32, I64, P, I64, P, P, I32, P],
+        "mpm_batch_create": [C.POINTER(P)],
+        "mpm_batch_destroy": [P],
+        "mpm_batch_add": [P, P],
+        "mpm_batch_remove": [P, P],
+        "mpm_batch_size": [P, C.POINTER(I32)],
+        "mpm_batch_advance": [P, P, P],
+        "mpm_batch_set_option": [P, I32, I64],
+        "mpm_batch_get_stream": [P, C.POINTER(P)],
+        "mpm_batch_launch_count": [P, C.POINTER(I64)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -90,15 +101,18 @@ def lib() -> C.CDLL:
         f.restype = C.c_int
     L.mpm_last_error.argtypes = [P]
     L.mpm_last_error.restype = C.c_char_p
+    L.mpm_batch_last_error.argtypes = [P]
+    L.mpm_batch_last_error.restype = C.c_char_p
     _lib = L
     return L
 
 
-def check(status: int, handle=None) -> None:
+def check(status: int, handle=None, batch=None) -> None:
     """Map a status to the exception the reference raises in the same situation."""
     if status == MPM_OK:
         return
-    msg = (lib().mpm_last_error(handle) or b"").decode(errors="replace")
+    err = lib().mpm_batch_last_error(batch) if batch is not None else lib().mpm_last_error(handle)
+    msg = (err or b"").decode(errors="replace")
     if status == MPM_ERR_VALUE:
         raise ValueError(msg)
     if status == MPM_ERR_NOT_IMPLEMENTED:

@@ -63,9 +63,13 @@ struct GraphCache {
     }
 };
 
+struct Batch;
+
 struct Handle {
     int device = 0;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // the stream all work runs on: own_stream, or the batch's
+    cudaStream_t own_stream = nullptr;
+    Batch* batch = nullptr;             // the batch this scene belongs to, if any
     MpmDomainDesc dom{};
     HostDomain hd{};
     double dx = 0, inv_dx = 0, p_vol = 0;
@@ -259,7 +263,9 @@ cudaEvent_t take_event(Handle* h) {
 
 SubstepArgs substep_args(Handle* h) {
     SubstepArgs a{};
-    a.P = h->P;
+    a.arena = static_cast<float*>(h->arena);
+    a.cap = h->P.cap;
+    a.n = h->P.n;
     a.mats = h->d_mats;
     a.g = h->g;
     a.sp = h->d_sp;
@@ -593,6 +599,21 @@ Status remove_escaped(Handle* h, int32_t* removed_out) {
     return {};
 }
 
+// CFL step from the bits of max |v| (warp/solver.py:176-185): dt = min(0.4 dx / (c_max + vmax), frame_dt)
+// over the materials present, then the frame split into equal substeps.
+void choose_dt(const Handle* h, unsigned int vmax_bits, double frame_dt, double* dt_out, int* steps_out) {
+    float vmax_f;
+    std::memcpy(&vmax_f, &vmax_bits, 4);
+    double vmax = std::isfinite(vmax_f) ? (double)vmax_f : 0.0;
+    double c = 0.0;
+    for (size_t m = 0; m < h->wave.size(); ++m)
+        if (h->mat_count[m] > 0) c = std::max(c, h->wave[m]);
+    double dt = std::min(kCFL * h->dx / (c + vmax), frame_dt);
+    int steps = (int)std::ceil(frame_dt / dt - 1e-9);
+    *dt_out = frame_dt / steps;
+    *steps_out = steps;
+}
+
 Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
     if (h->P.n == 0) {
         *stats = MpmAdvanceStats{0, frame_dt, 0};
@@ -605,15 +626,9 @@ Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
     h->launches += 1;
     CK(cudaMemcpyAsync(h->h_counters, h->d_counters, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->stream));
     CK(cudaStreamSynchronize(h->stream));
-    float vmax_f;
-    std::memcpy(&vmax_f, &h->h_counters[0], 4);
-    double vmax = std::isfinite(vmax_f) ? (double)vmax_f : 0.0;
-    double c = 0.0;
-    for (size_t m = 0; m < h->wave.size(); ++m)
-        if (h->mat_count[m] > 0) c = std::max(c, h->wave[m]);
-    double dt = std::min(kCFL * h->dx / (c + vmax), frame_dt);
-    int steps = (int)std::ceil(frame_dt / dt - 1e-9);
-    dt = frame_dt / steps;
+    int steps = 0;
+    double dt = 0.0;
+    choose_dt(h, h->h_counters[0], frame_dt, &dt, &steps);
     TRY(set_step(h, dt, 0.0, frame_dt, steps));
     TRY(ensure_sdf(h));
     TRY(prepare_poses(h, steps, 0.0, frame_dt));
@@ -707,7 +722,8 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     *out = h;
     h->device = device;
     DeviceGuard guard(device);
-    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+    h->stream = h->own_stream;
     h->dom = *dom;
     h->ppc = ppc;
     h->g = make_grid(*dom, gravity, ppc, &h->hd);
@@ -759,9 +775,12 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     return {};
 }
 
+Status batch_remove(Batch* b, Handle* h);
+
 void destroy(Handle* h) {
     if (!h) return;
     DeviceGuard guard(h->device);
+    if (h->batch) batch_remove(h->batch, h);
     if (h->stream) cudaStreamSynchronize(h->stream);
     invalidate_graph(h);
     for (auto& v : h->ev_pending)
@@ -796,7 +815,7 @@ void destroy(Handle* h) {
     cudaFree(h->ss_scan);
     cudaFree(h->stage);
     if (h->h_counters) cudaFreeHost(h->h_counters);
-    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
 }
 
@@ -852,6 +871,238 @@ Status set_colliders(Handle* h, int32_t n, const MpmColliderDesc* cs) {
     return {};
 }
 
+
+// ------------------------------------------------------------------------------------------------------
+// Batches: independent scenes (handles on one device) advanced together. Every kernel of a substep is
+// launched once for all scenes (mpm_batch_kernels.cu) from a device table of the scenes' SubstepArgs; the
+// launch sequence of one batched substep is a captured CUDA graph replayed as many times as the scene with
+// the most substeps needs, and scenes whose frame is done idle (StepParams::active). Member handles run
+// all their work on the batch's stream.
+// ------------------------------------------------------------------------------------------------------
+struct Batch {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    std::vector<Handle*> scenes;             // in the order they were added
+    std::vector<Handle*> live;               // scenes with particles in the current advance
+    SubstepArgs* d_table = nullptr;
+    int table_cap = 0;
+    int32_t* d_cta = nullptr;                // cta_scene (particle CTAs) followed by cta_first (per scene)
+    int64_t cta_cap = 0;
+    unsigned int particle_ctas = 0;
+    bool any_colliders = false;
+    std::vector<int64_t> layout;             // what the captured graph depends on
+    cudaGraphExec_t graph = nullptr;
+    unsigned int* d_vmax = nullptr;          // per scene: max |v| bits
+    unsigned int* h_vmax = nullptr;          // pinned
+    int vmax_cap = 0;
+    int sort_interval = 4;
+    int64_t launches = 0;
+    std::string err;
+};
+
+int finish_batch(Batch* b, Status s) {
+    if (s.code != MPM_OK) {
+        if (b) b->err = s.msg;
+        g_last_error = s.msg;
+    }
+    return s.code;
+}
+
+void batch_invalidate(Batch* b) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    b->layout.clear();
+}
+
+// Table of the live scenes and the CTA layout of the particle kernels (ceil(cap / 256) CTAs per scene, so
+// the layout changes only when a capacity does). The table itself is uploaded every time it is called.
+Status batch_upload(Batch* b) {
+    const int n = (int)b->live.size();
+    if (n > b->table_cap) {
+        CK(cudaStreamSynchronize(b->stream));
+        cudaFree(b->d_table);
+        b->d_table = nullptr;
+        b->table_cap = 0;
+        CK(cudaMalloc(&b->d_table, sizeof(SubstepArgs) * (size_t)std::max(n, 8)));
+        b->table_cap = std::max(n, 8);
+        batch_invalidate(b);
+    }
+    std::vector<SubstepArgs> table(n);
+    std::vector<int64_t> layout{n};
+    int64_t ctas = 0;
+    bool cols = false;
+    for (int s = 0; s < n; ++s) {
+        Handle* h = b->live[s];
+        table[s] = substep_args(h);
+        layout.push_back(h->P.cap);
+        ctas += (h->P.cap + 255) / 256;
+        cols = cols || h->n_col > 0;
+    }
+    layout.push_back(cols ? 1 : 0);
+    if (layout != b->layout) {
+        CK(cudaStreamSynchronize(b->stream));
+        batch_invalidate(b);
+        if (ctas + n > b->cta_cap) {
+            cudaFree(b->d_cta);
+            b->d_cta = nullptr;
+            b->cta_cap = 0;
+            CK(cudaMalloc(&b->d_cta, sizeof(int32_t) * (size_t)(ctas + n)));
+            b->cta_cap = ctas + n;
+        }
+        std::vector<int32_t> cta(ctas + n);
+        int64_t c = 0;
+        for (int s = 0; s < n; ++s) {
+            cta[ctas + s] = (int32_t)c;
+            const int64_t k = (b->live[s]->P.cap + 255) / 256;
+            for (int64_t i = 0; i < k; ++i) cta[c++] = s;
+        }
+        CK(cudaMemcpyAsync(b->d_cta, cta.data(), sizeof(int32_t) * cta.size(), cudaMemcpyHostToDevice, b->stream));
+        b->particle_ctas = (unsigned int)ctas;
+        b->any_colliders = cols;
+        b->layout = layout;
+    }
+    // a pageable source is staged by the driver before the call returns, so `table` may go out of scope
+    CK(cudaMemcpyAsync(b->d_table, table.data(), sizeof(SubstepArgs) * (size_t)n, cudaMemcpyHostToDevice, b->stream));
+    return {};
+}
+
+Status batch_replay(Batch* b) {
+    BatchLaunch bl{b->d_table, b->d_cta, b->d_cta + b->particle_ctas, (int)b->live.size(), b->particle_ctas,
+                   b->any_colliders};
+    if (!b->graph) {
+        cudaGraph_t graph;
+        CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        launch_batch_substep(b->stream, bl);
+        cudaError_t e0 = cudaGetLastError();
+        cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+        CK(e0);
+        CK(e);
+        e = cudaGraphInstantiate(&b->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        CK(e);
+    }
+    CK(cudaGraphLaunch(b->graph, b->stream));
+    b->launches += batch_substep_kernel_count(bl);
+    return {};
+}
+
+// One frame of every scene: per-scene CFL step (one read-back for all scenes), poses and voxel grids, then
+// max(steps) batched substeps with the reorder of every scene still running after each sort_interval of
+// them, then removal of escaped particles scene by scene.
+Status batch_advance(Batch* b, const double* frame_dt, MpmAdvanceStats* stats) {
+    const int S = (int)b->scenes.size();
+    if (S > b->vmax_cap) {
+        CK(cudaStreamSynchronize(b->stream));
+        cudaFree(b->d_vmax);
+        cudaFreeHost(b->h_vmax);
+        b->d_vmax = nullptr;
+        b->h_vmax = nullptr;
+        b->vmax_cap = 0;
+        CK(cudaMalloc(&b->d_vmax, sizeof(unsigned int) * (size_t)std::max(S, 8)));
+        CK(cudaMallocHost(&b->h_vmax, sizeof(unsigned int) * (size_t)std::max(S, 8)));
+        b->vmax_cap = std::max(S, 8);
+    }
+    if (S == 0) return {};
+    CK(cudaMemsetAsync(b->d_vmax, 0, sizeof(unsigned int) * (size_t)S, b->stream));
+    for (int s = 0; s < S; ++s) {
+        Handle* h = b->scenes[s];
+        if (h->P.n == 0) continue;
+        launch_max_speed(b->stream, h->P, b->d_vmax + s);
+        h->launches += 1;
+    }
+    CK(cudaMemcpyAsync(b->h_vmax, b->d_vmax, sizeof(unsigned int) * (size_t)S, cudaMemcpyDeviceToHost, b->stream));
+    CK(cudaStreamSynchronize(b->stream));
+    b->live.clear();
+    std::vector<int> steps(S, 0);
+    int max_steps = 0;
+    for (int s = 0; s < S; ++s) {
+        Handle* h = b->scenes[s];
+        stats[s] = MpmAdvanceStats{0, frame_dt[s], 0};
+        if (h->P.n == 0) continue;
+        double dt = 0.0;
+        choose_dt(h, b->h_vmax[s], frame_dt[s], &dt, &steps[s]);
+        stats[s] = MpmAdvanceStats{steps[s], dt, 0};
+        h->frame_dt = frame_dt[s];
+        TRY(set_step(h, dt, 0.0, frame_dt[s], steps[s]));
+        TRY(ensure_sdf(h));
+        TRY(prepare_poses(h, steps[s], 0.0, frame_dt[s]));
+        TRY(ensure_part_cand(h));
+        b->live.push_back(h);
+        max_steps = std::max(max_steps, steps[s]);
+    }
+    if (!b->live.empty()) {
+        TRY(batch_upload(b));
+        for (int k = 0; k < max_steps; ++k) {
+            TRY(batch_replay(b));
+            if (b->sort_interval > 0 && (k + 1) % b->sort_interval == 0 && k + 1 < max_steps) {
+                bool any = false;
+                for (int s = 0; s < S; ++s) {
+                    Handle* h = b->scenes[s];
+                    if (h->P.n == 0 || steps[s] <= k + 1) continue;  // done or empty: no later substep
+                    TRY(reorder_particles(h));
+                    any = true;
+                }
+                if (any) TRY(batch_upload(b));
+            }
+        }
+    }
+    for (int s = 0; s < S; ++s) {
+        Handle* h = b->scenes[s];
+        if (h->P.n == 0) continue;
+        int32_t removed = 0;
+        TRY(remove_escaped(h, &removed));
+        stats[s].removed = removed;
+    }
+    CK(cudaStreamSynchronize(b->stream));
+    return {};
+}
+
+Status batch_add(Batch* b, Handle* h) {
+    if (h->batch) return {MPM_ERR_VALUE, "the scene already belongs to a batch"};
+    if (b->device < 0) b->device = h->device;
+    if (h->device != b->device) return {MPM_ERR_VALUE, "the scenes of a batch must be on one device"};
+    if (!b->stream) CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CK(cudaStreamSynchronize(h->own_stream));
+    h->stream = b->stream;
+    h->batch = b;
+    invalidate_graph(h);
+    b->scenes.push_back(h);
+    batch_invalidate(b);
+    return {};
+}
+
+Status batch_remove(Batch* b, Handle* h) {
+    auto it = std::find(b->scenes.begin(), b->scenes.end(), h);
+    if (it == b->scenes.end()) return {MPM_ERR_VALUE, "the scene is not in this batch"};
+    CK(cudaStreamSynchronize(b->stream));
+    b->scenes.erase(it);
+    b->live.clear();
+    h->stream = h->own_stream;
+    h->batch = nullptr;
+    invalidate_graph(h);
+    batch_invalidate(b);
+    return {};
+}
+
+void batch_destroy(Batch* b) {
+    if (!b) return;
+    if (b->device >= 0) {
+        DeviceGuard guard(b->device);
+        if (b->stream) cudaStreamSynchronize(b->stream);
+        for (Handle* h : b->scenes) {
+            h->stream = h->own_stream;
+            h->batch = nullptr;
+            invalidate_graph(h);
+        }
+        batch_invalidate(b);
+        cudaFree(b->d_table);
+        cudaFree(b->d_cta);
+        cudaFree(b->d_vmax);
+        cudaFreeHost(b->h_vmax);
+        if (b->stream) cudaStreamDestroy(b->stream);
+    }
+    delete b;
+}
 }  // namespace
 
 void mpm::set_last_error(const std::string& msg) { g_last_error = msg; }
@@ -1112,4 +1363,82 @@ int mpm_fp64_lanes(void* handle, int64_t* lanes) {
     return MPM_OK;
 }
 
+
+int mpm_batch_create(void** batch) {
+    if (!batch) return finish(nullptr, {MPM_ERR_ARGUMENT, "null output"});
+    *batch = new Batch();
+    return MPM_OK;
+}
+
+int mpm_batch_destroy(void* batch) {
+    batch_destroy(static_cast<Batch*>(batch));
+    return MPM_OK;
+}
+
+const char* mpm_batch_last_error(void* batch) {
+    return batch ? static_cast<Batch*>(batch)->err.c_str() : g_last_error.c_str();
+}
+
+#define BATCH_OR_FAIL(bv)                                                                      \
+    Batch* b = static_cast<Batch*>(bv);                                                        \
+    if (!b) return finish(nullptr, Status{MPM_ERR_ARGUMENT, "null batch"})
+
+int mpm_batch_add(void* batch, void* handle) {
+    BATCH_OR_FAIL(batch);
+    Handle* h = static_cast<Handle*>(handle);
+    if (!h) return finish_batch(b, {MPM_ERR_ARGUMENT, "null handle"});
+    DeviceGuard guard(h->device);
+    return finish_batch(b, batch_add(b, h));
+}
+
+int mpm_batch_remove(void* batch, void* handle) {
+    BATCH_OR_FAIL(batch);
+    Handle* h = static_cast<Handle*>(handle);
+    if (!h) return finish_batch(b, {MPM_ERR_ARGUMENT, "null handle"});
+    DeviceGuard guard(h->device);
+    return finish_batch(b, batch_remove(b, h));
+}
+
+int mpm_batch_size(void* batch, int32_t* n) {
+    BATCH_OR_FAIL(batch);
+    if (!n) return finish_batch(b, {MPM_ERR_ARGUMENT, "null output"});
+    *n = (int32_t)b->scenes.size();
+    return MPM_OK;
+}
+
+int mpm_batch_advance(void* batch, const double* frame_dt, MpmAdvanceStats* stats) {
+    BATCH_OR_FAIL(batch);
+    if (b->scenes.empty()) return MPM_OK;
+    if (!frame_dt || !stats) return finish_batch(b, {MPM_ERR_ARGUMENT, "null frame_dt or stats"});
+    for (size_t s = 0; s < b->scenes.size(); ++s)
+        if (!(frame_dt[s] > 0.0)) return finish_batch(b, {MPM_ERR_VALUE, "frame_dt must be positive"});
+    DeviceGuard guard(b->device);
+    return finish_batch(b, batch_advance(b, frame_dt, stats));
+}
+
+int mpm_batch_set_option(void* batch, int32_t option, int64_t value) {
+    BATCH_OR_FAIL(batch);
+    if (option == MPM_OPT_SORT_INTERVAL) {
+        if (value < 0 || value > (1 << 30)) return finish_batch(b, {MPM_ERR_VALUE, "sort interval out of range"});
+        b->sort_interval = (int)value;
+        return MPM_OK;
+    }
+    return finish_batch(b, {MPM_ERR_VALUE, "unknown option"});
+}
+
+int mpm_batch_get_stream(void* batch, void** stream) {
+    BATCH_OR_FAIL(batch);
+    if (!stream) return finish_batch(b, {MPM_ERR_ARGUMENT, "null output"});
+    *stream = b->stream;
+    return MPM_OK;
+}
+
+int mpm_batch_launch_count(void* batch, int64_t* launches) {
+    BATCH_OR_FAIL(batch);
+    if (!launches) return finish_batch(b, {MPM_ERR_ARGUMENT, "null output"});
+    int64_t total = b->launches;
+    for (Handle* h : b->scenes) total += h->launches;
+    *launches = total;
+    return MPM_OK;
+}
 }  // extern "C"

@@ -20,17 +20,6 @@ void set_last_error(const std::string& msg);
 
 constexpr unsigned int kListCtas = 152 * 8;  // CTAs of the kernels that walk device-sized work lists
 
-// Everything one substep's kernels read; the pointers stay fixed while a captured graph is replayed.
-struct SubstepArgs {
-    Particles P;
-    const Material* mats;
-    GridDesc g;
-    StepParams* sp;
-    float4* grid;
-    unsigned int* fp64;
-    WorkLists wl;
-    ColliderData cd;  // poses: the start of the pose array; kernels add the substep's pose_base
-};
 
 void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, ColliderPose* poses, int steps,
                            float s_given, float inv_frame_dt);
@@ -39,6 +28,20 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 // nodes when `capturing`).
 void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool capturing);
 int substep_kernel_count(const SubstepArgs& a);
+
+// One batched substep over a device table of scenes (mpm_batch_kernels.cu). The particle kernels run
+// particle_ctas CTAs of 256 threads; CTA b works on scene cta_scene[b], particles
+// (b - cta_first[scene]) * 256 + thread.
+struct BatchLaunch {
+    const SubstepArgs* scenes;
+    const int32_t* cta_scene;
+    const int32_t* cta_first;
+    int n_scenes;
+    unsigned int particle_ctas;
+    bool any_colliders;
+};
+void launch_batch_substep(cudaStream_t st, const BatchLaunch& b);
+int batch_substep_kernel_count(const BatchLaunch& b);
 // Counting sort of the particles by the grid node of their stencil base: fills ss.order (scan_tmp: scan
 // scratch of scan_cap + 2 entries, at least scan_tile_count(n_nodes + 1) + 1).
 void launch_sort(cudaStream_t st, const Particles& P, const GridDesc& g, const SortScratch& ss, int64_t n_nodes,

@@ -1,15 +1,13 @@
-// sm_103a kernels of the MLS-MPM substep and of the particle-state bookkeeping around it.
-//
-// One substep = step_begin (substep fraction + collider poses, on the device) -> clear -> P2G -> grid update
-// (normalise, gravity, walls, mesh colliders) -> G2P (+ particle projection out of colliders). Every kernel
-// reads dt and s from a StepParams record in device memory, so a captured graph of one substep replays
-// for every substep of an advance.
+// sm_103a kernels around the MLS-MPM substep (collider poses, CFL speed, particle-state I/O, removal,
+// reorder, scans, occupancy, narrow-band voxel grids) and the launcher of one plain substep, whose kernels
+// (mpm_substep_kernels.cuh) read dt and s from a StepParams record in device memory, so a captured graph
+// of one substep replays for every substep of an advance.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 
 #include "mpm_internal.h"
-#include "mpm_substep.cuh"
+#include "mpm_substep_kernels.cuh"
 
 namespace mpm {
 
@@ -25,98 +23,6 @@ __global__ void k_collider_poses(const ColliderDev* __restrict__ cols, int n_col
     int k = (int)(t / n_col), c = (int)(t % n_col);
     float s = steps > 0 ? (float)((double)(k + 1) / (double)steps) : s_given;
     collider_pose_at(cols[c], s, inv_frame_dt, poses[t]);
-}
-
-// ------------------------------------------------------------------------------------------------------
-// Start of a substep: counters, substep fraction, pose offset; the work lists of this substep start empty.
-// ------------------------------------------------------------------------------------------------------
-__global__ void k_step_begin(StepParams* sp, unsigned int* counts, int n_col) {
-    StepParams p = *sp;
-    p.seq += 1;
-    if (p.steps > 0) {
-        p.k += 1;
-        p.s = (float)((double)(p.k + 1) / (double)p.steps);
-        p.pose_base = p.k * n_col;
-    } else {
-        p.pose_base = 0;
-    }
-    *sp = p;
-    counts[p.seq & 1u] = 0u;
-    counts[2] = 0u;
-    counts[3] = 0u;
-}
-
-// Zeroes the grid blocks the previous substep used (and their flags), so the whole grid is zero again.
-__global__ void __launch_bounds__(256) k_clear_blocks(const StepParams* __restrict__ sp, WorkLists wl,
-                                                      float4* __restrict__ grid) {
-    const unsigned int prev = (sp->seq - 1u) & 1u;
-    const unsigned int n = wl.counts[prev];
-    const int32_t* __restrict__ list = active_blocks(wl, prev);
-    for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
-        const int64_t b = list[i];
-        grid[b * 64 + (threadIdx.x & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if ((threadIdx.x & 63) == 0) wl.block_flag[b] = 0u;
-    }
-}
-
-// Warp-aggregated append: one atomic per warp.
-__device__ __forceinline__ void warp_append(int32_t* __restrict__ list, unsigned int* __restrict__ count, int32_t v) {
-    const unsigned int mask = __activemask();
-    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
-    unsigned int base = 0;
-    if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(mask));
-    base = __shfl_sync(mask, base, leader);
-    list[base + __popc(mask & ((1u << lane) - 1u))] = v;
-}
-
-// P2G with warp-level aggregation: lanes whose stencils start at the same grid node (neighbours in the
-// particle order after the reorder by grid node) form a segment; each of the 27 x 4 contributions is summed
-// over the segment with shuffles (after round r a lane holds the sum of the next 2^r lanes of its segment)
-// and only the segment's first lane issues the 16-byte reduction, so a cell of ~8 particles costs one
-// reduction per node instead of eight. Lanes past the end or with a stencil outside the grid are
-// single-lane segments that add nothing.
-__global__ void __launch_bounds__(256) k_p2g_scatter(Particles P, const Material* __restrict__ mats, GridDesc g,
-                                                     const StepParams* __restrict__ sp, float4* __restrict__ grid,
-                                                     WorkLists wl) {
-    const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = (int)(threadIdx.x & 31u);
-    if ((int64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u) >= P.n) return;  // whole warp past the end
-    P2gTerms t;
-    const bool valid = p < P.n && p2g_terms(P, p, mats, g, sp->dt, t);
-    const int64_t key = valid ? node_index(g, t.base[0], t.base[1], t.base[2]) : -1 - (int64_t)lane;
-    const int64_t key_prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const int64_t key_next = __shfl_down_sync(0xffffffffu, key, 1);
-    const bool first = lane == 0 || key_prev != key;
-    const bool last = lane == 31 || key_next != key;
-    const unsigned int ends = __ballot_sync(0xffffffffu, last);
-    const int tail = __ffs(ends >> lane) - 1;  // lanes after this one in its segment
-    const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned int)tail);
-    const bool leader = valid && first;
-    if (leader) {
-        const unsigned int cur = sp->seq & 1u;
-        mark_stencil_blocks(g, t.base, wl.block_flag, active_blocks(wl, cur), &wl.counts[cur]);
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                float val[4] = {0.f, 0.f, 0.f, 0.f};
-                if (valid) p2g_node(t, g, i, j, k, val);
-#pragma unroll
-                for (int s = 1; s < 32; s <<= 1) {
-                    if (s <= span) {  // warp-uniform
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            const float o = __shfl_down_sync(0xffffffffu, val[c], s);
-                            if (s <= tail) val[c] += o;
-                        }
-                    }
-                }
-                if (leader) grid_add(&grid[node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k)], val[0], val[1],
-                                     val[2], val[3]);
-            }
 }
 
 // exclusive scan of int32 in three passes: per-CTA sums, one CTA over the sums, per-CTA scan + offset.
@@ -196,69 +102,6 @@ __global__ void k_particle_stress(Particles P, int64_t off, int64_t n, const Mat
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     particle_stress(P, off + i, mats, fp64_lanes);
-}
-
-// Grid update over the active blocks, four 4x4x4 blocks per 256-thread CTA. Nodes inside a collider's
-// margin box are listed for k_grid_colliders.
-__global__ void __launch_bounds__(256) k_grid_update(GridDesc g, float4* __restrict__ grid,
-                                                     const StepParams* __restrict__ sp, WorkLists wl, ColliderData cd) {
-    const unsigned int cur = sp->seq & 1u;
-    const unsigned int n = wl.counts[cur];
-    const float dt = sp->dt;
-    cd.poses += sp->pose_base;
-    const int l = threadIdx.x & 63;
-    for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
-        const int64_t b = active_blocks(wl, cur)[i];
-        const int bk = (int)(b % g.nb[2]);
-        const int bj = (int)((b / g.nb[2]) % g.nb[1]);
-        const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
-        const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-        bool has_mass = grid_node_walls(g, &grid[b * 64 + l], idx, dt);
-        if (has_mass && cd.n_col > 0) {
-            float pos[3];
-            node_position(g, idx, pos);
-            if (near_any_collider(pos, cd)) warp_append(wl.node_cand, &wl.counts[2], (int32_t)(b * 64 + l));
-        }
-    }
-}
-
-// Mesh-collider contact of the listed nodes (full warps of candidates; BVH queries).
-__global__ void __launch_bounds__(128) k_grid_colliders(GridDesc g, float4* __restrict__ grid,
-                                                        const StepParams* __restrict__ sp, WorkLists wl, ColliderData cd) {
-    const unsigned int n = wl.counts[2];
-    cd.poses += sp->pose_base;
-    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int64_t q = wl.node_cand[i];
-        const int64_t b = q >> 6;
-        const int l = (int)(q & 63);
-        const int bk = (int)(b % g.nb[2]);
-        const int bj = (int)((b / g.nb[2]) % g.nb[1]);
-        const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
-        const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-        grid_node_colliders(g, &grid[q], idx, cd);
-    }
-}
-
-// G2P; particles that end inside a collider's margin box are listed for k_project_particles. Capped at 80
-// registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra resident warps
-// outweigh the few spilled values (measured 10 % faster than the uncapped 120 registers).
-__global__ void __launch_bounds__(256, 3) k_g2p(Particles P, const Material* __restrict__ mats, GridDesc g,
-                                             const StepParams* __restrict__ sp, const float4* __restrict__ grid,
-                                             unsigned int* fp64_lanes, WorkLists wl, ColliderData cd) {
-    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= P.n) return;
-    float nx[3];
-    g2p_particle(P, p, mats, g, sp->dt, grid, fp64_lanes, nx);
-    cd.poses += sp->pose_base;
-    if (cd.n_col > 0 && near_any_collider(nx, cd)) warp_append(wl.part_cand, &wl.counts[3], (int32_t)p);
-}
-
-__global__ void __launch_bounds__(128) k_project_particles(Particles P, GridDesc g, const StepParams* __restrict__ sp,
-                                                           WorkLists wl, ColliderData cd) {
-    const unsigned int n = wl.counts[3];
-    cd.poses += sp->pose_base;
-    for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        project_particle(P, wl.part_cand[i], g, cd);
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -525,21 +368,22 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 
 void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool capturing) {
     const unsigned int list_ctas = kListCtas;
+    const OneScene sc{a};
     // while a graph is being captured the records become event nodes that fire on every replay
     auto mark = [&](int i) {
         if (ev) cudaEventRecordWithFlags(ev[i], st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     };
     mark(0);
-    k_step_begin<<<1, 1, 0, st>>>(a.sp, a.wl.counts, a.cd.n_col);
-    k_clear_blocks<<<list_ctas, 256, 0, st>>>(a.sp, a.wl, a.grid);
+    k_step_begin<<<1, 1, 0, st>>>(sc);
+    k_clear_blocks<<<list_ctas, 256, 0, st>>>(sc);
     mark(1);
-    if (a.P.n > 0) k_p2g_scatter<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.wl);
+    if (a.n > 0) k_p2g_scatter<<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
     mark(2);
-    k_grid_update<<<list_ctas, 256, 0, st>>>(a.g, a.grid, a.sp, a.wl, a.cd);
-    if (a.cd.n_col > 0) k_grid_colliders<<<list_ctas, 128, 0, st>>>(a.g, a.grid, a.sp, a.wl, a.cd);
+    k_grid_update<<<list_ctas, 256, 0, st>>>(sc);
+    if (a.cd.n_col > 0) k_grid_colliders<<<list_ctas, 128, 0, st>>>(sc);
     mark(3);
-    if (a.P.n > 0) k_g2p<<<blocks_for(a.P.n, 256), 256, 0, st>>>(a.P, a.mats, a.g, a.sp, a.grid, a.fp64, a.wl, a.cd);
-    if (a.cd.n_col > 0) k_project_particles<<<list_ctas, 128, 0, st>>>(a.P, a.g, a.sp, a.wl, a.cd);
+    if (a.n > 0) k_g2p<<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+    if (a.cd.n_col > 0) k_project_particles<<<list_ctas, 128, 0, st>>>(sc);
     mark(4);
 }
 
@@ -577,7 +421,7 @@ void launch_sdf_fill(cudaStream_t st, const ColliderDev& col, const BvhNode* nod
 }
 
 int substep_kernel_count(const SubstepArgs& a) {
-    return 3 + (a.P.n > 0 ? 2 : 0) + (a.cd.n_col > 0 ? 2 : 0);
+    return 3 + (a.n > 0 ? 2 : 0) + (a.cd.n_col > 0 ? 2 : 0);
 }
 
 

@@ -115,6 +115,7 @@ struct StepParams {
     int k, steps;        // substep index within the advance; steps == 0 for a single explicit substep
     unsigned int seq;    // substeps run so far on this handle (selects the active-block list in use)
     int pose_base;       // first pose of this substep in the pose array
+    int active;          // 1 while this scene has a substep to run (a batch idles scenes whose advance is done)
 };
 
 // Work lists the substep builds on the device. Active blocks are the 4x4x4 grid blocks P2G touched;
@@ -143,5 +144,42 @@ struct SortScratch {
     unsigned int* count; // per key (grid nodes + 1)
     int32_t* start;      // per key: exclusive prefix sum of count
 };
+
+// Everything one substep's kernels read for one scene; the pointers stay fixed while a captured graph is
+// replayed (a batch keeps one per scene in a device table).
+struct SubstepArgs {
+    float* arena;  // kParticleFields planes of cap words (particles_of gives the field pointers)
+    int64_t cap, n;
+    const Material* mats;
+    GridDesc g;
+    StepParams* sp;
+    float4* grid;
+    unsigned int* fp64;
+    WorkLists wl;
+    ColliderData cd;  // poses: the start of the pose array; kernels add the substep's pose_base
+};
+
+// The field pointers of a particle arena: plane f starts at arena + f * cap (x3 v3 C9 F9 Jp tau6 mat
+// emitter id). Computed, not stored, so kernels that take a scene from a table keep two values live
+// instead of 34 pointers.
+__host__ __device__ __forceinline__ Particles make_particles(float* arena, int64_t cap, int64_t n) {
+    Particles P;
+    for (int a = 0; a < 3; ++a) P.x[a] = arena + (int64_t)a * cap;
+    for (int a = 0; a < 3; ++a) P.v[a] = arena + (int64_t)(3 + a) * cap;
+    for (int e = 0; e < 9; ++e) P.C[e] = arena + (int64_t)(6 + e) * cap;
+    for (int e = 0; e < 9; ++e) P.F[e] = arena + (int64_t)(15 + e) * cap;
+    P.Jp = arena + (int64_t)24 * cap;
+    for (int e = 0; e < 6; ++e) P.tau[e] = arena + (int64_t)(25 + e) * cap;
+    P.mat = reinterpret_cast<int32_t*>(arena + (int64_t)31 * cap);
+    P.emitter = reinterpret_cast<int32_t*>(arena + (int64_t)32 * cap);
+    P.id = reinterpret_cast<int32_t*>(arena + (int64_t)33 * cap);
+    P.n = n;
+    P.cap = cap;
+    return P;
+}
+
+__host__ __device__ __forceinline__ Particles particles_of(const SubstepArgs& a) {
+    return make_particles(a.arena, a.cap, a.n);
+}
 
 }  // namespace mpm
