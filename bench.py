@@ -136,6 +136,75 @@ def make_gpu_solver(device: str):
     return s, xf
 
 
+BATCH_FRAME_DT = 1 / 480
+
+
+def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
+    """The batched workload: 64 seeded scenes (n_hi = 2e6: about 24.9M particles, log-uniform 10k-1.7M per
+    scene, grids 33^3-176^3; n_hi = 1e5: small scenes of 10k-100k particles), four material models, 0-2
+    colliders of 1k-20k triangles, each advancing with its own CFL step. Times `frames` frames of 1/480 s of
+    every scene run one at a time through the plain solver, then the same number through one Gb300Batch;
+    both after one untimed frame (graph capture, voxel grids)."""
+    import torch
+
+    from mpm_plugin_gb300.batch import Gb300Batch
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+    from mpm_plugin_gb300.solver import Gb300Solver
+    from scenes import add, batched_scenes
+
+    specs = batched_scenes(seed=0, n_hi=n_hi)
+    solvers = []
+    for d, mats, pos, vel, cols in specs:
+        s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+        add(s, pos, 0, 0, vel)
+        if cols:
+            s.set_colliders([ColliderGeometry(MeshData(cv, ct), True, fr) for cv, ct, _, fr in cols])
+            xf = np.stack([c[2] for c in cols])
+            s.set_collider_transforms(xf, xf)
+        solvers.append(s)
+    counts = [s.particle_count for s in solvers]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        return out, time.perf_counter() - t0
+
+    # plain: one scene at a time (each scene's frames back to back, as separate bake jobs would run)
+    plain_ps, plain_s, plain_frame_ms = 0.0, 0.0, []
+    for s, n in zip(solvers, counts):
+        s.advance(BATCH_FRAME_DT)
+        for _ in range(frames):
+            st, el = timed(lambda: s.advance(BATCH_FRAME_DT))
+            plain_ps += n * st.substeps
+            plain_s += el
+            plain_frame_ms.append(1e3 * el)
+    batch = Gb300Batch(solvers)
+    batch.advance(BATCH_FRAME_DT)
+    launches0 = batch.launch_count()
+    batch_ps, batch_s, batch_frame_ms = 0.0, 0.0, []
+    for _ in range(frames):
+        stats, el = timed(lambda: batch.advance(BATCH_FRAME_DT))
+        batch_ps += sum(s.particle_count * st.substeps for s, st in zip(solvers, stats))
+        batch_s += el
+        batch_frame_ms.append(1e3 * el)
+    launches = batch.launch_count() - launches0
+    batch.close()
+    for s in solvers:
+        s.close()
+    plain = plain_ps / plain_s
+    batched = batch_ps / batch_s
+    return {"value": batched, "plain_value": plain, "unit": UNIT, "ratio": batched / plain,
+            "scenes": len(counts), "particles": int(sum(counts)), "frames": frames, "frame_dt": BATCH_FRAME_DT,
+            "batch_frame_ms": {"p50": float(np.percentile(batch_frame_ms, 50)),
+                               "p99": float(np.percentile(batch_frame_ms, 99))},
+            "plain_scene_frame_ms": {"p50": float(np.percentile(plain_frame_ms, 50)),
+                                     "p99": float(np.percentile(plain_frame_ms, 99))},
+            "gpu_launches_per_frame": launches / frames,
+            "timing": "host clock around advance calls with device synchronisation; state resident in HBM"}
+
+
 def cpu_oracle_time(threads: int, budget_s: float):
     """FP32 oracle (C restatement of the reference kernels, OpenMP) on the same scene; returns rate, sample."""
     from oracle.oracle import OracleSolver
@@ -275,7 +344,13 @@ def run_gpu(args, world, rank, local):
             traffic = json.loads(tfile.read_text()).get(dom)
         except Exception:
             traffic = None
+    fp64_lanes = solver.fp64_lanes()
     cpu_rate, cpu_n, cpu_k, cpu_el = cpu_oracle_time(os.cpu_count() or 1, args.cpu_budget)
+    batched = None
+    if args.batched_frames > 0:
+        solver.close()
+        batched = run_batched(device, args.batched_frames)
+        batched["small_scenes"] = run_batched(device, args.batched_frames, n_hi=1e5)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -295,7 +370,8 @@ def run_gpu(args, world, rank, local):
         "frame_latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
         "gpu_launches": launches,
         "clocks": clk.summary(),
-        "fp64_svd_lanes": solver.fp64_lanes(),
+        "fp64_svd_lanes": fp64_lanes,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -310,6 +386,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--e2e-frames", type=int, default=4, help="24 fps frames timed through the solver API")
+    ap.add_argument("--batched-frames", type=int, default=3,
+                    help="frames of the 64-scene batched workload, plain and batched (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()

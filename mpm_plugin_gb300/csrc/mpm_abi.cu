@@ -1059,6 +1059,8 @@ Status batch_advance(Batch* b, const double* frame_dt, MpmAdvanceStats* stats) {
 
 Status batch_add(Batch* b, Handle* h) {
     if (h->batch) return {MPM_ERR_VALUE, "the scene already belongs to a batch"};
+    if ((int)b->scenes.size() >= kMaxBatchScenes)
+        return {MPM_ERR_VALUE, "a batch holds at most " + std::to_string(kMaxBatchScenes) + " scenes"};
     if (b->device < 0) b->device = h->device;
     if (h->device != b->device) return {MPM_ERR_VALUE, "the scenes of a batch must be on one device"};
     if (!b->stream) CK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));

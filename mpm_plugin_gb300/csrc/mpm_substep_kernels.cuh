@@ -12,6 +12,7 @@
 namespace mpm {
 
 struct OneScene {
+    static constexpr bool kTable = false;
     SubstepArgs a;
     __device__ __forceinline__ int count() const { return 1; }
     __device__ __forceinline__ SubstepArgs get(int) const { return a; }
@@ -21,6 +22,7 @@ struct OneScene {
 };
 
 struct SceneTable {
+    static constexpr bool kTable = true;
     const SubstepArgs* __restrict__ scenes;
     const int32_t* __restrict__ cta_scene;  // particle kernels: the scene of each CTA
     const int32_t* __restrict__ cta_first;  // per scene: its first CTA in the particle kernels
@@ -40,6 +42,49 @@ __device__ __forceinline__ void warp_append(int32_t* __restrict__ list, unsigned
     if (lane == leader) base = atomicAdd(count, (unsigned int)__popc(mask));
     base = __shfl_sync(mask, base, leader);
     list[base + __popc(mask & ((1u << lane) - 1u))] = v;
+}
+
+// ------------------------------------------------------------------------------------------------------
+// (scene, item) work lists of a batch: every CTA loads the item count of each scene (0 for an idle scene)
+// into shared memory and scans it, so that the flattened items 0 .. total-1 are shared out over all CTAs and
+// item q belongs to the scene s with off[s] <= q < off[s + 1] (binary search). One warp scans, 32 scenes per
+// round. count(a) returns the scene's item count.
+// ------------------------------------------------------------------------------------------------------
+template <class Scenes, class Count>
+__device__ __forceinline__ unsigned int scene_offsets(const Scenes& sc, Count count, unsigned int* off) {
+    const int S = sc.count();
+    for (int s = threadIdx.x; s < S; s += blockDim.x) {
+        const SubstepArgs a = sc.get(s);
+        off[s + 1] = sc.active(a) ? count(a) : 0u;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned int carry = 0;
+        for (int base = 0; base < S; base += 32) {
+            const int s = base + (int)threadIdx.x;
+            unsigned int v = s < S ? off[s + 1] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const unsigned int y = __shfl_up_sync(0xffffffffu, v, o);
+                if ((int)threadIdx.x >= o) v += y;
+            }
+            if (s < S) off[s + 1] = carry + v;
+            carry += __shfl_sync(0xffffffffu, v, 31);
+        }
+        if (threadIdx.x == 0) off[0] = 0u;
+    }
+    __syncthreads();
+    return off[S];
+}
+
+// The scene of flattened item q: the last s with off[s] <= q.
+__device__ __forceinline__ int scene_of_item(const unsigned int* off, int S, unsigned int q) {
+    int lo = 0, hi = S - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= q) lo = mid; else hi = mid - 1;
+    }
+    return lo;
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -77,18 +122,28 @@ __global__ void k_step_begin(Scenes sc) {
 }
 
 // Zeroes the grid blocks the previous substep used (and their flags), so the whole grid is zero again.
+// Four blocks per 256-thread CTA.
+__device__ __forceinline__ void clear_block(const SubstepArgs& a, unsigned int i) {
+    const unsigned int prev = (a.sp->seq - 1u) & 1u;
+    const int64_t b = active_blocks(a.wl, prev)[i];
+    a.grid[b * 64 + (threadIdx.x & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if ((threadIdx.x & 63) == 0) a.wl.block_flag[b] = 0u;
+}
+
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
-    for (int s = 0; s < sc.count(); ++s) {
-        const SubstepArgs a = sc.get(s);
-        if (!sc.active(a)) continue;
-        const unsigned int prev = (a.sp->seq - 1u) & 1u;
-        const unsigned int n = a.wl.counts[prev];
-        const int32_t* __restrict__ list = active_blocks(a.wl, prev);
-        for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
-            const int64_t b = list[i];
-            a.grid[b * 64 + (threadIdx.x & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
-            if ((threadIdx.x & 63) == 0) a.wl.block_flag[b] = 0u;
+    if constexpr (!Scenes::kTable) {
+        const SubstepArgs a = sc.get(0);
+        const unsigned int n = a.wl.counts[(a.sp->seq - 1u) & 1u];
+        for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) clear_block(a, i);
+    } else {
+        __shared__ unsigned int off[kMaxBatchScenes + 1];
+        const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
+            return a.wl.counts[(a.sp->seq - 1u) & 1u];
+        }, off);
+        for (unsigned int q = blockIdx.x * 4u + (threadIdx.x >> 6); q < total; q += gridDim.x * 4u) {
+            const int s = scene_of_item(off, sc.count(), q);
+            clear_block(sc.get(s), q - off[s]);
         }
     }
 }
@@ -151,53 +206,73 @@ __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
 
 // Grid update (normalise, gravity, walls) over the active blocks, four 4x4x4 blocks per 256-thread CTA;
 // nodes with mass inside some collider's margin box are listed for k_grid_colliders.
-template <class Scenes>
-__global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
-    for (int s = 0; s < sc.count(); ++s) {
-        const SubstepArgs a = sc.get(s);
-        if (!sc.active(a)) continue;
-        const GridDesc& g = a.g;
-        const unsigned int cur = a.sp->seq & 1u;
-        const unsigned int n = a.wl.counts[cur];
-        const float dt = a.sp->dt;
+__device__ __forceinline__ void grid_update_block(const SubstepArgs& a, unsigned int i) {
+    const GridDesc& g = a.g;
+    const unsigned int cur = a.sp->seq & 1u;
+    const int l = threadIdx.x & 63;
+    const int64_t b = active_blocks(a.wl, cur)[i];
+    const int bk = (int)(b % g.nb[2]);
+    const int bj = (int)((b / g.nb[2]) % g.nb[1]);
+    const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
+    const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+    bool has_mass = grid_node_walls(g, &a.grid[b * 64 + l], idx, a.sp->dt);
+    if (has_mass && a.cd.n_col > 0) {
         ColliderData cd = a.cd;
         cd.poses += a.sp->pose_base;
-        const int l = threadIdx.x & 63;
-        for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) {
-            const int64_t b = active_blocks(a.wl, cur)[i];
-            const int bk = (int)(b % g.nb[2]);
-            const int bj = (int)((b / g.nb[2]) % g.nb[1]);
-            const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
-            const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-            bool has_mass = grid_node_walls(g, &a.grid[b * 64 + l], idx, dt);
-            if (has_mass && cd.n_col > 0) {
-                float pos[3];
-                node_position(g, idx, pos);
-                if (near_any_collider(pos, cd)) warp_append(a.wl.node_cand, &a.wl.counts[2], (int32_t)(b * 64 + l));
-            }
+        float pos[3];
+        node_position(g, idx, pos);
+        if (near_any_collider(pos, cd)) warp_append(a.wl.node_cand, &a.wl.counts[2], (int32_t)(b * 64 + l));
+    }
+}
+
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
+    if constexpr (!Scenes::kTable) {
+        const SubstepArgs a = sc.get(0);
+        const unsigned int n = a.wl.counts[a.sp->seq & 1u];
+        for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u)
+            grid_update_block(a, i);
+    } else {
+        __shared__ unsigned int off[kMaxBatchScenes + 1];
+        const unsigned int total =
+            scene_offsets(sc, [](const SubstepArgs& a) { return a.wl.counts[a.sp->seq & 1u]; }, off);
+        for (unsigned int q = blockIdx.x * 4u + (threadIdx.x >> 6); q < total; q += gridDim.x * 4u) {
+            const int s = scene_of_item(off, sc.count(), q);
+            grid_update_block(sc.get(s), q - off[s]);
         }
     }
 }
 
 // Mesh-collider contact of the listed nodes (full warps of candidates; voxel grid, then BVH queries).
+__device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigned int i) {
+    const GridDesc& g = a.g;
+    ColliderData cd = a.cd;
+    cd.poses += a.sp->pose_base;
+    const int64_t q = a.wl.node_cand[i];
+    const int64_t b = q >> 6;
+    const int l = (int)(q & 63);
+    const int bk = (int)(b % g.nb[2]);
+    const int bj = (int)((b / g.nb[2]) % g.nb[1]);
+    const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
+    const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+    grid_node_colliders(g, &a.grid[q], idx, cd);
+}
+
 template <class Scenes>
 __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
-    for (int s = 0; s < sc.count(); ++s) {
-        const SubstepArgs a = sc.get(s);
-        if (!sc.active(a) || a.cd.n_col == 0) continue;
-        const GridDesc& g = a.g;
+    if constexpr (!Scenes::kTable) {
+        const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[2];
-        ColliderData cd = a.cd;
-        cd.poses += a.sp->pose_base;
-        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-            const int64_t q = a.wl.node_cand[i];
-            const int64_t b = q >> 6;
-            const int l = (int)(q & 63);
-            const int bk = (int)(b % g.nb[2]);
-            const int bj = (int)((b / g.nb[2]) % g.nb[1]);
-            const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
-            const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-            grid_node_colliders(g, &a.grid[q], idx, cd);
+        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+            grid_collider_node(a, i);
+    } else {
+        __shared__ unsigned int off[kMaxBatchScenes + 1];
+        const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
+            return a.cd.n_col > 0 ? a.wl.counts[2] : 0u;
+        }, off);
+        for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+            const int s = scene_of_item(off, sc.count(), q);
+            grid_collider_node(sc.get(s), q - off[s]);
         }
     }
 }
@@ -221,17 +296,28 @@ __global__ void __launch_bounds__(256, 3) k_g2p(Scenes sc) {
     }
 }
 
+__device__ __forceinline__ void project_candidate(const SubstepArgs& a, unsigned int i) {
+    ColliderData cd = a.cd;
+    cd.poses += a.sp->pose_base;
+    project_particle(particles_of(a), a.wl.part_cand[i], a.g, cd);
+}
+
 template <class Scenes>
 __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
-    for (int s = 0; s < sc.count(); ++s) {
-        const SubstepArgs a = sc.get(s);
-        if (!sc.active(a) || a.cd.n_col == 0) continue;
+    if constexpr (!Scenes::kTable) {
+        const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[3];
-        ColliderData cd = a.cd;
-        cd.poses += a.sp->pose_base;
-        const Particles P = particles_of(a);
         for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            project_particle(P, a.wl.part_cand[i], a.g, cd);
+            project_candidate(a, i);
+    } else {
+        __shared__ unsigned int off[kMaxBatchScenes + 1];
+        const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
+            return a.cd.n_col > 0 ? a.wl.counts[3] : 0u;
+        }, off);
+        for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+            const int s = scene_of_item(off, sc.count(), q);
+            project_candidate(sc.get(s), q - off[s]);
+        }
     }
 }
 

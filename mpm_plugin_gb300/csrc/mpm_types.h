@@ -145,6 +145,9 @@ struct SortScratch {
     int32_t* start;      // per key: exclusive prefix sum of count
 };
 
+// Most scenes a batch holds (the kernels over work lists keep one count per scene in shared memory).
+constexpr int kMaxBatchScenes = 1024;
+
 // Everything one substep's kernels read for one scene; the pointers stay fixed while a captured graph is
 // replayed (a batch keeps one per scene in a device table).
 struct SubstepArgs {

@@ -158,3 +158,50 @@ def mix_scene(res: int = 128, seed: int = 0):
     cv, ct = icosphere(1.0, 4, seed=seed + 3, jitter=0.03)
     xf = translate(0.75, 0.7, 0.1) @ scale(0.12)
     return d, mats, groups, (cv, ct, xf)
+
+
+def lattice_box(lo, hi, spacing: float, rng) -> np.ndarray:
+    """Particles on a lattice of the given spacing filling [lo, hi], each jittered by U(+-spacing / 4)."""
+    axes = [np.arange(lo[a] + spacing / 2, hi[a], spacing, dtype=np.float64) for a in range(3)]
+    g = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
+    g += rng.uniform(-0.25 * spacing, 0.25 * spacing, g.shape)
+    return g.astype(np.float32)
+
+
+BATCH_MODELS = ("elastic", "von_mises", "drucker_prager", "snow")
+
+
+def batched_scenes(seed: int = 0, count: int = 64, n_lo: float = 1e4, n_hi: float = 2e6):
+    """Independent scenes of the batched workload: particle counts log-uniform in [n_lo, n_hi], grids from 32^3
+    to 192^3 matched to the count (a cube of material filling the same fraction of every grid, 8 per cell),
+    one material per scene with the model uniform over the four and parameters uniform within the ranges of the
+    jelly and mixed-materials workloads, a random initial velocity, and 0-2 static seeded perturbed icosphere
+    colliders of 1,280, 5,120 or 20,480 triangles below the material.
+
+    Returns [(domain, [material], positions, velocity, [(verts, tris, world matrix, friction)])].
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        n_target = float(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
+        res = int(np.clip(round(32 * (n_target / 1e4) ** (1 / 3)), 32, 192))
+        d = domain(res=res)
+        side = min((n_target / 8) ** (1 / 3) / res, 0.6)
+        lo = (0.5 - side / 2, 0.5 - side / 2, 0.25)
+        hi = (0.5 + side / 2, 0.5 + side / 2, 0.25 + side)
+        pos = lattice_box(lo, hi, d.dx / 2, rng)
+        model = BATCH_MODELS[int(rng.integers(4))]
+        mat = MaterialParams(f"batch{i}", model, float(rng.uniform(2e4, 3.5e5)), float(rng.uniform(0.2, 0.45)),
+                             float(rng.uniform(400.0, 1600.0)), yield_stress=float(rng.uniform(300.0, 3000.0)),
+                             friction_angle_deg=float(rng.uniform(30.0, 35.0)), hardening=10.0,
+                             critical_compression=2.5e-2, critical_stretch=7.5e-3,
+                             max_hardening=float(rng.uniform(5.0, 20.0)))
+        vel = tuple(float(c) for c in rng.uniform(-1.0, 1.0, 3))
+        cols = []
+        for c in range(int(rng.integers(0, 3))):
+            cv, ct = icosphere(1.0, int(rng.choice([3, 4, 5])), seed=seed * 1000 + i * 10 + c, jitter=0.03)
+            r = float(rng.uniform(0.06, 0.12))
+            xf = translate(float(rng.uniform(0.25, 0.75)), float(rng.uniform(0.25, 0.75)), r) @ scale(r)
+            cols.append((cv, ct, xf, float(rng.uniform(0.0, 0.5))))
+        out.append((d, [mat], pos, vel, cols))
+    return out
