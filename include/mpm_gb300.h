@@ -138,6 +138,9 @@ int mpm_read_collider_pose(void *handle, int32_t c, float *M12, float *Minv12, f
 /* Kernels of this library launched on the handle's stream since it was created. */
 int mpm_launch_count(void *handle, int64_t *launches);
 
+/* Device memory the handle holds now, in bytes (no counterpart in the reference; serving admission). */
+int mpm_device_bytes(void *handle, int64_t *bytes);
+
 /* Number of SVD lanes that took the FP64 path since the handle was created. */
 int mpm_fp64_lanes(void *handle, int64_t *lanes);
 

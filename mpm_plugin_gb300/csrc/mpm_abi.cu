@@ -103,6 +103,7 @@ struct Handle {
     int64_t part_cand_cap = 0;
     int2* d_sdf_cells = nullptr;      // narrow-band voxel grids of all colliders
     int32_t* d_sdf_cand = nullptr;
+    size_t sdf_bytes = 0, collider_bytes = 0;
     bool sdf_dirty = true;
     BvhNode* d_nodes = nullptr;
     MeshTri* d_tris = nullptr;
@@ -239,6 +240,20 @@ Status ensure_stage(Handle* h, size_t bytes) {
     return {};
 }
 
+// Device memory the handle holds now (the allocations it made, by their sizes).
+int64_t handle_device_bytes(const Handle* h) {
+    const int64_t nblk = (int64_t)h->g.nb[0] * h->g.nb[1] * h->g.nb[2];
+    int64_t b = (int64_t)h->P.cap * kFields * 4 * (h->spare_arena ? 2 : 1);
+    b += h->grid_nodes * 16 + (h->vol ? h->grid_nodes * 4 : 0);
+    b += nblk * 12 + h->grid_nodes * 4 + h->part_cand_cap * 4 + 16;                      // work lists
+    b += h->ss_cap * 12 + (h->grid_nodes + 1) * 8 + (h->ss_scan_cap + 2) * 4;           // sort
+    b += h->keep_cap * 16 + (h->scan_cap + 2) * 4;                                       // removal
+    b += h->pose_cap * (int64_t)sizeof(ColliderPose) + (int64_t)h->collider_bytes + (int64_t)h->sdf_bytes;
+    b += (int64_t)h->stage_bytes + (int64_t)sizeof(StepParams) + 4 * (2 + kMaxMaterials);
+    b += (int64_t)sizeof(Material) * (int64_t)std::max<size_t>(1, h->mat_desc.size());
+    return b;
+}
+
 // ---- substep sequence ---------------------------------------------------------------------------------
 
 void free_colliders(Handle* h) {
@@ -248,6 +263,7 @@ void free_colliders(Handle* h) {
     h->d_cols = nullptr;
     h->d_nodes = nullptr;
     h->d_tris = nullptr;
+    h->collider_bytes = 0;
 }
 
 cudaEvent_t take_event(Handle* h) {
@@ -442,6 +458,7 @@ Status ensure_sdf(Handle* h) {
     if (h->d_sdf_cand) cudaFree(h->d_sdf_cand);
     h->d_sdf_cells = nullptr;
     h->d_sdf_cand = nullptr;
+    h->sdf_bytes = 0;
     invalidate_graph(h);
     if (total == 0) {
         h->sdf_dirty = false;
@@ -449,6 +466,7 @@ Status ensure_sdf(Handle* h) {
     }
     int32_t *counts = nullptr, *starts = nullptr, *tmp = nullptr;
     const int64_t tiles = scan_tile_count(total) + 2;
+    h->sdf_bytes = sizeof(int2) * (size_t)total;
     bool ok = cudaMalloc(&h->d_sdf_cells, sizeof(int2) * (size_t)total) == cudaSuccess &&
               cudaMalloc(&counts, sizeof(int32_t) * (size_t)total) == cudaSuccess &&
               cudaMalloc(&starts, sizeof(int32_t) * (size_t)total) == cudaSuccess &&
@@ -471,6 +489,7 @@ Status ensure_sdf(Handle* h) {
     int32_t n_cand = 0;
     cudaError_t e = cudaMemcpyAsync(&n_cand, tmp + tiles, sizeof n_cand, cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    h->sdf_bytes += sizeof(int32_t) * (size_t)std::max(n_cand, 1);
     if (e == cudaSuccess && cudaMalloc(&h->d_sdf_cand, sizeof(int32_t) * (size_t)std::max(n_cand, 1)) != cudaSuccess)
         e = cudaErrorMemoryAllocation;
     if (e == cudaSuccess) {
@@ -857,6 +876,8 @@ Status set_colliders(Handle* h, int32_t n, const MpmColliderDesc* cs) {
         all_tris.insert(all_tris.end(), tris.begin(), tris.end());
     }
     if (n > 0) {
+        h->collider_bytes = sizeof(ColliderDev) * n + sizeof(BvhNode) * std::max<size_t>(1, all_nodes.size()) +
+                            sizeof(MeshTri) * std::max<size_t>(1, all_tris.size());
         CK(cudaMalloc(&h->d_cols, sizeof(ColliderDev) * n));
         CK(cudaMalloc(&h->d_nodes, sizeof(BvhNode) * std::max<size_t>(1, all_nodes.size())));
         CK(cudaMalloc(&h->d_tris, sizeof(MeshTri) * std::max<size_t>(1, all_tris.size())));
@@ -1365,6 +1386,13 @@ int mpm_fp64_lanes(void* handle, int64_t* lanes) {
     return MPM_OK;
 }
 
+
+int mpm_device_bytes(void* handle, int64_t* bytes) {
+    HANDLE_OR_FAIL(handle);
+    if (!bytes) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    *bytes = handle_device_bytes(h);
+    return MPM_OK;
+}
 
 int mpm_batch_create(void** batch) {
     if (!batch) return finish(nullptr, {MPM_ERR_ARGUMENT, "null output"});

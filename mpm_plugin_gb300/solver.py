@@ -193,6 +193,12 @@ class Gb300Solver(Solver):
         self._check(self._lib.mpm_launch_count(self._h, C.byref(v)))
         return v.value
 
+    def device_bytes(self) -> int:
+        """Device memory this solver holds now."""
+        n = C.c_int64()
+        self._check(self._lib.mpm_device_bytes(self._h, C.byref(n)))
+        return n.value
+
     def fp64_lanes(self) -> int:
         v = C.c_int64()
         self._check(self._lib.mpm_fp64_lanes(self._h, C.byref(v)))
