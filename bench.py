@@ -205,6 +205,83 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
             "timing": "host clock around advance calls with device synchronisation; state resident in HBM"}
 
 
+class _FrameSink:
+    """Stands in for the cache writer: receives every frame (positions, velocities) and counts the bytes."""
+
+    def __init__(self):
+        self.bytes = 0
+
+    def write_frame(self, frame, particles):
+        self.bytes += particles.positions.nbytes + particles.velocities.nbytes
+
+
+def serve_trace(seconds: float, rate: float, seed: int = 0):
+    """Poisson arrivals (mean `rate` per second) over `seconds`; each request one seeded pour job."""
+    from mpm_plugin_gb300.serve import BakeJob
+    from scenes import pour_job_spec
+
+    rng = np.random.default_rng(seed)
+    t, trace, i = 0.0, [], 0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t > seconds:
+            return trace
+        d, mats, setup, before, frames, fps, max_n, tris = pour_job_spec(seed * 1000 + i)
+        trace.append((t, BakeJob(f"job{i}", d, mats, frames, fps, setup=setup, before_frame=before,
+                                 writer=_FrameSink(), max_particles=max_n, collider_triangles=tris)))
+        i += 1
+
+
+def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float = 150.0) -> dict:
+    """Serving: a Poisson trace of pour jobs (96^3, pile of 28k-230k particles plus a 2 m/s disc inflow, a
+    2,048-triangle torus turning at 1 rev/s, 12 frames at 24 fps each) served by the bake server with a
+    150 GB admission budget, against the same trace served sequentially by the plain solver (each job alone,
+    in arrival order, starting when it has arrived and the one before has finished)."""
+    import torch
+
+    from mpm_plugin_gb300.serve import BakeServer
+    from mpm_plugin_gb300.solver import Gb300Solver
+
+    trace = serve_trace(seconds, rate)
+    srv = BakeServer(int(budget_gb * (1 << 30)), device=device)
+    rep = srv.run(trace)
+    srv.close()
+    served = rep.summary()
+
+    # the same trace, sequentially through the plain solver
+    trace = serve_trace(seconds, rate)
+    clock, frame_ms, job_s, ps = 0.0, [], [], 0.0
+    for arrival, job in trace:
+        clock = max(clock, arrival)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s = Gb300Solver(job.domain, job.materials, job.gravity, job.particles_per_cell, device=device)
+        job.setup(s)
+        last = time.perf_counter()
+        for k in range(1, job.frames + 1):
+            job.before_frame(s, k)
+            n = s.particle_count
+            st = s.advance(1.0 / job.fps)
+            ps += n * st.substeps
+            job.writer.write_frame(k, s.get_particles())
+            now = time.perf_counter()
+            frame_ms.append(1e3 * (now - last))
+            last = now
+        s.close()
+        clock += time.perf_counter() - t0
+        job_s.append(clock - arrival)
+    plain = {"frame_latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
+             "job_latency_s": {"p50": float(np.percentile(job_s, 50)), "p99": float(np.percentile(job_s, 99))},
+             "particle_substeps_per_s": ps / clock}
+    jl = list(rep.job_latency_s.values())
+    served["job_latency_s"] = {"p50": float(np.percentile(jl, 50)), "p99": float(np.percentile(jl, 99))}
+    return {"requests": len(trace), "rate_per_s": rate, "seconds": seconds, "budget_gb": budget_gb,
+            "served": served, "plain_sequential": plain,
+            "ratio": served["particle_substeps_per_s"] / plain["particle_substeps_per_s"],
+            "workload": "Poisson pour jobs, 96^3, 12 frames at 24 fps, inflow + rotating 2,048-triangle torus; "
+                        "frames handed to an in-memory sink in place of the cache writer"}
+
+
 def cpu_oracle_time(threads: int, budget_s: float):
     """FP32 oracle (C restatement of the reference kernels, OpenMP) on the same scene; returns rate, sample."""
     from oracle.oracle import OracleSolver
@@ -351,6 +428,7 @@ def run_gpu(args, world, rank, local):
         solver.close()
         batched = run_batched(device, args.batched_frames)
         batched["small_scenes"] = run_batched(device, args.batched_frames, n_hi=1e5)
+    serving = run_serving(device, args.serve_seconds) if args.serve_seconds > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -372,6 +450,7 @@ def run_gpu(args, world, rank, local):
         "clocks": clk.summary(),
         "fp64_svd_lanes": fp64_lanes,
         "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -386,6 +465,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--e2e-frames", type=int, default=4, help="24 fps frames timed through the solver API")
+    ap.add_argument("--serve-seconds", type=float, default=5.0,
+                    help="seconds of Poisson bake requests (4 per second) for the serving measurement (0: skip)")
     ap.add_argument("--batched-frames", type=int, default=3,
                     help="frames of the 64-scene batched workload, plain and batched (0: skip)")
     args = ap.parse_args()

@@ -205,3 +205,67 @@ def batched_scenes(seed: int = 0, count: int = 64, n_lo: float = 1e4, n_hi: floa
             cols.append((cv, ct, xf, float(rng.uniform(0.0, 0.5))))
         out.append((d, [mat], pos, vel, cols))
     return out
+
+
+def torus(major: float, minor: float, n_major: int, n_minor: int, seed: int | None = None, jitter: float = 0.0):
+    """Closed torus around the z axis (2 * n_major * n_minor triangles, outward winding); with a seed every
+    vertex's tube radius is scaled by 1 + U(-jitter, jitter)."""
+    u = 2 * np.pi * np.arange(n_major) / n_major
+    v = 2 * np.pi * np.arange(n_minor) / n_minor
+    r = np.full((n_major, n_minor), minor)
+    if seed is not None:
+        r = r * (1 + np.random.default_rng(seed).uniform(-jitter, jitter, r.shape))
+    cu, su, cv, sv = np.cos(u)[:, None], np.sin(u)[:, None], np.cos(v)[None, :], np.sin(v)[None, :]
+    verts = np.stack([(major + r * cv) * cu, (major + r * cv) * su, r * sv], -1).reshape(-1, 3)
+    i, j = np.meshgrid(np.arange(n_major), np.arange(n_minor), indexing="ij")
+    a = i * n_minor + j
+    b = ((i + 1) % n_major) * n_minor + j
+    c = ((i + 1) % n_major) * n_minor + (j + 1) % n_minor
+    d = i * n_minor + (j + 1) % n_minor
+    tris = np.concatenate([np.stack([a, b, c], -1).reshape(-1, 3), np.stack([a, c, d], -1).reshape(-1, 3)])
+    return verts.astype(np.float32), tris.astype(np.int32)
+
+
+def rot_z(deg: float) -> np.ndarray:
+    c, s = np.cos(np.radians(deg)), np.sin(np.radians(deg))
+    m = np.eye(4)
+    m[:2, :2] = [[c, -s], [s, c]]
+    return m
+
+
+def pour_job_spec(seed: int, res: int = 96, frames: int = 12, fps: float = 24.0):
+    """A granular pour (the large inflow workload's distribution at a serving size): a Drucker-Prager pile
+    (E 3.5e5, nu 0.3, 30 deg, rho 1600) of seeded size, a disc inflow r = 0.05 m at 2 m/s downward whose slab
+    of one frame is added where no material is, and a seeded torus collider (2,048 triangles, friction 0.4)
+    turning at 1 rev/s. Returns (domain, materials, setup(solver), before_frame(solver, k), frames, fps,
+    max_particles, collider_triangles)."""
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+
+    rng = np.random.default_rng(seed)
+    d = domain(res=res)
+    mat = MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)
+    side = float(rng.uniform(0.2, 0.4))
+    pile = lattice_box((0.5 - side / 2, 0.5 - side / 2, 0.0), (0.5 + side / 2, 0.5 + side / 2, side / 2), d.dx / 2,
+                       rng)
+    tv, tt = torus(0.18, 0.04, 64, 16, seed=seed, jitter=0.05)
+
+    def pose(t):
+        return translate(0.5, 0.5, 0.35) @ rot_z(360.0 * t) @ rot_x(90.0)
+
+    def setup(s):
+        s.add_particles(pile, np.zeros_like(pile), np.zeros(len(pile), np.int32), np.zeros(len(pile), np.int32))
+        s.set_colliders([ColliderGeometry(MeshData(tv, tt), closed=True, friction=0.4)])
+
+    def before_frame(s, k):
+        s.set_collider_transforms(pose((k - 1) / fps)[None], pose(k / fps)[None])
+        r = np.random.default_rng(seed * 1000 + k)
+        slab = lattice_box((0.45, 0.45, 0.85), (0.55, 0.55, 0.85 + 2.0 / fps), d.dx / 2, r)
+        slab = slab[np.hypot(slab[:, 0] - 0.5, slab[:, 1] - 0.5) <= 0.05]
+        free = ~s.is_occupied(slab)
+        if free.any():
+            p = slab[free]
+            s.add_particles(p, np.tile(np.float32([0.0, 0.0, -2.0]), (len(p), 1)), np.zeros(len(p), np.int32),
+                            np.zeros(len(p), np.int32))
+
+    slab_n = int(np.pi * 0.05 ** 2 * 2.0 / fps * 8 * res ** 3) + 1
+    return d, [mat], setup, before_frame, frames, fps, len(pile) + frames * slab_n, len(tt)
