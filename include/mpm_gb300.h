@@ -112,8 +112,11 @@ enum {
     MPM_OPT_USE_GRAPH = 1,     /* 1 (default): replay a captured CUDA graph per substep */
     MPM_OPT_KERNEL_TIMING = 2, /* 1: record CUDA events between the kernel groups of every substep (event nodes
                                   in the captured graph); each substep then waits for its own completion */
-    MPM_OPT_SORT_INTERVAL = 3  /* N (default 4): after every N substeps the particle storage is reordered into
+    MPM_OPT_SORT_INTERVAL = 3, /* N (default 4): after every N substeps the particle storage is reordered into
                                   grid-block order (ids travel along, so host order is unchanged); 0: never */
+    MPM_OPT_DETERMINISTIC = 4  /* 1: bit-reproducible runs. P2G and the occupancy splat sum in 64-bit fixed point
+                                  (exact integer additions, independent of particle order and atomic timing);
+                                  results agree with the default mode within float rounding. 0 (default) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

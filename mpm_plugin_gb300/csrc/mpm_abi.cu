@@ -127,6 +127,11 @@ struct Handle {
     int sort_interval = 4;       // reorder the particles by grid node after every this many substeps (0: never)
     int64_t since_sort = 0;
 
+    bool deterministic = false;
+    unsigned long long* d_fixed = nullptr;  // deterministic mode: fixed-point node sums (4 per node)
+    unsigned int* d_poison = nullptr;       // deterministic mode: non-finite marks (1 per node)
+    int fixed_exp = 0;
+
     bool use_graph = true;
     GraphCache graphs;           // the substep graph, one per particle arena (the reorder alternates two)
 
@@ -240,11 +245,41 @@ Status ensure_stage(Handle* h, size_t bytes) {
     return {};
 }
 
+// Deterministic mode: fixed-point accumulators for every node, zeroed (the active-block clear keeps them
+// zero afterwards), and the fixed-point exponent: 2^-e = 2^-40 of the heaviest particle's mass, so a node
+// (at most 27 x 8 particles) stays far below 2^63 while one particle's contribution keeps ~40 bits.
+Status set_deterministic(Handle* h, bool on) {
+    if (on == h->deterministic) return {};
+    CK(cudaStreamSynchronize(h->stream));
+    invalidate_graph(h);
+    if (on && !h->d_fixed) {
+        if (cudaMalloc(&h->d_fixed, sizeof(unsigned long long) * 4 * (size_t)h->grid_nodes) != cudaSuccess ||
+            cudaMalloc(&h->d_poison, sizeof(unsigned int) * (size_t)h->grid_nodes) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(h->d_fixed);
+            h->d_fixed = nullptr;
+            return {MPM_ERR_MEMORY, "device allocation of the deterministic-mode accumulators failed"};
+        }
+    }
+    if (on) {
+        CK(cudaMemsetAsync(h->d_fixed, 0, sizeof(unsigned long long) * 4 * (size_t)h->grid_nodes, h->stream));
+        CK(cudaMemsetAsync(h->d_poison, 0, sizeof(unsigned int) * (size_t)h->grid_nodes, h->stream));
+        double pm = 0.0;
+        for (const auto& m : h->mat_desc) pm = std::max(pm, (double)(float)(m.density * h->p_vol));
+        h->fixed_exp = std::clamp(40 - (int)std::ceil(std::log2(std::max(pm, 1e-30))), -60, 100);
+        // the grid must start zero, as the float path leaves it: clear whatever the last substep touched
+        CK(cudaMemsetAsync(h->grid, 0, (size_t)h->grid_nodes * sizeof(float4), h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+    }
+    h->deterministic = on;
+    return {};
+}
+
 // Device memory the handle holds now (the allocations it made, by their sizes).
 int64_t handle_device_bytes(const Handle* h) {
     const int64_t nblk = (int64_t)h->g.nb[0] * h->g.nb[1] * h->g.nb[2];
     int64_t b = (int64_t)h->P.cap * kFields * 4 * (h->spare_arena ? 2 : 1);
-    b += h->grid_nodes * 16 + (h->vol ? h->grid_nodes * 4 : 0);
+    b += h->grid_nodes * 16 + (h->vol ? h->grid_nodes * 4 : 0) + (h->d_fixed ? h->grid_nodes * 36 : 0);
     b += nblk * 12 + h->grid_nodes * 4 + h->part_cand_cap * 4 + 16;                      // work lists
     b += h->ss_cap * 12 + (h->grid_nodes + 1) * 8 + (h->ss_scan_cap + 2) * 4;           // sort
     b += h->keep_cap * 16 + (h->scan_cap + 2) * 4;                                       // removal
@@ -295,6 +330,9 @@ SubstepArgs substep_args(Handle* h) {
     a.cd.tris = h->d_tris;
     a.cd.cells = h->d_sdf_cells;
     a.cd.cand = h->d_sdf_cand;
+    a.fixed = h->deterministic ? h->d_fixed : nullptr;
+    a.poison = h->deterministic ? h->d_poison : nullptr;
+    a.fixed_exp = h->fixed_exp;
     return a;
 }
 
@@ -828,6 +866,8 @@ void destroy(Handle* h) {
     cudaFree(h->wl.counts);
     cudaFree(h->wl.node_cand);
     cudaFree(h->wl.part_cand);
+    cudaFree(h->d_fixed);
+    cudaFree(h->d_poison);
     cudaFree(h->ss.key);
     cudaFree(h->ss.count);
     cudaFree(h->ss.start);
@@ -1264,9 +1304,15 @@ int mpm_is_occupied(void* handle, int64_t m, const float* points, uint8_t* out) 
         float* dpts = static_cast<float*>(h->stage);
         uint8_t* dout = reinterpret_cast<uint8_t*>(dpts + 3 * m);
         CK(cudaMemsetAsync(h->vol, 0, (size_t)h->grid_nodes * sizeof(float), h->stream));
-        launch_scatter_volume(h->stream, h->P, h->g, h->vol);
         CK(cudaMemcpyAsync(dpts, points, (size_t)m * 12, cudaMemcpyHostToDevice, h->stream));
-        launch_query_fill(h->stream, h->g, h->vol, (float)std::pow(h->dx, 3.0), m, dpts, dout);
+        if (h->deterministic) {
+            unsigned int* vol = reinterpret_cast<unsigned int*>(h->vol);
+            launch_scatter_volume_fixed(h->stream, h->P, h->g, vol);
+            launch_query_fill_fixed(h->stream, h->g, vol, std::pow(h->dx, 3.0), m, dpts, dout);
+        } else {
+            launch_scatter_volume(h->stream, h->P, h->g, h->vol);
+            launch_query_fill(h->stream, h->g, h->vol, (float)std::pow(h->dx, 3.0), m, dpts, dout);
+        }
         h->launches += 2;
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(out, dout, (size_t)m, cudaMemcpyDeviceToHost, h->stream));
@@ -1286,6 +1332,8 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
         case MPM_OPT_KERNEL_TIMING:
             h->timing = value != 0;
             return MPM_OK;
+        case MPM_OPT_DETERMINISTIC:
+            return finish(h, set_deterministic(h, value != 0));
         case MPM_OPT_SORT_INTERVAL:
             if (value < 0 || value > (1 << 30)) return finish(h, {MPM_ERR_VALUE, "sort interval out of range"});
             h->sort_interval = (int)value;

@@ -42,6 +42,11 @@ struct BatchLaunch {
 };
 void launch_batch_substep(cudaStream_t st, const BatchLaunch& b);
 int batch_substep_kernel_count(const BatchLaunch& b);
+// Occupancy in deterministic mode: the volume splat as fixed-point integers (unsigned per node, 2^-20
+// particle volumes per unit) and the query against 0.5 cell_vol in those units.
+void launch_scatter_volume_fixed(cudaStream_t st, const Particles& P, const GridDesc& g, unsigned int* vol);
+void launch_query_fill_fixed(cudaStream_t st, const GridDesc& g, const unsigned int* vol, double cell_vol, int64_t m,
+                             const float* pts, uint8_t* out);
 // Counting sort of the particles by the grid node of their stencil base: fills ss.order (scan_tmp: scan
 // scratch of scan_cap + 2 entries, at least scan_tile_count(n_nodes + 1) + 1).
 void launch_sort(cudaStream_t st, const Particles& P, const GridDesc& g, const SortScratch& ss, int64_t n_nodes,

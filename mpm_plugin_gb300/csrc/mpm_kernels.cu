@@ -316,6 +316,49 @@ __global__ void k_query_fill(GridDesc g, const float* __restrict__ vol, float ce
     out[q] = inside && vol[node_index(g, idx[0], idx[1], idx[2])] >= 0.5f * cell_vol ? 1 : 0;
 }
 
+// Deterministic mode: the same splat in fixed point, 2^-20 particle volumes per unit (integer sums do not
+// depend on the order they arrive in; a node holds at most 27 x 8 x 2^20 < 2^28 units at 8 per cell).
+constexpr float kVolUnits = 1048576.0f;  // 2^20
+
+__global__ void k_scatter_volume_fixed(Particles P, GridDesc g, unsigned int* __restrict__ vol) {
+    int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= P.n) return;
+    int base[3];
+    float fx, w[3][3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float xp = (P.x[a][p] - g.origin[a]) * g.inv_dx;
+        inside &= stencil_axis(xp, g.dims[a], &base[a], &fx);
+        bspline_weights(fx, w[a]);
+    }
+    if (!inside) return;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+                atomicAdd(&vol[node_index(g, base[0] + i, base[1] + j, base[2] + k)],
+                          __float2uint_rn(w[0][i] * w[1][j] * w[2][k] * kVolUnits));
+}
+
+// threshold: 0.5 dx^3 in the same units (0.5 dx^3 / p_vol * 2^20)
+__global__ void k_query_fill_fixed(GridDesc g, const unsigned int* __restrict__ vol, double threshold, int64_t m,
+                                   const float* __restrict__ pts, uint8_t* __restrict__ out) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    int idx[3];
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float gq = (pts[q * 3 + a] - g.origin[a]) * g.inv_dx;
+        idx[a] = (int)copysignf(floorf(fabsf(gq) + 0.5f), gq);  // round half away from zero
+        if (idx[a] < 0 || idx[a] >= g.dims[a]) inside = false;
+    }
+    out[q] = inside && (double)vol[node_index(g, idx[0], idx[1], idx[2])] >= threshold ? 1 : 0;
+}
+
 // grid read-back: blocked layout -> C order (i, j, k) with 4 floats per node
 __global__ void k_grid_unblock(GridDesc g, const float4* __restrict__ grid, float4* __restrict__ out) {
     int64_t n = (int64_t)g.dims[0] * g.dims[1] * g.dims[2];
@@ -470,6 +513,18 @@ void launch_exclusive_scan(cudaStream_t st, const int32_t* in, int64_t n, int32_
 void launch_scatter_volume(cudaStream_t st, const Particles& P, const GridDesc& g, float* vol) {
     if (P.n == 0) return;
     k_scatter_volume<<<blocks_for(P.n, 256), 256, 0, st>>>(P, g, vol);
+}
+
+void launch_scatter_volume_fixed(cudaStream_t st, const Particles& P, const GridDesc& g, unsigned int* vol) {
+    if (P.n == 0) return;
+    k_scatter_volume_fixed<<<blocks_for(P.n, 256), 256, 0, st>>>(P, g, vol);
+}
+
+void launch_query_fill_fixed(cudaStream_t st, const GridDesc& g, const unsigned int* vol, double cell_vol, int64_t m,
+                             const float* pts, uint8_t* out) {
+    if (m == 0) return;
+    const double threshold = 0.5 * cell_vol / (double)g.p_vol * (double)kVolUnits;
+    k_query_fill_fixed<<<blocks_for(m, 256), 256, 0, st>>>(g, vol, threshold, m, pts, out);
 }
 
 void launch_grid_unblock(cudaStream_t st, const GridDesc& g, const float4* grid, float4* out) {

@@ -126,8 +126,58 @@ __global__ void k_step_begin(Scenes sc) {
 __device__ __forceinline__ void clear_block(const SubstepArgs& a, unsigned int i) {
     const unsigned int prev = (a.sp->seq - 1u) & 1u;
     const int64_t b = active_blocks(a.wl, prev)[i];
-    a.grid[b * 64 + (threadIdx.x & 63)] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t q = b * 64 + (threadIdx.x & 63);
+    a.grid[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.fixed) {
+        reinterpret_cast<ulonglong2*>(a.fixed)[2 * q] = make_ulonglong2(0ull, 0ull);
+        reinterpret_cast<ulonglong2*>(a.fixed)[2 * q + 1] = make_ulonglong2(0ull, 0ull);
+        a.poison[q] = 0u;
+    }
     if ((threadIdx.x & 63) == 0) a.wl.block_flag[b] = 0u;
+}
+
+// Deterministic-mode P2G of one warp (k_p2g_scatter's arguments): every contribution becomes a 64-bit
+// fixed-point integer (the float times 2^fixed_exp, exact, then rounded to an integer) before it is summed,
+// so the warp sums and the global atomics are exact integer additions and the node totals do not depend on
+// particle order or atomic timing. A non-finite or out-of-range contribution poisons its node instead (the
+// grid update then makes that node NaN, as a float sum would).
+__device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTerms& t, bool valid, bool leader,
+                                               int tail, int span) {
+    const GridDesc& g = a.g;
+    const float scale = __int_as_float((127 + a.fixed_exp) << 23);  // 2^fixed_exp
+#pragma unroll
+    for (int n = 0; n < 27; ++n) {
+        const int i = n / 9, j = (n / 3) % 3, k = n % 3;
+        float val[4] = {0.f, 0.f, 0.f, 0.f};
+        if (valid) p2g_node(t, g, i, j, k, val);
+        long long q[4];
+        bool bad = false;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const float x = val[c] * scale;
+            const bool ok = fabsf(x) < 4.0e18f;  // false for NaN and inf too
+            bad |= !ok;
+            q[c] = ok ? __float2ll_rn(x) : 0ll;
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            if (d <= span) {  // warp-uniform
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const long long o = __shfl_down_sync(0xffffffffu, q[c], d);
+                    if (d <= tail) q[c] += o;
+                }
+            }
+        }
+        const int64_t node = valid ? node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k) : 0;
+        if (valid && bad) atomicOr(&a.poison[node], 1u);
+        if (leader) {
+            unsigned long long* f = a.fixed + node * 4;
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+                if (q[c] != 0) atomicAdd(&f[c], (unsigned long long)q[c]);
+        }
+    }
 }
 
 template <class Scenes>
@@ -180,6 +230,10 @@ __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
         const unsigned int cur = a.sp->seq & 1u;
         mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, cur), &a.wl.counts[cur]);
     }
+    if (a.fixed) {
+        p2g_fixed_warp(a, t, valid, leader, tail, span);
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -215,6 +269,17 @@ __device__ __forceinline__ void grid_update_block(const SubstepArgs& a, unsigned
     const int bj = (int)((b / g.nb[2]) % g.nb[1]);
     const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
     const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+    if (a.fixed) {  // deterministic mode: the node's fixed-point sums become its float momentum and mass
+        const int64_t q = b * 64 + l;
+        const ulonglong2 f01 = reinterpret_cast<const ulonglong2*>(a.fixed)[2 * q];
+        const ulonglong2 f23 = reinterpret_cast<const ulonglong2*>(a.fixed)[2 * q + 1];
+        const double inv = ldexp(1.0, -a.fixed_exp);
+        float4 v = make_float4((float)((double)(long long)f01.x * inv), (float)((double)(long long)f01.y * inv),
+                               (float)((double)(long long)f23.x * inv), (float)((double)(long long)f23.y * inv));
+        if (a.poison[q]) v = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                                         __int_as_float(0x7fc00000), v.w);
+        a.grid[q] = v;
+    }
     bool has_mass = grid_node_walls(g, &a.grid[b * 64 + l], idx, a.sp->dt);
     if (has_mass && a.cd.n_col > 0) {
         ColliderData cd = a.cd;

@@ -160,6 +160,12 @@ struct SubstepArgs {
     unsigned int* fp64;
     WorkLists wl;
     ColliderData cd;  // poses: the start of the pose array; kernels add the substep's pose_base
+    // Deterministic mode (null when off): P2G accumulates momentum xyz and mass of every node as 64-bit
+    // fixed point in units of 2^-fixed_exp (integer sums are exact, so the result does not depend on the
+    // order contributions arrive in); poison marks nodes that received a non-finite or out-of-range value.
+    unsigned long long* fixed;
+    unsigned int* poison;
+    int fixed_exp;
 };
 
 // The field pointers of a particle arena: plane f starts at arena + f * cap (x3 v3 C9 F9 Jp tau6 mat
