@@ -181,6 +181,9 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
             plain_s += el
             plain_frame_ms.append(1e3 * el)
     batch = Gb300Batch(solvers)
+    from mpm_plugin_gb300 import tune
+
+    tuned = tune.tune_batch(batch, BATCH_FRAME_DT, frames=1)
     batch.advance(BATCH_FRAME_DT)
     launches0 = batch.launch_count()
     batch_ps, batch_s, batch_frame_ms = 0.0, 0.0, []
@@ -201,7 +204,7 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
                                "p99": float(np.percentile(batch_frame_ms, 99))},
             "plain_scene_frame_ms": {"p50": float(np.percentile(plain_frame_ms, 50)),
                                      "p99": float(np.percentile(plain_frame_ms, 99))},
-            "gpu_launches_per_frame": launches / frames,
+            "gpu_launches_per_frame": launches / frames, "tuned": tuned,
             "timing": "host clock around advance calls with device synchronisation; state resident in HBM"}
 
 
@@ -355,6 +358,9 @@ def run_gpu(args, world, rank, local):
     stream = torch.cuda.ExternalStream(solver.stream, device=device)  # the flush runs on the solver's stream
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
 
+    from mpm_plugin_gb300 import tune
+
+    tuned = tune.tune_solver(solver, DT, FRAME_DT, substeps=10)  # launch choices for this GPU and workload
     for _ in range(args.warmup):
         solver.substep(DT, 1.0, FRAME_DT)
     solver.synchronize()
@@ -379,6 +385,21 @@ def run_gpu(args, world, rank, local):
     launches = solver.launch_count() - launches0
     ktimes = solver.kernel_times(reset=True)
     total_ms = sum(t for t, _ in ktimes.values())
+
+    # the same timed substeps in deterministic mode (fixed-point P2G)
+    solver.set_option(_abi.OPT_DETERMINISTIC, 1)
+    for _ in range(3):
+        solver.substep(DT, 1.0, FRAME_DT)
+    solver.kernel_times(reset=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            solver.substep(DT, 1.0, FRAME_DT)
+    torch.cuda.synchronize()
+    det_times = solver.kernel_times(reset=True)
+    det_ms = sum(t for t, _ in det_times.values())
+    solver.set_option(_abi.OPT_DETERMINISTIC, 0)
     solver.set_option(_abi.OPT_KERNEL_TIMING, 0)
 
     # end to end through the solver API: one bake frame per step, host buffers
@@ -449,6 +470,9 @@ def run_gpu(args, world, rank, local):
         "gpu_launches": launches,
         "clocks": clk.summary(),
         "fp64_svd_lanes": fp64_lanes,
+        "tuned": tuned,
+        "deterministic": {"value": n * args.steps / (det_ms / 1e3), "unit": UNIT,
+                          "kernels_ms_per_launch": {k: t / max(c, 1) for k, (t, c) in det_times.items()}},
         "batched": batched,
         "serving": serving,
     }

@@ -36,7 +36,7 @@ struct Status {
 // Instantiated substep graphs keyed by what the kernels' arguments depend on; two entries, so the two
 // particle arenas that the reorder alternates between both keep their graph.
 struct GraphCache {
-    static constexpr int kKey = 6;
+    static constexpr int kKey = 8;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     int64_t key[2][kKey] = {};
     int last = 0;
@@ -127,6 +127,7 @@ struct Handle {
     int sort_interval = 4;       // reorder the particles by grid node after every this many substeps (0: never)
     int64_t since_sort = 0;
 
+    LaunchShape shape;                      // autotuned launch choices
     bool deterministic = false;
     unsigned long long* d_fixed = nullptr;  // deterministic mode: fixed-point node sums (4 per node)
     unsigned int* d_poison = nullptr;       // deterministic mode: non-finite marks (1 per node)
@@ -418,7 +419,7 @@ void accumulate_times(Handle* h, const cudaEvent_t* ev) {  // ev: | clear | P2G 
 Status capture_graph(Handle* h, const SubstepArgs& a, cudaEvent_t* ev, cudaGraphExec_t* out) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    launch_substep(h->stream, a, ev, true);
+    launch_substep(h->stream, a, h->shape, ev, true);
     cudaError_t e0 = cudaGetLastError();
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     CK(e0);
@@ -434,16 +435,17 @@ Status run_substep(Handle* h) {
     SubstepArgs a = substep_args(h);
     const int kernels = substep_kernel_count(a);
     h->launches += kernels;
-    int64_t key[6] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena, (int64_t)(intptr_t)h->d_poses,
-                      (int64_t)(intptr_t)h->wl.part_cand};
+    int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
+                                     (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
+                                     (int64_t)h->shape.list_ctas, (int64_t)h->shape.g2p_variant};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
             for (auto& e : ev) e = take_event(h);
-            launch_substep(h->stream, a, ev.data(), false);
+            launch_substep(h->stream, a, h->shape, ev.data(), false);
             h->ev_pending.push_back(ev);
         } else {
-            launch_substep(h->stream, a, nullptr, false);
+            launch_substep(h->stream, a, h->shape, nullptr, false);
         }
         CK(cudaGetLastError());
         return {};
@@ -957,6 +959,7 @@ struct Batch {
     unsigned int* h_vmax = nullptr;          // pinned
     int vmax_cap = 0;
     int sort_interval = 4;
+    LaunchShape shape;
     int64_t launches = 0;
     std::string err;
 };
@@ -1029,7 +1032,7 @@ Status batch_upload(Batch* b) {
 
 Status batch_replay(Batch* b) {
     BatchLaunch bl{b->d_table, b->d_cta, b->d_cta + b->particle_ctas, (int)b->live.size(), b->particle_ctas,
-                   b->any_colliders};
+                   b->any_colliders, b->shape};
     if (!b->graph) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -1334,6 +1337,14 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             return MPM_OK;
         case MPM_OPT_DETERMINISTIC:
             return finish(h, set_deterministic(h, value != 0));
+        case MPM_OPT_G2P_VARIANT:
+            if (value != 0 && value != 1) return finish(h, {MPM_ERR_VALUE, "G2P variant must be 0 or 1"});
+            h->shape.g2p_variant = (int)value;
+            return MPM_OK;
+        case MPM_OPT_LIST_CTAS:
+            if (value < 1 || value > (1 << 20)) return finish(h, {MPM_ERR_VALUE, "work-list CTAs out of range"});
+            h->shape.list_ctas = (unsigned int)value;
+            return MPM_OK;
         case MPM_OPT_SORT_INTERVAL:
             if (value < 0 || value > (1 << 30)) return finish(h, {MPM_ERR_VALUE, "sort interval out of range"});
             h->sort_interval = (int)value;
@@ -1499,6 +1510,18 @@ int mpm_batch_set_option(void* batch, int32_t option, int64_t value) {
     if (option == MPM_OPT_SORT_INTERVAL) {
         if (value < 0 || value > (1 << 30)) return finish_batch(b, {MPM_ERR_VALUE, "sort interval out of range"});
         b->sort_interval = (int)value;
+        return MPM_OK;
+    }
+    if (option == MPM_OPT_G2P_VARIANT) {
+        if (value != 0 && value != 1) return finish_batch(b, {MPM_ERR_VALUE, "G2P variant must be 0 or 1"});
+        b->shape.g2p_variant = (int)value;
+        batch_invalidate(b);
+        return MPM_OK;
+    }
+    if (option == MPM_OPT_LIST_CTAS) {
+        if (value < 1 || value > (1 << 20)) return finish_batch(b, {MPM_ERR_VALUE, "work-list CTAs out of range"});
+        b->shape.list_ctas = (unsigned int)value;
+        batch_invalidate(b);
         return MPM_OK;
     }
     return finish_batch(b, {MPM_ERR_VALUE, "unknown option"});

@@ -26,7 +26,13 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 // One substep: step counters, clear of the previous blocks, P2G, grid update, collider contact, G2P,
 // particle projection. With ev (5 events), records ev[0..4] around: clear | P2G | grid | G2P (as event
 // nodes when `capturing`).
-void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool capturing);
+// Launch choices the autotuner sets: CTAs of the kernels that walk work lists, and the G2P build (0: capped
+// at 80 registers, 3 CTAs of 256 per SM; 1: uncapped).
+struct LaunchShape {
+    unsigned int list_ctas = kListCtas;
+    int g2p_variant = 0;
+};
+void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing);
 int substep_kernel_count(const SubstepArgs& a);
 
 // One batched substep over a device table of scenes (mpm_batch_kernels.cu). The particle kernels run
@@ -39,6 +45,7 @@ struct BatchLaunch {
     int n_scenes;
     unsigned int particle_ctas;
     bool any_colliders;
+    LaunchShape shape;
 };
 void launch_batch_substep(cudaStream_t st, const BatchLaunch& b);
 int batch_substep_kernel_count(const BatchLaunch& b);

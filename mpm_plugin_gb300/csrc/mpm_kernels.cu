@@ -409,8 +409,8 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
     k_collider_poses<<<blocks_for(total, 128), 128, 0, st>>>(cols, n_col, poses, steps, s_given, inv_frame_dt);
 }
 
-void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool capturing) {
-    const unsigned int list_ctas = kListCtas;
+void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing) {
+    const unsigned int list_ctas = shape.list_ctas;
     const OneScene sc{a};
     // while a graph is being captured the records become event nodes that fire on every replay
     auto mark = [&](int i) {
@@ -425,7 +425,12 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, cudaEvent_t* ev, bool
     k_grid_update<<<list_ctas, 256, 0, st>>>(sc);
     if (a.cd.n_col > 0) k_grid_colliders<<<list_ctas, 128, 0, st>>>(sc);
     mark(3);
-    if (a.n > 0) k_g2p<<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+    if (a.n > 0) {
+        if (shape.g2p_variant == 1)
+            k_g2p<OneScene, 1><<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+        else
+            k_g2p<OneScene, 3><<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+    }
     if (a.cd.n_col > 0) k_project_particles<<<list_ctas, 128, 0, st>>>(sc);
     mark(4);
 }

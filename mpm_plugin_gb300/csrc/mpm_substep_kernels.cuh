@@ -342,11 +342,12 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
     }
 }
 
-// G2P; particles that end inside a collider's margin box are listed for k_project_particles. Capped at 80
-// registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra resident warps
-// outweigh the few spilled values (measured 10 % faster than the uncapped 120 registers).
-template <class Scenes>
-__global__ void __launch_bounds__(256, 3) k_g2p(Scenes sc) {
+// G2P; particles that end inside a collider's margin box are listed for k_project_particles. kMinCtas = 3
+// caps it at 80 registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra
+// resident warps outweighed the few spilled values on the mixed workload (10 % faster than kMinCtas = 1,
+// 120 registers). Both are built; the autotuner picks one per workload.
+template <class Scenes, int kMinCtas>
+__global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
     if (!sc.active(a)) return;

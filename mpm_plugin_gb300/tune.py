@@ -1,0 +1,163 @@
+"""Autotuner: picks a solver's (or batch's) launch choices by timing them on the workload itself, and caches
+the choice per GPU and workload class.
+
+Knobs (C options of include/mpm_gb300.h):
+  sort_interval      reorder of the particles by grid node after every N substeps (0: never);
+  g2p_variant        G2P build: 0 capped at 80 registers (3 CTAs of 256 per SM), 1 uncapped;
+  list_ctas_per_sm   CTAs per SM of the kernels that walk the active-block and candidate lists.
+
+Search: coordinate descent from the defaults, one knob at a time over its candidates with the others fixed,
+keeping a change only when it is at least 2 % faster. A configuration is timed by the CUDA events the
+solver records between its kernel groups (MPM_OPT_KERNEL_TIMING) over `substeps` substeps after 3 warm-up
+substeps. The solver's state is saved before and loaded back after, so tuning does not advance the bake
+(a load recomputes the stored stress from F, a last-bit change).
+
+Cache: JSON at $MPM_GB300_TUNE_CACHE or ~/.cache/mpm_plugin_gb300/autotune.json, keyed by the GPU (name,
+SM count) and the workload class (grid resolution and particle count rounded to powers of two, colliders,
+deterministic mode).
+"""
+
+from __future__ import annotations
+
+import json
+import math
+import os
+from pathlib import Path
+
+from mpm_plugin_gb300 import _abi
+
+DEFAULTS = {"sort_interval": 4, "g2p_variant": 0, "list_ctas_per_sm": 8}
+CANDIDATES = {"sort_interval": (0, 2, 4, 8, 16), "g2p_variant": (0, 1), "list_ctas_per_sm": (4, 8, 16)}
+KNOB_ORDER = ("g2p_variant", "sort_interval", "list_ctas_per_sm")
+MIN_GAIN = 0.02
+
+
+def cache_path() -> Path:
+    env = os.environ.get("MPM_GB300_TUNE_CACHE")
+    return Path(env) if env else Path.home() / ".cache" / "mpm_plugin_gb300" / "autotune.json"
+
+
+def gpu_key(device: str = "cuda:0") -> tuple[str, int]:
+    import torch
+
+    p = torch.cuda.get_device_properties(torch.device(device))
+    return f"{p.name}|{p.multi_processor_count}", int(p.multi_processor_count)
+
+
+def workload_key(resolution: int, particles: int, colliders: bool, deterministic: bool = False) -> str:
+    r = 2 ** round(math.log2(max(resolution, 1)))
+    n = 2 ** round(math.log2(max(particles, 1)))
+    return f"res{r}|n{n}|col{int(bool(colliders))}|det{int(bool(deterministic))}"
+
+
+def load_cache(path: Path | None = None) -> dict:
+    path = path or cache_path()
+    try:
+        return json.loads(Path(path).read_text())
+    except (OSError, ValueError):
+        return {}
+
+
+def store_cache(cache: dict, path: Path | None = None) -> None:
+    path = Path(path or cache_path())
+    path.parent.mkdir(parents=True, exist_ok=True)
+    tmp = path.with_suffix(".tmp")
+    tmp.write_text(json.dumps(cache, indent=1, sort_keys=True))
+    tmp.replace(path)
+
+
+def apply(target, cfg: dict, sms: int) -> None:
+    """Set a configuration on a Gb300Solver or Gb300Batch."""
+    target.set_option(_abi.OPT_SORT_INTERVAL, int(cfg["sort_interval"]))
+    target.set_option(_abi.OPT_G2P_VARIANT, int(cfg["g2p_variant"]))
+    target.set_option(_abi.OPT_LIST_CTAS, int(cfg["list_ctas_per_sm"]) * sms)
+
+
+def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, min_gain=MIN_GAIN):
+    """Coordinate descent: measure(cfg) -> seconds (lower is better). Returns (best cfg, its time, trials)."""
+    best = dict(defaults)
+    best_t = measure(best)
+    trials = [(dict(best), best_t)]
+    seen = {tuple(sorted(best.items()))}
+    for knob in order:
+        for value in candidates[knob]:
+            cfg = {**best, knob: value}
+            key = tuple(sorted(cfg.items()))
+            if key in seen:
+                continue
+            seen.add(key)
+            t = measure(cfg)
+            trials.append((cfg, t))
+            if t < best_t * (1.0 - min_gain):
+                best, best_t = cfg, t
+    return best, best_t, trials
+
+
+def _time_solver(solver, cfg, sms, dt, frame_dt, substeps):
+    apply(solver, cfg, sms)
+    for _ in range(3):
+        solver.substep(dt, 1.0, frame_dt)
+    solver.set_option(_abi.OPT_KERNEL_TIMING, 1)
+    solver.kernel_times(reset=True)
+    for _ in range(substeps):
+        solver.substep(dt, 1.0, frame_dt)
+    ms = sum(t for t, _ in solver.kernel_times(reset=True).values())
+    solver.set_option(_abi.OPT_KERNEL_TIMING, 0)
+    return ms / 1e3 / substeps
+
+
+def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20, path: Path | None = None,
+                force: bool = False, deterministic: bool = False) -> dict:
+    """Choose and set the solver's launch choices for its current scene; returns the configuration with
+    ``cached`` (whether it came from the cache) and, when measured, ``seconds_per_substep``."""
+    gkey, sms = gpu_key(solver.device)
+    wkey = workload_key(max(solver.domain.grid_shape), solver.particle_count, solver._n_colliders > 0, deterministic)
+    cache = load_cache(path)
+    hit = cache.get(gkey, {}).get(wkey)
+    if hit and not force:
+        apply(solver, hit, sms)
+        return {**hit, "cached": True}
+    snapshot = solver.save_state()
+    best, best_t, trials = search(lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps))
+    solver.load_state(snapshot)
+    apply(solver, best, sms)
+    cache.setdefault(gkey, {})[wkey] = best
+    store_cache(cache, path)
+    return {**best, "cached": False, "seconds_per_substep": best_t, "trials": len(trials)}
+
+
+def tune_batch(batch, frame_dt: float, frames: int = 2, path: Path | None = None, force: bool = False) -> dict:
+    """The same for a batch, timing whole batched frames; every scene's state is restored afterwards."""
+    import time
+
+    import torch
+
+    scenes = batch.scenes
+    gkey, sms = gpu_key(scenes[0].device)
+    n = sum(s.particle_count for s in scenes)
+    res = max(max(s.domain.grid_shape) for s in scenes)
+    wkey = "batch|" + workload_key(res, n, any(s._n_colliders > 0 for s in scenes)) + f"|scenes{len(scenes)}"
+    cache = load_cache(path)
+    hit = cache.get(gkey, {}).get(wkey)
+    if hit and not force:
+        apply(batch, hit, sms)
+        return {**hit, "cached": True}
+    snapshots = [s.save_state() for s in scenes]
+
+    def measure(cfg):
+        apply(batch, cfg, sms)
+        batch.advance(frame_dt)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            batch.advance(frame_dt)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / frames
+
+    best, best_t, trials = search(measure)
+    for s, st in zip(scenes, snapshots):
+        s.load_state(st)
+    apply(batch, best, sms)
+    cache.setdefault(gkey, {})[wkey] = best
+    store_cache(cache, path)
+    return {**best, "cached": False, "seconds_per_frame": best_t, "trials": len(trials)}
