@@ -118,8 +118,10 @@ enum {
                                   (exact integer additions, independent of particle order and atomic timing);
                                   results agree with the default mode within float rounding. 0 (default) */
     MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 80 registers, 3 CTAs of 256 per SM; 1 uncapped */
-    MPM_OPT_LIST_CTAS = 6      /* CTAs of the kernels that walk the active-block and candidate lists (default
+    MPM_OPT_LIST_CTAS = 6,     /* CTAs of the kernels that walk the active-block and candidate lists (default
                                   1216 = 8 per SM of a GB300) */
+    MPM_OPT_P2G_GROUP = 7      /* P2G sums same-cell lanes within aligned groups of this many lanes before one
+                                  reduction each: 1, 2, 4, 8, 16 or 32 (default) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 
@@ -180,7 +182,7 @@ int mpm_batch_size(void *batch, int32_t *n);
 /* One frame of every scene, in the order they were added: frame_dt[i] for scene i (its advance(frame_dt),
  * mpm_core/solver.py:67-68), stats[i] as mpm_advance returns them. */
 int mpm_batch_advance(void *batch, const double *frame_dt, MpmAdvanceStats *stats);
-/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS for the batch's launches */
+/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP for the batch's launches */
 int mpm_batch_set_option(void *batch, int32_t option, int64_t value);
 int mpm_batch_get_stream(void *batch, void **stream);
 /* Kernels launched by the batch and its scenes so far. */

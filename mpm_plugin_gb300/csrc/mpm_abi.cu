@@ -334,6 +334,7 @@ SubstepArgs substep_args(Handle* h) {
     a.fixed = h->deterministic ? h->d_fixed : nullptr;
     a.poison = h->deterministic ? h->d_poison : nullptr;
     a.fixed_exp = h->fixed_exp;
+    a.p2g_group = h->shape.p2g_group;
     return a;
 }
 
@@ -437,7 +438,8 @@ Status run_substep(Handle* h) {
     h->launches += kernels;
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
-                                     (int64_t)h->shape.list_ctas, (int64_t)h->shape.g2p_variant};
+                                     (int64_t)h->shape.list_ctas,
+                                     (int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -998,6 +1000,7 @@ Status batch_upload(Batch* b) {
     for (int s = 0; s < n; ++s) {
         Handle* h = b->live[s];
         table[s] = substep_args(h);
+        table[s].p2g_group = b->shape.p2g_group;
         layout.push_back(h->P.cap);
         ctas += (h->P.cap + 255) / 256;
         cols = cols || h->n_col > 0;
@@ -1345,6 +1348,11 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             if (value < 1 || value > (1 << 20)) return finish(h, {MPM_ERR_VALUE, "work-list CTAs out of range"});
             h->shape.list_ctas = (unsigned int)value;
             return MPM_OK;
+        case MPM_OPT_P2G_GROUP:
+            if (value < 1 || value > 32 || (value & (value - 1)))
+                return finish(h, {MPM_ERR_VALUE, "P2G group must be a power of two from 1 to 32"});
+            h->shape.p2g_group = (int)value;
+            return MPM_OK;
         case MPM_OPT_SORT_INTERVAL:
             if (value < 0 || value > (1 << 30)) return finish(h, {MPM_ERR_VALUE, "sort interval out of range"});
             h->sort_interval = (int)value;
@@ -1516,6 +1524,12 @@ int mpm_batch_set_option(void* batch, int32_t option, int64_t value) {
         if (value != 0 && value != 1) return finish_batch(b, {MPM_ERR_VALUE, "G2P variant must be 0 or 1"});
         b->shape.g2p_variant = (int)value;
         batch_invalidate(b);
+        return MPM_OK;
+    }
+    if (option == MPM_OPT_P2G_GROUP) {
+        if (value < 1 || value > 32 || (value & (value - 1)))
+            return finish_batch(b, {MPM_ERR_VALUE, "P2G group must be a power of two from 1 to 32"});
+        b->shape.p2g_group = (int)value;
         return MPM_OK;
     }
     if (option == MPM_OPT_LIST_CTAS) {

@@ -26,11 +26,12 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 // One substep: step counters, clear of the previous blocks, P2G, grid update, collider contact, G2P,
 // particle projection. With ev (5 events), records ev[0..4] around: clear | P2G | grid | G2P (as event
 // nodes when `capturing`).
-// Launch choices the autotuner sets: CTAs of the kernels that walk work lists, and the G2P build (0: capped
-// at 80 registers, 3 CTAs of 256 per SM; 1: uncapped).
+// Launch choices the autotuner sets: CTAs of the kernels that walk work lists, the G2P build (0: capped
+// at 80 registers, 3 CTAs of 256 per SM; 1: uncapped) and P2G's reduction group.
 struct LaunchShape {
     unsigned int list_ctas = kListCtas;
     int g2p_variant = 0;
+    int p2g_group = 32;  // lanes of the aligned groups P2G sums within (a power of two, 1 .. 32)
 };
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing);
 int substep_kernel_count(const SubstepArgs& a);

@@ -202,8 +202,9 @@ __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
 // particle order after the reorder by grid node) form a segment; each of the 27 x 4 contributions is summed
 // over the segment with shuffles (after round r a lane holds the sum of the next 2^r lanes of its segment)
 // and only the segment's first lane issues the 16-byte reduction, so a cell of ~8 particles costs one
-// reduction per node instead of eight. Lanes past the end or with a stencil outside the grid are
-// single-lane segments that add nothing. The segment's first lane also lists the grid blocks it touches.
+// reduction per node instead of eight. Runs are also cut at aligned groups of p2g_group lanes: fewer shuffle
+// rounds for more reductions (the autotuner picks the group). Lanes past the end or with a stencil outside
+// the grid are single-lane segments that add nothing. The segment's first lane lists the blocks it touches.
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
     const int s = sc.scene_of_cta(blockIdx.x);
@@ -220,8 +221,9 @@ __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
     const int64_t key = valid ? node_index(g, t.base[0], t.base[1], t.base[2]) : -1 - (int64_t)lane;
     const int64_t key_prev = __shfl_up_sync(0xffffffffu, key, 1);
     const int64_t key_next = __shfl_down_sync(0xffffffffu, key, 1);
-    const bool seg_first = lane == 0 || key_prev != key;
-    const bool seg_last = lane == 31 || key_next != key;
+    const int gmask = a.p2g_group - 1;  // runs are also cut at group boundaries
+    const bool seg_first = (lane & gmask) == 0 || key_prev != key;
+    const bool seg_last = (lane & gmask) == gmask || key_next != key;
     const unsigned int ends = __ballot_sync(0xffffffffu, seg_last);
     const int tail = __ffs(ends >> lane) - 1;  // lanes after this one in its segment
     const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned int)tail);
