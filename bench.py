@@ -285,6 +285,137 @@ def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float
                         "frames handed to an in-memory sink in place of the cache writer"}
 
 
+def large_scene(res: int, pile_top: float, seed: int = 3):
+    """The large inflow workload at resolution `res`: a Drucker-Prager pile (E 3.5e5, nu 0.3, 30 deg,
+    rho 1600) filling (0.2-0.8)^2 x (0-pile_top) at 8 per cell, a seeded perturbed torus of 20,480 triangles
+    (R 0.2, r 0.05, friction 0.4) turning at 1 rev/s about z, and a disc inflow r = 0.05 m at 2 m/s downward.
+    Returns (domain, materials, pile, torus mesh, pose(t), emit(solver, piece))."""
+    from mpm_plugin_gb300.interface import MaterialParams
+    from scenes import domain, lattice_box, rot_x, rot_z, torus, translate
+
+    d = domain(res=res)
+    mats = [MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)]
+    pile = lattice_box((0.2, 0.2, 0.0), (0.8, 0.8, pile_top), d.dx / 2, np.random.default_rng(seed))
+    tv, tt = torus(0.2, 0.05, 256, 40, seed=seed, jitter=0.05)
+
+    def pose(t):
+        return translate(0.5, 0.5, pile_top + 0.12) @ rot_z(360.0 * t) @ rot_x(90.0)
+
+    def emit(s, piece):  # one emission substep: the slab 2 m/s x 1/96 s below the disc, where no material is
+        r = np.random.default_rng(seed * 100000 + piece)
+        slab = lattice_box((0.45, 0.45, 0.9), (0.55, 0.55, 0.9 + 2.0 / 96), d.dx / 2, r)
+        slab = slab[np.hypot(slab[:, 0] - 0.5, slab[:, 1] - 0.5) <= 0.05]
+        free = ~s.is_occupied(slab)
+        p = slab[free]
+        if len(p):
+            s.add_particles(p, np.tile(np.float32([0.0, 0.0, -2.0]), (len(p), 1)), np.zeros(len(p), np.int32),
+                            np.zeros(len(p), np.int32))
+        return len(p)
+
+    return d, mats, pile, (tv, tt), pose, emit
+
+
+def run_large(device: str, frames: int) -> dict:
+    """The 256^3 inflow workload (about 7.5M particles at the start), driven as the bake runner drives it:
+    per 24 fps frame, four pieces of 1/96 s, each with the collider's start and end pose, an advance at the
+    CFL step and an emission (occupancy query + add_particles); then the frame's particles are read back.
+    One untimed frame first. FP64 conservation totals are read at the start and the end."""
+    import torch
+
+    from mpm_plugin_gb300 import tune
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+    from mpm_plugin_gb300.solver import Gb300Solver
+
+    d, mats, pile, (tv, tt), pose, emit = large_scene(256, 0.155)
+    s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+    s.add_particles(pile, np.zeros_like(pile), np.zeros(len(pile), np.int32), np.zeros(len(pile), np.int32))
+    s.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
+    s.set_collider_transforms(pose(0.0)[None], pose(0.0)[None])
+    tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=6)
+    n0 = s.particle_count
+    c0 = s.conservation()
+    t_adv = t_emit = t_read = 0.0
+    ps, substeps, emitted, frame_ms = 0.0, 0, 0, []
+    for f in range(frames + 1):
+        f0 = time.perf_counter()
+        fa = fe = 0.0
+        for piece in range(4):
+            k = 4 * f + piece
+            s.set_collider_transforms(pose(k / 96)[None], pose((k + 1) / 96)[None])
+            n = s.particle_count
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = s.advance(1 / 96)
+            t1 = time.perf_counter()
+            added = emit(s, k)
+            t2 = time.perf_counter()
+            if f > 0:
+                ps += n * st.substeps
+                substeps += st.substeps
+                emitted += added
+                fa += t1 - t0
+                fe += t2 - t1
+        t3 = time.perf_counter()
+        s.get_particles()
+        t4 = time.perf_counter()
+        if f > 0:
+            t_adv += fa
+            t_emit += fe
+            t_read += t4 - t3
+            frame_ms.append(1e3 * (t4 - f0))
+    c1 = s.conservation()
+    n1 = s.particle_count
+    s.close()
+    total = t_adv + t_emit + t_read
+    return {"value": ps / total, "advance_only": ps / t_adv, "unit": UNIT, "frames": frames,
+            "particles_start": n0, "particles_end": n1, "emitted": emitted, "substeps": substeps,
+            "seconds": {"advance": t_adv, "emission": t_emit, "read_back": t_read},
+            "frame_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
+            "tuned": tuned,
+            "conservation_fp64": {"mass": [c0["mass"], c1["mass"]], "ke": [c0["ke"], c1["ke"]],
+                                  "momentum_z": [float(c0["momentum"][2]), float(c1["momentum"][2])]},
+            "fp64_oracle_error": fp64_error_sample(device)}
+
+
+def fp64_error_sample(device: str, substeps: int = 100) -> dict:
+    """The large workload's physics at 48^3 (pile, turning torus; about 22k particles), 100 substeps at
+    dt = 2e-4 on the GPU (FP32) and on the FP64 oracle: relative error of x, v and of the invariants."""
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+    from mpm_plugin_gb300.solver import Gb300Solver
+    from oracle.oracle import OracleSolver
+
+    d, mats, pile, (tv, tt), pose, _ = large_scene(48, 0.1)
+    g = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+    o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f64", threads=os.cpu_count() or 1)
+    z = np.zeros(len(pile), np.int32)
+    g.add_particles(pile, np.zeros_like(pile), z, z)
+    o.add_particles(pile, np.zeros_like(pile), z, z)
+    g.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
+    o.set_colliders([(tv, tt, True, 0.4)])
+    xf0, xf1 = pose(0.0), pose(1 / 24)
+    g.set_collider_transforms(xf0[None], xf1[None])
+    o.set_collider_transforms(xf0[None], xf1[None])
+    o.frame_dt = 1 / 24
+    t0 = time.perf_counter()
+    for k in range(substeps):
+        sk = (k + 1) / substeps
+        g.substep(2e-4, sk, 1 / 24)
+        o.substep(2e-4, sk)
+    a, b = g.save_state(), o.save_state()
+    g.close()
+    pm = float(np.float32(1600.0) * np.float32(d.dx ** 3 / 8))
+
+    def inv(st):
+        x, v = st["x"].astype(np.float64), st["v"].astype(np.float64)
+        return (pm * v).sum(0), (x.mean(0)), 0.5 * pm * (v * v).sum()
+
+    (pa, ca, ka), (pb, cb, kb) = inv(a), inv(b)
+    rel = lambda u, w: float(np.linalg.norm(u - w) / max(np.linalg.norm(w), 1e-30))
+    return {"particles": len(pile), "substeps": substeps, "dt": 2e-4, "x": rel(a["x"], b["x"]),
+            "v": rel(a["v"], b["v"]), "momentum": rel(pa, pb), "com": rel(ca, cb), "ke": abs(ka - kb) / kb,
+            "oracle_seconds": time.perf_counter() - t0}
+
+
 def cpu_oracle_time(threads: int, budget_s: float):
     """FP32 oracle (C restatement of the reference kernels, OpenMP) on the same scene; returns rate, sample."""
     from oracle.oracle import OracleSolver
@@ -450,6 +581,7 @@ def run_gpu(args, world, rank, local):
         batched = run_batched(device, args.batched_frames)
         batched["small_scenes"] = run_batched(device, args.batched_frames, n_hi=1e5)
     serving = run_serving(device, args.serve_seconds) if args.serve_seconds > 0 else None
+    large = run_large(device, args.large_frames) if args.large_frames > 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -475,6 +607,7 @@ def run_gpu(args, world, rank, local):
                           "kernels_ms_per_launch": {k: t / max(c, 1) for k, (t, c) in det_times.items()}},
         "batched": batched,
         "serving": serving,
+        "large": large,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -489,6 +622,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--e2e-frames", type=int, default=4, help="24 fps frames timed through the solver API")
+    ap.add_argument("--large-frames", type=int, default=1,
+                    help="24 fps frames of the 256^3 inflow workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=5.0,
                     help="seconds of Poisson bake requests (4 per second) for the serving measurement (0: skip)")
     ap.add_argument("--batched-frames", type=int, default=3,

@@ -146,6 +146,11 @@ int mpm_read_collider_pose(void *handle, int32_t c, float *M12, float *Minv12, f
 /* Kernels of this library launched on the handle's stream since it was created. */
 int mpm_launch_count(void *handle, int64_t *launches);
 
+/* Conservation accumulators in FP64 over the particles (no counterpart in the reference; the reference's
+ * tests sum host copies): out[0] total mass, out[1..3] momentum, out[4..6] mass-weighted position (centre of
+ * mass = out[4..6] / out[0]), out[7] kinetic energy, out[8] particles skipped as non-finite. */
+int mpm_conservation(void *handle, double *out);
+
 /* Device memory the handle holds now, in bytes (no counterpart in the reference; serving admission). */
 int mpm_device_bytes(void *handle, int64_t *bytes);
 

@@ -24,7 +24,7 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_set_collider_transforms", "mpm_advance", "mpm_substep", "mpm_particle_count", "mpm_get_particles",
            "mpm_is_occupied", "mpm_save_state", "mpm_load_state", "mpm_set_option", "mpm_get_stream",
            "mpm_synchronize", "mpm_kernel_times", "mpm_grid_dims", "mpm_read_grid", "mpm_read_collider_pose",
-           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_device_bytes", "mpm_batch_create", "mpm_batch_destroy",
+           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_conservation", "mpm_device_bytes", "mpm_batch_create", "mpm_batch_destroy",
            "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
            "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count")
 
@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
         "mpm_launch_count": [P, C.POINTER(I64)],
         "mpm_fp64_lanes": [P, C.POINTER(I64)],
         "mpm_is_occupied_noalloc": [C.POINTER(MpmDomainDesc), I32, I64, P, I64, P, P, I32, P],
+        "mpm_conservation": [P, P],
         "mpm_device_bytes": [P, C.POINTER(I64)],
         "mpm_batch_create": [C.POINTER(P)],
         "mpm_batch_destroy": [P],

@@ -1454,6 +1454,22 @@ int mpm_fp64_lanes(void* handle, int64_t* lanes) {
 }
 
 
+int mpm_conservation(void* handle, double* out) {
+    HANDLE_OR_FAIL(handle);
+    if (!out) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
+    auto run = [&]() -> Status {
+        TRY(ensure_stage(h, sizeof(double) * 9));
+        double* d = static_cast<double*>(h->stage);
+        launch_conservation(h->stream, h->P, h->d_mats, d);
+        h->launches += 1;
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(out, d, sizeof(double) * 9, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        return {};
+    };
+    return finish(h, run());
+}
+
 int mpm_device_bytes(void* handle, int64_t* bytes) {
     HANDLE_OR_FAIL(handle);
     if (!bytes) return finish(h, {MPM_ERR_ARGUMENT, "null output"});

@@ -55,6 +55,8 @@ int batch_substep_kernel_count(const BatchLaunch& b);
 void launch_scatter_volume_fixed(cudaStream_t st, const Particles& P, const GridDesc& g, unsigned int* vol);
 void launch_query_fill_fixed(cudaStream_t st, const GridDesc& g, const unsigned int* vol, double cell_vol, int64_t m,
                              const float* pts, uint8_t* out);
+// FP64 totals: mass, momentum xyz, mass-weighted position xyz, kinetic energy, non-finite particles.
+void launch_conservation(cudaStream_t st, const Particles& P, const Material* mats, double* out);
 // Counting sort of the particles by the grid node of their stencil base: fills ss.order (scan_tmp: scan
 // scratch of scan_cap + 2 entries, at least scan_tile_count(n_nodes + 1) + 1).
 void launch_sort(cudaStream_t st, const Particles& P, const GridDesc& g, const SortScratch& ss, int64_t n_nodes,

@@ -119,6 +119,44 @@ __global__ void k_max_speed(Particles P, unsigned int* out) {
 }
 
 // ------------------------------------------------------------------------------------------------------
+// Conservation accumulators in FP64: total mass, momentum, mass-weighted position and kinetic energy
+// (out[0], out[1..3], out[4..6], out[7]); per-CTA sums in shared memory, then one FP64 atomic per CTA and
+// value. Non-finite particles are skipped and counted in out[8].
+// ------------------------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_conservation(Particles P, const Material* __restrict__ mats,
+                                                      double* __restrict__ out) {
+    __shared__ double sh[9][8];
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P.n; p += (int64_t)gridDim.x * blockDim.x) {
+        const double m = mats[P.mat[p]].p_mass;
+        const double x[3] = {P.x[0][p], P.x[1][p], P.x[2][p]}, v[3] = {P.v[0][p], P.v[1][p], P.v[2][p]};
+        if (!(isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(v[0]) && isfinite(v[1]) && isfinite(v[2]))) {
+            acc[8] += 1.0;
+            continue;
+        }
+        acc[0] += m;
+        for (int a = 0; a < 3; ++a) {
+            acc[1 + a] += m * v[a];
+            acc[4 + a] += m * x[a];
+        }
+        acc[7] += 0.5 * m * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = 0; k < 9; ++k) {
+        double v = acc[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[k][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 9) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[threadIdx.x][w];
+        atomicAdd(&out[threadIdx.x], v);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------
 // Particle-state I/O: host-order arrays (N,3) / (N,3,3) / (N,) <-> SoA, ordered by the insertion id.
 // ------------------------------------------------------------------------------------------------------
 __global__ void k_state_in(Particles P, int64_t off, int64_t n, const float* __restrict__ x, const float* __restrict__ v,
@@ -530,6 +568,12 @@ void launch_query_fill_fixed(cudaStream_t st, const GridDesc& g, const unsigned 
     if (m == 0) return;
     const double threshold = 0.5 * cell_vol / (double)g.p_vol * (double)kVolUnits;
     k_query_fill_fixed<<<blocks_for(m, 256), 256, 0, st>>>(g, vol, threshold, m, pts, out);
+}
+
+void launch_conservation(cudaStream_t st, const Particles& P, const Material* mats, double* out) {
+    cudaMemsetAsync(out, 0, sizeof(double) * 9, st);
+    if (P.n == 0) return;
+    k_conservation<<<std::min<unsigned int>(blocks_for(P.n, 256), 152 * 8), 256, 0, st>>>(P, mats, out);
 }
 
 void launch_grid_unblock(cudaStream_t st, const GridDesc& g, const float4* grid, float4* out) {

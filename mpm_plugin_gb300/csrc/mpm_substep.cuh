@@ -296,13 +296,26 @@ MPM_HD void node_position(const GridDesc& g, const int idx[3], float pos[3]) {
     for (int a = 0; a < 3; ++a) pos[a] = fadd(g.origin[a], fmul((float)idx[a], g.dx));
 }
 
+// True when some collider's query at pos can report contact (collider_may_touch).
 MPM_HD bool near_any_collider(const float pos[3], const ColliderData& cd) {
     for (int c = 0; c < cd.n_col; ++c)
-        if (in_margin_box(cd.cols[c], cd.poses[c], pos)) return true;
+        if (collider_may_touch(cd.cols[c], cd.poses[c], cd.cells, pos)) return true;
     return false;
 }
 
-// Mesh-collider contact of one node after the wall pass (colliders.py:77-117).
+// True for the lane that stores a result: every thread, or lane 0 of a warp that works on one item together.
+template <bool kWarp>
+MPM_HD bool stores_result() {
+#ifdef __CUDA_ARCH__
+    return !kWarp || (threadIdx.x & 31) == 0;
+#else
+    return true;
+#endif
+}
+
+// Mesh-collider contact of one node after the wall pass (colliders.py:77-117). kWarp: the whole warp works
+// on this node (every lane passes the same node; the mesh queries are shared), lane 0 stores it.
+template <bool kWarp = false>
 MPM_HD void grid_node_colliders(const GridDesc& g, float4* node, const int idx[3], const ColliderData& cd) {
     float4 nv = *node;
     float vel[3] = {nv.x, nv.y, nv.z};
@@ -311,7 +324,7 @@ MPM_HD void grid_node_colliders(const GridDesc& g, float4* node, const int idx[3
     for (int c = 0; c < cd.n_col; ++c) {
         const ColliderDev& col = cd.cols[c];
         float n[3], phi;
-        collider_sdf(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, pos, g.thickness, n, &phi);
+        collider_sdf<kWarp>(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, pos, g.thickness, n, &phi);
         if (phi < g.band) {
             float vcol[3];
             collider_velocity(cd.poses[c], pos, vcol);
@@ -334,7 +347,7 @@ MPM_HD void grid_node_colliders(const GridDesc& g, float4* node, const int idx[3
             }
         }
     }
-    *node = make_float4(vel[0], vel[1], vel[2], nv.w);
+    if (stores_result<kWarp>()) *node = make_float4(vel[0], vel[1], vel[2], nv.w);
 }
 
 // ------------------------------------------------------------------------------------------------------
@@ -467,13 +480,14 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity
-// relative to the collider (colliders.py:120-148).
+// relative to the collider (colliders.py:120-148). kWarp as for grid_node_colliders.
+template <bool kWarp = false>
 MPM_HD void project_particle(const Particles& P, int64_t p, const GridDesc& g, const ColliderData& cd) {
     float nx[3] = {P.x[0][p], P.x[1][p], P.x[2][p]}, nv[3] = {P.v[0][p], P.v[1][p], P.v[2][p]};
     for (int c = 0; c < cd.n_col; ++c) {
         const ColliderDev& col = cd.cols[c];
         float n[3], phi;
-        collider_sdf(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, nx, g.thickness, n, &phi);
+        collider_sdf<kWarp>(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, nx, g.thickness, n, &phi);
         if (phi < 0.0f) {
 #pragma unroll
             for (int a = 0; a < 3; ++a) nx[a] = nx[a] - phi * n[a];
@@ -486,6 +500,7 @@ MPM_HD void project_particle(const Particles& P, int64_t p, const GridDesc& g, c
             }
         }
     }
+    if (!stores_result<kWarp>()) return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         P.x[a][p] = nx[a];

@@ -310,7 +310,8 @@ __global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
     }
 }
 
-// Mesh-collider contact of the listed nodes (full warps of candidates; voxel grid, then BVH queries).
+// Mesh-collider contact of the listed nodes, one warp per node: the lanes share each mesh query (32
+// candidate triangles at a time), so a node whose voxel lists many triangles no longer holds up the kernel.
 __device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigned int i) {
     const GridDesc& g = a.g;
     ColliderData cd = a.cd;
@@ -322,22 +323,22 @@ __device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigne
     const int bj = (int)((b / g.nb[2]) % g.nb[1]);
     const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
     const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-    grid_node_colliders(g, &a.grid[q], idx, cd);
+    grid_node_colliders<true>(g, &a.grid[q], idx, cd);
 }
 
 template <class Scenes>
 __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
+    const unsigned int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[2];
-        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            grid_collider_node(a, i);
+        for (unsigned int i = warp; i < n; i += warps) grid_collider_node(a, i);
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
             return a.cd.n_col > 0 ? a.wl.counts[2] : 0u;
         }, off);
-        for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        for (unsigned int q = warp; q < total; q += warps) {
             const int s = scene_of_item(off, sc.count(), q);
             grid_collider_node(sc.get(s), q - off[s]);
         }
@@ -364,25 +365,26 @@ __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     }
 }
 
+// One warp per listed particle, as for the nodes.
 __device__ __forceinline__ void project_candidate(const SubstepArgs& a, unsigned int i) {
     ColliderData cd = a.cd;
     cd.poses += a.sp->pose_base;
-    project_particle(particles_of(a), a.wl.part_cand[i], a.g, cd);
+    project_particle<true>(particles_of(a), a.wl.part_cand[i], a.g, cd);
 }
 
 template <class Scenes>
 __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
+    const unsigned int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[3];
-        for (unsigned int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-            project_candidate(a, i);
+        for (unsigned int i = warp; i < n; i += warps) project_candidate(a, i);
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
             return a.cd.n_col > 0 ? a.wl.counts[3] : 0u;
         }, off);
-        for (unsigned int q = blockIdx.x * blockDim.x + threadIdx.x; q < total; q += gridDim.x * blockDim.x) {
+        for (unsigned int q = warp; q < total; q += warps) {
             const int s = scene_of_item(off, sc.count(), q);
             project_candidate(sc.get(s), q - off[s]);
         }

@@ -193,6 +193,14 @@ class Gb300Solver(Solver):
         self._check(self._lib.mpm_launch_count(self._h, C.byref(v)))
         return v.value
 
+    def conservation(self) -> dict:
+        """FP64 totals over the particles on the device: mass, momentum, centre of mass, kinetic energy."""
+        out = np.zeros(9, np.float64)
+        self._check(self._lib.mpm_conservation(self._h, out.ctypes.data_as(C.c_void_p)))
+        m = out[0]
+        return {"mass": m, "momentum": out[1:4].copy(), "com": out[4:7] / m if m > 0 else np.zeros(3),
+                "ke": out[7], "non_finite": int(out[8])}
+
     def device_bytes(self) -> int:
         """Device memory this solver holds now."""
         n = C.c_int64()

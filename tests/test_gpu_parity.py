@@ -235,3 +235,26 @@ def test_errors_match_reference():
     st = g.advance(1 / 24)
     assert (st.substeps, st.dt, st.removed) == (0, 1 / 24, 0)
     assert g.is_occupied(np.zeros((0, 3))).shape == (0,)
+
+
+def test_conservation_accumulators_match_host_sums():
+    """mpm_conservation (FP64 on the device) against float64 sums of the downloaded state, NaN skipped."""
+    d = domain(res=32)
+    mats = [preset("jelly"), preset("sand_dry")]
+    g = gpu_solver(d, mats)
+    add(g, box_particles((0.2, 0.3, 0.1), (0.4, 0.6, 0.4), d.dx, seed=1), 0, 0, (1.0, 0.0, 0.0))
+    add(g, box_particles((0.5, 0.3, 0.0), (0.7, 0.6, 0.3), d.dx, seed=2), 1, 1, (0.0, -0.5, 0.2))
+    for _ in range(10):
+        g.substep(2e-4, 1.0, 1 / 24)
+    st = g.save_state()
+    st["x"][3] = np.nan
+    g.load_state(st)
+    c = g.conservation()
+    pm = np.array([np.float32(m.density) * np.float32(d.dx ** 3 / 8) for m in mats], np.float64)[st["mat"]]
+    ok = np.isfinite(st["x"]).all(1) & np.isfinite(st["v"]).all(1)
+    m, x, v = pm[ok], st["x"][ok].astype(np.float64), st["v"][ok].astype(np.float64)
+    assert c["non_finite"] == 1
+    assert c["mass"] == pytest.approx(m.sum(), rel=1e-12)
+    np.testing.assert_allclose(c["momentum"], (m[:, None] * v).sum(0), rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(c["com"], (m[:, None] * x).sum(0) / m.sum(), rtol=1e-10)
+    assert c["ke"] == pytest.approx(0.5 * (m * (v * v).sum(1)).sum(), rel=1e-10)
