@@ -60,10 +60,9 @@ def peaks() -> tuple[float, str]:
 
 
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from mpm_plugin_gb300.replicas import dist_env as env
+
+    return env()
 
 
 class Clocks:
@@ -549,16 +548,15 @@ def run_gpu(args, world, rank, local):
         substeps += st.substeps
     e2e = n * substeps / (sum(frame_ms) / 1e3)
 
-    times = torch.tensor([total_ms, sum(frame_ms)], dtype=torch.float64, device=device)
-    rates = torch.tensor([float(n), e2e], dtype=torch.float64, device=device)
-    if world > 1:
-        torch.distributed.all_reduce(times, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(rates, op=torch.distributed.ReduceOp.SUM)
+    from mpm_plugin_gb300.replicas import reduce_timing
+
+    total_s, units = reduce_timing(total_ms / 1e3, float(n) * args.steps, device)  # slowest rank, all ranks' units
+    e2e_s, e2e_units = reduce_timing(sum(frame_ms) / 1e3, float(n) * substeps, device)
     if rank != 0:
         return
-    total_ms, _ = times.tolist()
-    n_all, e2e_all = rates.tolist()
-    value = n_all * args.steps / (total_ms / 1e3)
+    total_ms = 1e3 * total_s
+    value = units / total_s
+    e2e_all = e2e_units / e2e_s
 
     names = {"p2g": P2G_BYTES, "g2p": G2P_BYTES}
     dom = max(("p2g", "grid_update", "g2p"), key=lambda k: ktimes[k][0])
