@@ -415,6 +415,50 @@ def fp64_error_sample(device: str, substeps: int = 100) -> dict:
             "oracle_seconds": time.perf_counter() - t0}
 
 
+def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict:
+    """The small plain workload: a fixed-corotated jelly cube of side 0.25 centred at (0.5, 0.6, 0.5) in a
+    1 m box at 64^3, 8 particles per cell from a seeded stratified jitter (32,768 particles), E 1e5, nu 0.3,
+    rho 1000, at rest, dt 1e-4, `substeps` substeps through the fixed-dt entry (advance(1e-4) takes exactly
+    one substep at this dt, under the CFL limit). The reference's single wall friction applies to all walls
+    (its sticky-floor / slip-wall split is not expressible there). The FP32 oracle is timed on the first
+    `cpu_substeps` substeps of the same scene on all host cores."""
+    import torch
+
+    from mpm_plugin_gb300.interface import MaterialParams
+    from mpm_plugin_gb300.solver import Gb300Solver
+    from oracle.oracle import OracleSolver
+    from scenes import domain, lattice_box
+
+    d = domain(res=64)
+    mats = [MaterialParams("jelly_cube", "elastic", 1e5, 0.3, 1000.0)]
+    pos = lattice_box((0.375, 0.475, 0.375), (0.625, 0.725, 0.625), d.dx / 2, np.random.default_rng(0))
+    z = np.zeros(len(pos), np.int32)
+    g = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+    g.add_particles(pos, np.zeros_like(pos), z, z)
+    g.run_substeps(1e-4, 10)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g.run_substeps(1e-4, substeps)  # one call, the captured substep graph replayed `substeps` times
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    g.close()
+    threads = os.cpu_count() or 1
+    o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f32", threads=threads)
+    o.add_particles(pos, np.zeros_like(pos), z, z)
+    o.frame_dt = 1e-4
+    t0 = time.perf_counter()
+    for _ in range(cpu_substeps):
+        o.substep(1e-4, 1.0)
+    cpu_s = time.perf_counter() - t0
+    n = len(pos)
+    return {"value": n * substeps / gpu_s, "unit": UNIT, "particles": n, "substeps": substeps,
+            "ms_per_substep": 1e3 * gpu_s / substeps,
+            "timing": "host clock around one run_substeps call with device synchronisation (launch-bound at this "
+                      "size: about 7 kernels per substep)",
+            "cpu_baseline": {"value": n * cpu_substeps / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{cpu_substeps} substeps of the same scene"}}
+
+
 def cpu_oracle_time(threads: int, budget_s: float):
     """FP32 oracle (C restatement of the reference kernels, OpenMP) on the same scene; returns rate, sample."""
     from oracle.oracle import OracleSolver
@@ -535,17 +579,26 @@ def run_gpu(args, world, rank, local):
     # end to end through the solver API: one bake frame per step, host buffers
     e2e_frames, frame_ms, substeps = max(2, args.e2e_frames), [], 0
     h2d = 2 * 64  # the collider's start and end world matrices
-    d2h = n * (12 + 12 + 4 + 4) + n * (12 + 12 + 36 + 36 + 4 + 4 + 4)  # get_particles + save_state
+    d2h = n * (12 + 12 + 36 + 36 + 4 + 4 + 4)  # the full state (x v C F Jp mat emitter) covers get_particles too
     solver.advance(FRAME_DT)  # warm the CFL path and the graph
+    solver.read_begin(("x", "v", "C", "F", "Jp", "mat", "emitter")).wait()
+    # As the bake runner does per frame (transforms, advance, particles for the cache, state for the checkpoint)
+    # but with the frame's read-back overlapping the next frame's substeps: read_begin right after an advance,
+    # wait for it once the next advance has run (the state read covers get_particles' arrays too).
+    pending = None
     for _ in range(e2e_frames):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         solver.set_collider_transforms(xf[None], xf[None])
         st = solver.advance(FRAME_DT)
-        solver.get_particles()
-        solver.save_state()
+        if pending is not None:
+            pending.wait()
+        pending = solver.read_begin(("x", "v", "C", "F", "Jp", "mat", "emitter"))
         frame_ms.append(1e3 * (time.perf_counter() - t0))
         substeps += st.substeps
+    t0 = time.perf_counter()
+    pending.wait()
+    frame_ms[-1] += 1e3 * (time.perf_counter() - t0)
     e2e = n * substeps / (sum(frame_ms) / 1e3)
 
     from mpm_plugin_gb300.replicas import reduce_timing
@@ -580,6 +633,7 @@ def run_gpu(args, world, rank, local):
         batched["small_scenes"] = run_batched(device, args.batched_frames, n_hi=1e5)
     serving = run_serving(device, args.serve_seconds) if args.serve_seconds > 0 else None
     large = run_large(device, args.large_frames) if args.large_frames > 0 else None
+    small = run_small(device) if args.small else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -595,7 +649,9 @@ def run_gpu(args, world, rank, local):
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
                          "sample": f"{cpu_k} substeps of the full {cpu_n}-particle scene, {cpu_el:.1f} s"},
         "e2e": {"value": e2e_all, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "step": "one 24 fps frame via the solver API", "substeps_per_frame": substeps / e2e_frames},
+                "step": "one 24 fps frame via the solver API (transforms, advance, full state read back; each "
+                        "frame's read-back overlaps the next frame's substeps)",
+                "substeps_per_frame": substeps / e2e_frames},
         "frame_latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
         "gpu_launches": launches,
         "clocks": clk.summary(),
@@ -606,6 +662,7 @@ def run_gpu(args, world, rank, local):
         "batched": batched,
         "serving": serving,
         "large": large,
+        "small": small,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -620,6 +677,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--e2e-frames", type=int, default=4, help="24 fps frames timed through the solver API")
+    ap.add_argument("--small", type=int, default=1, help="measure the 32k-particle jelly workload (0: skip)")
     ap.add_argument("--large-frames", type=int, default=1,
                     help="24 fps frames of the 256^3 inflow workload (0: skip)")
     ap.add_argument("--serve-seconds", type=float, default=5.0,

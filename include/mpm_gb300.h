@@ -93,6 +93,11 @@ int mpm_advance(void *handle, double frame_dt, MpmAdvanceStats *stats);
 int mpm_substep(void *handle, double dt, double s, double frame_dt);
 
 /* Solver.particle_count (mpm_core/solver.py:67-69). */
+/* `count` substeps of a fixed dt in one call (no CFL choice, no removal): the substeps of one advance of
+ * frame_dt, collider poses interpolated at s = (k + 1) / count (warp/solver.py:216-219). No counterpart in the
+ * reference; the fixed-dt workloads (and tests) use it to run many substeps without a call per substep. */
+int mpm_run_substeps(void *handle, double dt, int32_t count, double frame_dt);
+
 int mpm_particle_count(void *handle, int64_t *n);
 
 /* Solver.get_particles (mpm_core/solver.py:71-72; warp/solver.py:131-132). Any output may be NULL. */
@@ -120,8 +125,10 @@ enum {
     MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 80 registers, 3 CTAs of 256 per SM; 1 uncapped */
     MPM_OPT_LIST_CTAS = 6,     /* CTAs of the kernels that walk the active-block and candidate lists (default
                                   1216 = 8 per SM of a GB300) */
-    MPM_OPT_P2G_GROUP = 7      /* P2G sums same-cell lanes within aligned groups of this many lanes before one
+    MPM_OPT_P2G_GROUP = 7,     /* P2G sums same-cell lanes within aligned groups of this many lanes before one
                                   reduction each: 1, 2, 4, 8, 16 or 32 (default) */
+    MPM_OPT_PDL = 8            /* 1 (default): the substep kernels use programmatic dependent launch, so each
+                                  kernel's launch overlaps the tail of the one before; 0: plain stream order */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 
@@ -145,6 +152,18 @@ int mpm_read_collider_pose(void *handle, int32_t c, float *M12, float *Minv12, f
 
 /* Kernels of this library launched on the handle's stream since it was created. */
 int mpm_launch_count(void *handle, int64_t *launches);
+
+/* Read-back that does not hold up the next advance (no counterpart in the reference, whose get_particles
+ * and save_state return once the copy is done, bake.py:205-206). The requested arrays (any may be NULL; the
+ * layouts and particle order of mpm_save_state) are gathered into device storage on the handle's stream and
+ * copied into the host buffers on a separate copy stream; the call returns at once and the caller may advance
+ * again. The host buffers must stay valid and unread until mpm_read_wait returns. Page-locked buffers
+ * (mpm_host_alloc) make the copy asynchronous. One read is in flight per handle: a second mpm_read_begin
+ * first waits for the one before. */
+int mpm_read_begin(void *handle, float *x, float *v, float *C, float *F, float *Jp, int32_t *mat, int32_t *emitter);
+int mpm_read_wait(void *handle);
+int mpm_host_alloc(int64_t bytes, void **ptr);
+int mpm_host_free(void *ptr);
 
 /* Conservation accumulators in FP64 over the particles (no counterpart in the reference; the reference's
  * tests sum host copies): out[0] total mass, out[1..3] momentum, out[4..6] mass-weighted position (centre of
@@ -187,7 +206,7 @@ int mpm_batch_size(void *batch, int32_t *n);
 /* One frame of every scene, in the order they were added: frame_dt[i] for scene i (its advance(frame_dt),
  * mpm_core/solver.py:67-68), stats[i] as mpm_advance returns them. */
 int mpm_batch_advance(void *batch, const double *frame_dt, MpmAdvanceStats *stats);
-/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP for the batch's launches */
+/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP, MPM_OPT_PDL for the batch */
 int mpm_batch_set_option(void *batch, int32_t option, int64_t value);
 int mpm_batch_get_stream(void *batch, void **stream);
 /* Kernels launched by the batch and its scenes so far. */

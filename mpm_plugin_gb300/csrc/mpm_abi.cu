@@ -33,27 +33,36 @@ struct Status {
     std::string msg;
 };
 
-// Instantiated substep graphs keyed by what the kernels' arguments depend on; two entries, so the two
-// particle arenas that the reorder alternates between both keep their graph.
+// Instantiated substep graphs keyed by what the kernels' arguments depend on (and how many substeps one
+// graph holds); four entries, so the two particle arenas the reorder alternates between, each with its
+// many-substep and one-substep graph, all keep theirs.
 struct GraphCache {
-    static constexpr int kKey = 8;
-    cudaGraphExec_t exec[2] = {nullptr, nullptr};
-    int64_t key[2][kKey] = {};
-    int last = 0;
+    static constexpr int kKey = 8, kSlots = 4;
+    cudaGraphExec_t exec[kSlots] = {};
+    int64_t key[kSlots][kKey] = {};
+    int64_t used[kSlots] = {};
+    int64_t tick = 0;
     cudaGraphExec_t find(const int64_t* k) {
-        for (int i = 0; i < 2; ++i)
+        for (int i = 0; i < kSlots; ++i)
             if (exec[i] && std::memcmp(key[i], k, sizeof(int64_t) * kKey) == 0) {
-                last = i;
+                used[i] = ++tick;
                 return exec[i];
             }
         return nullptr;
     }
-    int victim() const { return exec[0] == nullptr ? 0 : exec[1] == nullptr ? 1 : 1 - last; }
+    int victim() const {
+        int v = 0;
+        for (int i = 0; i < kSlots; ++i) {
+            if (!exec[i]) return i;
+            if (used[i] < used[v]) v = i;
+        }
+        return v;
+    }
     void put(int i, const int64_t* k, cudaGraphExec_t g) {
         if (exec[i]) cudaGraphExecDestroy(exec[i]);
         exec[i] = g;
         std::memcpy(key[i], k, sizeof(int64_t) * kKey);
-        last = i;
+        used[i] = ++tick;
     }
     void clear() {
         for (auto& e : exec) {
@@ -116,6 +125,13 @@ struct Handle {
 
     void* stage = nullptr;  // device staging for host-order arrays
     size_t stage_bytes = 0;
+
+    // asynchronous read-back (mpm_read_begin / mpm_read_wait)
+    void* rb_dev = nullptr;
+    size_t rb_bytes = 0;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t rb_ready = nullptr, rb_done = nullptr;
+    bool rb_pending = false;
 
     int64_t launches = 0;       // kernels of this library launched so far (graph replays count their kernels)
     int64_t graph_kernels = 0;  // kernels in the captured substep graph
@@ -417,10 +433,11 @@ void accumulate_times(Handle* h, const cudaEvent_t* ev) {  // ev: | clear | P2G 
     }
 }
 
-Status capture_graph(Handle* h, const SubstepArgs& a, cudaEvent_t* ev, cudaGraphExec_t* out) {
+// reps substeps in one graph (the launch cost of one graph per reps substeps); events only with reps == 1.
+Status capture_graph(Handle* h, const SubstepArgs& a, cudaEvent_t* ev, cudaGraphExec_t* out, int reps = 1) {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    launch_substep(h->stream, a, h->shape, ev, true);
+    for (int r = 0; r < reps; ++r) launch_substep(h->stream, a, h->shape, reps == 1 ? ev : nullptr, true);
     cudaError_t e0 = cudaGetLastError();
     cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
     CK(e0);
@@ -431,15 +448,17 @@ Status capture_graph(Handle* h, const SubstepArgs& a, cudaEvent_t* ev, cudaGraph
     return {};
 }
 
-Status run_substep(Handle* h) {
+// reps substeps (reps > 1 only with graphs and without kernel timing).
+Status run_substep(Handle* h, int reps = 1) {
     TRY(ensure_part_cand(h));
     SubstepArgs a = substep_args(h);
     const int kernels = substep_kernel_count(a);
-    h->launches += kernels;
+    h->launches += (int64_t)kernels * reps;
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
                                      (int64_t)h->shape.list_ctas,
-                                     (int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group};
+                                     (((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
+                                             64 + reps};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -467,7 +486,7 @@ Status run_substep(Handle* h) {
     }
     cudaGraphExec_t g = h->graphs.find(key);
     if (!g) {
-        TRY(capture_graph(h, a, nullptr, &g));
+        TRY(capture_graph(h, a, nullptr, &g, reps));
         h->graphs.put(h->graphs.victim(), key, g);
     }
     CK(cudaGraphLaunch(g, h->stream));
@@ -480,6 +499,29 @@ Status substep_and_sort(Handle* h) {
     if (h->sort_interval > 0 && ++h->since_sort >= h->sort_interval) {
         TRY(reorder_particles(h));
         h->since_sort = 0;
+    }
+    return {};
+}
+
+// count substeps, kGraphReps per graph launch where they fit between reorders (one launch per substep
+// costs more host time than a small scene's substep takes on the GPU).
+constexpr int kGraphReps = 8;
+
+Status substeps_and_sort(Handle* h, int count) {
+    while (count > 0) {
+        int reps = 1;
+        if (h->use_graph && !h->timing && count >= kGraphReps) {
+            reps = kGraphReps;
+            if (h->sort_interval > 0) reps = (int)std::min<int64_t>(reps, h->sort_interval - h->since_sort);
+            reps = std::max(reps, 1);
+        }
+        TRY(run_substep(h, reps));
+        count -= reps;
+        h->since_sort += reps;
+        if (h->sort_interval > 0 && h->since_sort >= h->sort_interval) {
+            TRY(reorder_particles(h));
+            h->since_sort = 0;
+        }
     }
     return {};
 }
@@ -693,7 +735,7 @@ Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
     TRY(set_step(h, dt, 0.0, frame_dt, steps));
     TRY(ensure_sdf(h));
     TRY(prepare_poses(h, steps, 0.0, frame_dt));
-    for (int k = 0; k < steps; ++k) TRY(substep_and_sort(h));
+    TRY(substeps_and_sort(h, steps));
     int32_t removed = 0;
     TRY(remove_escaped(h, &removed));
     CK(cudaStreamSynchronize(h->stream));
@@ -771,6 +813,71 @@ Status download_particles(Handle* h, float* x, float* v, float* C, float* F, flo
     return {};
 }
 
+Status read_wait(Handle* h) {
+    if (!h->rb_pending) return {};
+    h->rb_pending = false;
+    CK(cudaEventSynchronize(h->rb_done));
+    return {};
+}
+
+// Gathers the requested arrays into the handle's read-back storage on its stream (host order), then copies
+// them to the host buffers on a copy stream, so the caller's next launches overlap the transfer.
+Status read_begin(Handle* h, float* x, float* v, float* C, float* F, float* Jp, int32_t* mat, int32_t* emitter) {
+    TRY(read_wait(h));
+    const int64_t n = h->P.n;
+    if (n == 0) return {};
+    const size_t per = ((x ? 3 : 0) + (v ? 3 : 0) + (C ? 9 : 0) + (F ? 9 : 0) + (Jp ? 1 : 0) + (mat ? 1 : 0) +
+                        (emitter ? 1 : 0)) * 4;
+    if (per * (size_t)n > h->rb_bytes) {
+        CK(cudaStreamSynchronize(h->stream));
+        cudaFree(h->rb_dev);
+        h->rb_dev = nullptr;
+        h->rb_bytes = 0;
+        const size_t b = std::max(per * (size_t)n, h->rb_bytes * 2);
+        if (cudaMalloc(&h->rb_dev, b) != cudaSuccess) {
+            cudaGetLastError();
+            h->rb_dev = nullptr;
+            return {MPM_ERR_MEMORY, "device allocation of the read-back storage failed"};
+        }
+        h->rb_bytes = b;
+    }
+    if (!h->copy_stream) CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    if (!h->rb_ready) CK(cudaEventCreateWithFlags(&h->rb_ready, cudaEventDisableTiming));
+    if (!h->rb_done) CK(cudaEventCreateWithFlags(&h->rb_done, cudaEventDisableTiming));
+    char* s = static_cast<char*>(h->rb_dev);
+    auto slot = [&](const void* host, size_t bytes) -> void* {
+        if (!host) return nullptr;
+        void* d = s;
+        s += bytes;
+        return d;
+    };
+    float* dx_ = (float*)slot(x, (size_t)n * 12);
+    float* dv = (float*)slot(v, (size_t)n * 12);
+    float* dC = (float*)slot(C, (size_t)n * 36);
+    float* dF = (float*)slot(F, (size_t)n * 36);
+    float* dJ = (float*)slot(Jp, (size_t)n * 4);
+    int32_t* dm = (int32_t*)slot(mat, (size_t)n * 4);
+    int32_t* de = (int32_t*)slot(emitter, (size_t)n * 4);
+    launch_state_out(h->stream, h->P, dx_, dv, dC, dF, dJ, dm, de);
+    h->launches += 1;
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(h->rb_ready, h->stream));
+    CK(cudaStreamWaitEvent(h->copy_stream, h->rb_ready, 0));
+    auto get = [&](void* host, const void* dev, size_t bytes) -> cudaError_t {
+        return host ? cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, h->copy_stream) : cudaSuccess;
+    };
+    CK(get(x, dx_, (size_t)n * 12));
+    CK(get(v, dv, (size_t)n * 12));
+    CK(get(C, dC, (size_t)n * 36));
+    CK(get(F, dF, (size_t)n * 36));
+    CK(get(Jp, dJ, (size_t)n * 4));
+    CK(get(mat, dm, (size_t)n * 4));
+    CK(get(emitter, de, (size_t)n * 4));
+    CK(cudaEventRecord(h->rb_done, h->copy_stream));
+    h->rb_pending = true;
+    return {};
+}
+
 Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_mat, const double gravity[3], int32_t ppc,
               int32_t device, Handle** out) {
     if (!dom || !gravity || !out || (n_mat > 0 && !mats)) return {MPM_ERR_ARGUMENT, "null argument"};
@@ -841,6 +948,7 @@ Status batch_remove(Batch* b, Handle* h);
 void destroy(Handle* h) {
     if (!h) return;
     DeviceGuard guard(h->device);
+    read_wait(h);
     if (h->batch) batch_remove(h->batch, h);
     if (h->stream) cudaStreamSynchronize(h->stream);
     invalidate_graph(h);
@@ -877,6 +985,10 @@ void destroy(Handle* h) {
     cudaFree(h->ss.start);
     cudaFree(h->ss_scan);
     cudaFree(h->stage);
+    cudaFree(h->rb_dev);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->rb_ready) cudaEventDestroy(h->rb_ready);
+    if (h->rb_done) cudaEventDestroy(h->rb_done);
     if (h->h_counters) cudaFreeHost(h->h_counters);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -1256,6 +1368,22 @@ int mpm_substep(void* handle, double dt, double s, double frame_dt) {
     return finish(h, run());
 }
 
+int mpm_run_substeps(void* handle, double dt, int32_t count, double frame_dt) {
+    HANDLE_OR_FAIL(handle);
+    if (!(dt > 0.0) || count < 0 || !(frame_dt > 0.0)) return finish(h, {MPM_ERR_VALUE, "bad dt, count or frame_dt"});
+    auto run = [&]() -> Status {
+        if (h->P.n == 0 || count == 0) return {};
+        h->frame_dt = frame_dt;
+        TRY(set_step(h, dt, 0.0, frame_dt, count));
+        TRY(ensure_sdf(h));
+        TRY(prepare_poses(h, count, 0.0, frame_dt));
+        TRY(substeps_and_sort(h, count));
+        CK(cudaStreamSynchronize(h->stream));
+        return {};
+    };
+    return finish(h, run());
+}
+
 int mpm_particle_count(void* handle, int64_t* n) {
     HANDLE_OR_FAIL(handle);
     if (!n) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
@@ -1347,6 +1475,9 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
         case MPM_OPT_LIST_CTAS:
             if (value < 1 || value > (1 << 20)) return finish(h, {MPM_ERR_VALUE, "work-list CTAs out of range"});
             h->shape.list_ctas = (unsigned int)value;
+            return MPM_OK;
+        case MPM_OPT_PDL:
+            h->shape.pdl = value != 0;
             return MPM_OK;
         case MPM_OPT_P2G_GROUP:
             if (value < 1 || value > 32 || (value & (value - 1)))
@@ -1454,6 +1585,33 @@ int mpm_fp64_lanes(void* handle, int64_t* lanes) {
 }
 
 
+int mpm_read_begin(void* handle, float* x, float* v, float* C, float* F, float* Jp, int32_t* mat, int32_t* emitter) {
+    HANDLE_OR_FAIL(handle);
+    return finish(h, read_begin(h, x, v, C, F, Jp, mat, emitter));
+}
+
+int mpm_read_wait(void* handle) {
+    HANDLE_OR_FAIL(handle);
+    return finish(h, read_wait(h));
+}
+
+int mpm_host_alloc(int64_t bytes, void** ptr) {
+    if (!ptr || bytes < 0) return finish(nullptr, {MPM_ERR_ARGUMENT, "bad arguments"});
+    *ptr = nullptr;
+    if (bytes == 0) return MPM_OK;
+    if (cudaMallocHost(ptr, (size_t)bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *ptr = nullptr;
+        return finish(nullptr, {MPM_ERR_MEMORY, "page-locked host allocation failed"});
+    }
+    return MPM_OK;
+}
+
+int mpm_host_free(void* ptr) {
+    if (ptr) cudaFreeHost(ptr);
+    return MPM_OK;
+}
+
 int mpm_conservation(void* handle, double* out) {
     HANDLE_OR_FAIL(handle);
     if (!out) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
@@ -1539,6 +1697,11 @@ int mpm_batch_set_option(void* batch, int32_t option, int64_t value) {
     if (option == MPM_OPT_G2P_VARIANT) {
         if (value != 0 && value != 1) return finish_batch(b, {MPM_ERR_VALUE, "G2P variant must be 0 or 1"});
         b->shape.g2p_variant = (int)value;
+        batch_invalidate(b);
+        return MPM_OK;
+    }
+    if (option == MPM_OPT_PDL) {
+        b->shape.pdl = value != 0;
         batch_invalidate(b);
         return MPM_OK;
     }

@@ -10,18 +10,19 @@ namespace mpm {
 void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
     const SceneTable sc{b.scenes, b.cta_scene, b.cta_first, b.n_scenes};
     const unsigned int list_ctas = b.shape.list_ctas;
-    k_step_begin<<<1, 128, 0, st>>>(sc);
-    k_clear_blocks<<<list_ctas, 256, 0, st>>>(sc);
-    if (b.particle_ctas > 0) k_p2g_scatter<<<b.particle_ctas, 256, 0, st>>>(sc);
-    k_grid_update<<<list_ctas, 256, 0, st>>>(sc);
-    if (b.any_colliders) k_grid_colliders<<<list_ctas, 128, 0, st>>>(sc);
+    const bool pdl = b.shape.pdl != 0;
+    launch_step_kernel(k_step_begin<SceneTable>, 1, 128, st, pdl, sc);
+    launch_step_kernel(k_clear_blocks<SceneTable>, list_ctas, 256, st, pdl, sc);
+    if (b.particle_ctas > 0) launch_step_kernel(k_p2g_scatter<SceneTable>, b.particle_ctas, 256, st, pdl, sc);
+    launch_step_kernel(k_grid_update<SceneTable>, list_ctas, 256, st, pdl, sc);
+    if (b.any_colliders) launch_step_kernel(k_grid_colliders<SceneTable>, list_ctas, 128, st, pdl, sc);
     if (b.particle_ctas > 0) {
         if (b.shape.g2p_variant == 1)
-            k_g2p<SceneTable, 1><<<b.particle_ctas, 256, 0, st>>>(sc);
+            launch_step_kernel(k_g2p<SceneTable, 1>, b.particle_ctas, 256, st, pdl, sc);
         else
-            k_g2p<SceneTable, 3><<<b.particle_ctas, 256, 0, st>>>(sc);
+            launch_step_kernel(k_g2p<SceneTable, 3>, b.particle_ctas, 256, st, pdl, sc);
     }
-    if (b.any_colliders) k_project_particles<<<list_ctas, 128, 0, st>>>(sc);
+    if (b.any_colliders) launch_step_kernel(k_project_particles<SceneTable>, list_ctas, 128, st, pdl, sc);
 }
 
 int batch_substep_kernel_count(const BatchLaunch& b) {

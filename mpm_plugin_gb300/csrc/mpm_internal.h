@@ -32,7 +32,26 @@ struct LaunchShape {
     unsigned int list_ctas = kListCtas;
     int g2p_variant = 0;
     int p2g_group = 32;  // lanes of the aligned groups P2G sums within (a power of two, 1 .. 32)
+    int pdl = 1;         // 1: the substep kernels launch with programmatic dependent launch
 };
+
+// Launch of a substep kernel: with shape.pdl the launch carries the programmatic-stream-serialization
+// attribute (the kernel's launch may overlap the previous kernel's tail; the kernel waits for it itself).
+template <typename... KArgs, typename... Args>
+inline void launch_step_kernel(void (*kernel)(KArgs...), unsigned int grid, unsigned int block, cudaStream_t st,
+                               bool pdl, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
+}
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing);
 int substep_kernel_count(const SubstepArgs& a);
 

@@ -450,26 +450,28 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing) {
     const unsigned int list_ctas = shape.list_ctas;
     const OneScene sc{a};
-    // while a graph is being captured the records become event nodes that fire on every replay
+    // while a graph is being captured the records become event nodes that fire on every replay; with them
+    // in place the kernels around them launch in plain stream order
     auto mark = [&](int i) {
         if (ev) cudaEventRecordWithFlags(ev[i], st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     };
+    const bool pdl = shape.pdl != 0;
     mark(0);
-    k_step_begin<<<1, 1, 0, st>>>(sc);
-    k_clear_blocks<<<list_ctas, 256, 0, st>>>(sc);
+    launch_step_kernel(k_step_begin<OneScene>, 1, 1, st, pdl, sc);
+    launch_step_kernel(k_clear_blocks<OneScene>, list_ctas, 256, st, pdl, sc);
     mark(1);
-    if (a.n > 0) k_p2g_scatter<<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+    if (a.n > 0) launch_step_kernel(k_p2g_scatter<OneScene>, blocks_for(a.n, 256), 256, st, pdl, sc);
     mark(2);
-    k_grid_update<<<list_ctas, 256, 0, st>>>(sc);
-    if (a.cd.n_col > 0) k_grid_colliders<<<list_ctas, 128, 0, st>>>(sc);
+    launch_step_kernel(k_grid_update<OneScene>, list_ctas, 256, st, pdl, sc);
+    if (a.cd.n_col > 0) launch_step_kernel(k_grid_colliders<OneScene>, list_ctas, 128, st, pdl, sc);
     mark(3);
     if (a.n > 0) {
         if (shape.g2p_variant == 1)
-            k_g2p<OneScene, 1><<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+            launch_step_kernel(k_g2p<OneScene, 1>, blocks_for(a.n, 256), 256, st, pdl, sc);
         else
-            k_g2p<OneScene, 3><<<blocks_for(a.n, 256), 256, 0, st>>>(sc);
+            launch_step_kernel(k_g2p<OneScene, 3>, blocks_for(a.n, 256), 256, st, pdl, sc);
     }
-    if (a.cd.n_col > 0) k_project_particles<<<list_ctas, 128, 0, st>>>(sc);
+    if (a.cd.n_col > 0) launch_step_kernel(k_project_particles<OneScene>, list_ctas, 128, st, pdl, sc);
     mark(4);
 }
 

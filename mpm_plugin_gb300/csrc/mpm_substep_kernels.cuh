@@ -34,6 +34,16 @@ struct SceneTable {
     __device__ __forceinline__ bool active(const SubstepArgs& a) const { return a.sp->active != 0; }
 };
 
+// Programmatic dependent launch: every substep kernel first lets the next kernel of the sequence start
+// launching (its CTAs are placed once all CTAs of this one have begun), then waits until the kernel before
+// it has completed and its writes are visible. Launch latency overlaps the previous kernel's tail; without
+// the launch attribute both instructions do nothing. The wait ends when a grid that is already running
+// completes, so it cannot hang.
+__device__ __forceinline__ void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // Warp-aggregated append: one atomic per warp.
 __device__ __forceinline__ void warp_append(int32_t* __restrict__ list, unsigned int* __restrict__ count, int32_t v) {
     const unsigned int mask = __activemask();
@@ -115,6 +125,7 @@ __device__ __forceinline__ void step_begin(StepParams* sp, unsigned int* counts,
 
 template <class Scenes>
 __global__ void k_step_begin(Scenes sc) {
+    pdl_begin();
     for (int s = threadIdx.x; s < sc.count(); s += blockDim.x) {
         const SubstepArgs a = sc.get(s);
         step_begin(a.sp, a.wl.counts, a.cd.n_col);
@@ -182,6 +193,7 @@ __device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTe
 
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
+    pdl_begin();
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[(a.sp->seq - 1u) & 1u];
@@ -207,6 +219,7 @@ __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
 // the grid are single-lane segments that add nothing. The segment's first lane lists the blocks it touches.
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
+    pdl_begin();
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
     if (!sc.active(a)) return;
@@ -294,6 +307,7 @@ __device__ __forceinline__ void grid_update_block(const SubstepArgs& a, unsigned
 
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
+    pdl_begin();
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[a.sp->seq & 1u];
@@ -310,8 +324,14 @@ __global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
     }
 }
 
-// Mesh-collider contact of the listed nodes, one warp per node: the lanes share each mesh query (32
-// candidate triangles at a time), so a node whose voxel lists many triangles no longer holds up the kernel.
+// Contact work lists run in one of two shapes, chosen per launch from the list's length (identical
+// results): up to kWarpItemsPerWarp items per warp of the launch, one warp per item, whose lanes share the
+// item's mesh queries (32 candidate triangles at a time), so a few slow queries do not hold up the kernel;
+// beyond that, one thread per item, for throughput when contact is widespread.
+constexpr unsigned int kWarpItemsPerWarp = 4;
+
+// Mesh-collider contact of one listed node.
+template <bool kWarp>
 __device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigned int i) {
     const GridDesc& g = a.g;
     ColliderData cd = a.cd;
@@ -323,24 +343,37 @@ __device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigne
     const int bj = (int)((b / g.nb[2]) % g.nb[1]);
     const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
     const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-    grid_node_colliders<true>(g, &a.grid[q], idx, cd);
+    grid_node_colliders<kWarp>(g, &a.grid[q], idx, cd);
 }
 
 template <class Scenes>
 __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
-    const unsigned int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+    pdl_begin();
+    const unsigned int tid = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
+    const unsigned int warp = tid >> 5, warps = threads >> 5;
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[2];
-        for (unsigned int i = warp; i < n; i += warps) grid_collider_node(a, i);
+        if (n <= warps * kWarpItemsPerWarp) {
+            for (unsigned int i = warp; i < n; i += warps) grid_collider_node<true>(a, i);
+        } else {
+            for (unsigned int i = tid; i < n; i += threads) grid_collider_node<false>(a, i);
+        }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
             return a.cd.n_col > 0 ? a.wl.counts[2] : 0u;
         }, off);
-        for (unsigned int q = warp; q < total; q += warps) {
-            const int s = scene_of_item(off, sc.count(), q);
-            grid_collider_node(sc.get(s), q - off[s]);
+        if (total <= warps * kWarpItemsPerWarp) {
+            for (unsigned int q = warp; q < total; q += warps) {
+                const int s = scene_of_item(off, sc.count(), q);
+                grid_collider_node<true>(sc.get(s), q - off[s]);
+            }
+        } else {
+            for (unsigned int q = tid; q < total; q += threads) {
+                const int s = scene_of_item(off, sc.count(), q);
+                grid_collider_node<false>(sc.get(s), q - off[s]);
+            }
         }
     }
 }
@@ -351,6 +384,7 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
 // 120 registers). Both are built; the autotuner picks one per workload.
 template <class Scenes, int kMinCtas>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
+    pdl_begin();
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
     if (!sc.active(a)) return;
@@ -365,28 +399,42 @@ __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     }
 }
 
-// One warp per listed particle, as for the nodes.
+// Projection of one listed particle (the same two shapes as for the nodes).
+template <bool kWarp>
 __device__ __forceinline__ void project_candidate(const SubstepArgs& a, unsigned int i) {
     ColliderData cd = a.cd;
     cd.poses += a.sp->pose_base;
-    project_particle<true>(particles_of(a), a.wl.part_cand[i], a.g, cd);
+    project_particle<kWarp>(particles_of(a), a.wl.part_cand[i], a.g, cd);
 }
 
 template <class Scenes>
 __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
-    const unsigned int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+    pdl_begin();
+    const unsigned int tid = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
+    const unsigned int warp = tid >> 5, warps = threads >> 5;
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[3];
-        for (unsigned int i = warp; i < n; i += warps) project_candidate(a, i);
+        if (n <= warps * kWarpItemsPerWarp) {
+            for (unsigned int i = warp; i < n; i += warps) project_candidate<true>(a, i);
+        } else {
+            for (unsigned int i = tid; i < n; i += threads) project_candidate<false>(a, i);
+        }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
             return a.cd.n_col > 0 ? a.wl.counts[3] : 0u;
         }, off);
-        for (unsigned int q = warp; q < total; q += warps) {
-            const int s = scene_of_item(off, sc.count(), q);
-            project_candidate(sc.get(s), q - off[s]);
+        if (total <= warps * kWarpItemsPerWarp) {
+            for (unsigned int q = warp; q < total; q += warps) {
+                const int s = scene_of_item(off, sc.count(), q);
+                project_candidate<true>(sc.get(s), q - off[s]);
+            }
+        } else {
+            for (unsigned int q = tid; q < total; q += threads) {
+                const int s = scene_of_item(off, sc.count(), q);
+                project_candidate<false>(sc.get(s), q - off[s]);
+            }
         }
     }
 }

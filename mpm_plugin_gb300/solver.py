@@ -16,6 +16,63 @@ from mpm_plugin_gb300 import _abi
 from mpm_plugin_gb300.interface import AdvanceStats, ColliderGeometry, ParticleData, Solver
 
 STATE_KEYS = ("x", "v", "C", "F", "Jp", "mat", "emitter")
+_SHAPES = {"x": ((3,), np.float32), "v": ((3,), np.float32), "C": ((3, 3), np.float32), "F": ((3, 3), np.float32),
+           "Jp": ((), np.float32), "mat": ((), np.int32), "emitter": ((), np.int32)}
+
+
+class _PinnedPool:
+    """Page-locked host buffers for asynchronous reads. A read leases one; the numpy arrays of that read keep
+    the lease alive, and the buffer returns to the pool when the last of them is freed."""
+
+    def __init__(self, lib):
+        self.lib = lib
+        self.free: list[tuple[int, int]] = []  # (address, bytes)
+        self.closed = False
+
+    def take(self, nbytes: int):
+        for i, (addr, size) in enumerate(self.free):
+            if size >= nbytes:
+                return self.free.pop(i)
+        p = C.c_void_p()
+        _abi.check(self.lib.mpm_host_alloc(max(int(nbytes), 1 << 20) * 5 // 4, C.byref(p)))
+        return p.value, max(int(nbytes), 1 << 20) * 5 // 4
+
+    def give(self, block) -> None:
+        if self.closed:
+            self.lib.mpm_host_free(C.c_void_p(block[0]))
+        else:
+            self.free.append(block)
+
+    def close(self) -> None:
+        self.closed = True
+        for addr, _ in self.free:
+            self.lib.mpm_host_free(C.c_void_p(addr))
+        self.free = []
+
+
+class _Lease:
+    def __init__(self, pool, block):
+        self.pool, self.block = pool, block
+
+    def __del__(self):
+        try:
+            self.pool.give(self.block)
+        except Exception:
+            pass
+
+
+class PendingRead:
+    """A read in flight (Gb300Solver.read_begin). wait() returns the arrays; they stay valid after later reads
+    (each read has its own page-locked buffer, recycled when its arrays are freed)."""
+
+    def __init__(self, solver, arrays):
+        self._solver, self._arrays = solver, arrays
+
+    def wait(self) -> dict[str, np.ndarray]:
+        if self._solver is not None:
+            self._solver._check(self._solver._lib.mpm_read_wait(self._solver._h))
+            self._solver = None
+        return self._arrays
 
 
 def _f32(a, shape) -> np.ndarray:
@@ -72,6 +129,9 @@ class Gb300Solver(Solver):
         if getattr(self, "_h", None) and self._h.value:
             self._lib.mpm_destroy(self._h)
             self._h = C.c_void_p()
+        if hasattr(self, "_pool"):
+            self._pool.close()  # buffers still leased by live arrays are freed when those arrays go
+            del self._pool
 
     def __del__(self):
         try:
@@ -103,6 +163,32 @@ class Gb300Solver(Solver):
         mat, em = np.empty(n, np.int32), np.empty(n, np.int32)
         self._check(self._lib.mpm_get_particles(self._h, _ptr(x), _ptr(v), _ptr(mat), _ptr(em)))
         return ParticleData(x, v, mat, em)
+
+    def read_begin(self, keys=("x", "v", "mat", "emitter")) -> PendingRead:
+        """Start reading the given state arrays (keys of save_state) without waiting: the copy runs beside the
+        next advance; PendingRead.wait() returns them (mpm_read_begin / mpm_read_wait)."""
+        n = self.particle_count
+        if not hasattr(self, "_pool"):
+            self._pool = _PinnedPool(self._lib)
+        sizes = {k: n * int(np.prod(_SHAPES[k][0], dtype=np.int64)) * 4 for k in keys}
+        total = sum(-(-b // 256) * 256 for b in sizes.values())
+        block = self._pool.take(total)
+        raw = (C.c_char * block[1]).from_address(block[0])
+        raw._lease = _Lease(self._pool, block)
+        arrays, ptrs, off = {}, {}, 0
+        for k in keys:
+            shape, dt = _SHAPES[k]
+            arrays[k] = np.frombuffer(raw, dt, count=n * int(np.prod(shape, dtype=np.int64)), offset=off).reshape(
+                (n, *shape))
+            ptrs[k] = C.c_void_p(block[0] + off)
+            off += -(-sizes[k] // 256) * 256
+        del raw
+        self._check(self._lib.mpm_read_begin(self._h, *(ptrs.get(k) for k in STATE_KEYS)))
+        return PendingRead(self, arrays)
+
+    def get_particles_async(self) -> PendingRead:
+        """read_begin for the frame arrays; ParticleData(*wait()'s x, v, mat, emitter)."""
+        return self.read_begin(("x", "v", "mat", "emitter"))
 
     def save_state(self) -> dict[str, np.ndarray]:
         n = self.particle_count
@@ -146,6 +232,12 @@ class Gb300Solver(Solver):
     def substep(self, dt: float, s: float = 1.0, frame_dt: float = 1.0) -> None:
         """One substep with a given dt (fixed-dt runs and parity checks); asynchronous on the device."""
         self._check(self._lib.mpm_substep(self._h, float(dt), float(s), float(frame_dt)))
+
+    def run_substeps(self, dt: float, count: int, frame_dt: float | None = None) -> None:
+        """count substeps of a fixed dt in one call, as the substeps of one advance of frame_dt (default
+        count * dt): no CFL choice, no removal of escaped particles."""
+        fdt = float(frame_dt) if frame_dt is not None else float(dt) * int(count)
+        self._check(self._lib.mpm_run_substeps(self._h, float(dt), int(count), fdt))
 
     def synchronize(self) -> None:
         self._check(self._lib.mpm_synchronize(self._h))

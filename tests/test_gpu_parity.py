@@ -258,3 +258,39 @@ def test_conservation_accumulators_match_host_sums():
     np.testing.assert_allclose(c["momentum"], (m[:, None] * v).sum(0), rtol=1e-10, atol=1e-14)
     np.testing.assert_allclose(c["com"], (m[:, None] * x).sum(0) / m.sum(), rtol=1e-10)
     assert c["ke"] == pytest.approx(0.5 * (m * (v * v).sum(1)).sum(), rel=1e-10)
+
+
+def test_asynchronous_read_matches_synchronous_and_survives_the_next_advance():
+    """read_begin / wait returns the state as save_state does at that moment, while the solver advances on;
+    arrays of an earlier read stay intact after later reads."""
+    d = domain(res=32)
+    g = gpu_solver(d, [preset("jelly")])
+    add(g, box_particles((0.4, 0.4, 0.3), (0.6, 0.6, 0.5), d.dx, seed=1), 0, 0, (0.0, 0.5, 0.0))
+    g.substep(2e-4, 1.0, 1 / 24)
+    ref = g.save_state()
+    pending = g.read_begin(tuple(ref))
+    for _ in range(5):
+        g.substep(2e-4, 1.0, 1 / 24)
+    first = pending.wait()
+    for k in ref:
+        np.testing.assert_array_equal(first[k], ref[k])
+    later = g.get_particles_async().wait()
+    np.testing.assert_array_equal(later["x"], g.get_particles().positions)
+    for k in ref:
+        np.testing.assert_array_equal(first[k], ref[k])  # the earlier read's buffer was not reused
+
+
+def test_run_substeps_equals_substeps_one_by_one():
+    """mpm_run_substeps(dt, k) runs the same substeps as k calls of mpm_substep at s = (i + 1) / k."""
+    d = domain(res=32)
+    mats = [preset("jelly"), preset("sand_dry")]
+    a, b = gpu_solver(d, mats), gpu_solver(d, mats)
+    for s in (a, b):
+        add(s, box_particles((0.3, 0.3, 0.1), (0.5, 0.6, 0.4), d.dx, seed=1), 0, 0, (1.0, 0.0, 0.0))
+        add(s, box_particles((0.55, 0.3, 0.0), (0.7, 0.6, 0.3), d.dx, seed=2), 1, 1)
+    a.run_substeps(2e-4, 12)
+    for i in range(12):
+        b.substep(2e-4, (i + 1) / 12, 12 * 2e-4)
+    sa, sb = a.save_state(), b.save_state()
+    for k in ("x", "v", "F"):
+        assert rel_err(sa[k], sb[k]) <= 1e-5, (k, rel_err(sa[k], sb[k]))
