@@ -364,6 +364,15 @@ def run_large(device: str, frames: int) -> dict:
             frame_ms.append(1e3 * (t4 - f0))
     c1 = s.conservation()
     n1 = s.particle_count
+    # kernel-group times of a few substeps at the end state (event nodes in the substep graph)
+    from mpm_plugin_gb300 import _abi
+
+    s.set_option(_abi.OPT_KERNEL_TIMING, 1)
+    s.kernel_times(reset=True)
+    for _ in range(4):
+        s.substep(8e-5, 1.0, 1 / 96)
+    kt = s.kernel_times(reset=True)
+    s.set_option(_abi.OPT_KERNEL_TIMING, 0)
     s.close()
     total = t_adv + t_emit + t_read
     return {"value": ps / total, "advance_only": ps / t_adv, "unit": UNIT, "frames": frames,
@@ -371,6 +380,7 @@ def run_large(device: str, frames: int) -> dict:
             "seconds": {"advance": t_adv, "emission": t_emit, "read_back": t_read},
             "frame_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
             "tuned": tuned,
+            "kernels_ms_per_substep": {k: t / max(c, 1) for k, (t, c) in kt.items()},
             "conservation_fp64": {"mass": [c0["mass"], c1["mass"]], "ke": [c0["ke"], c1["ke"]],
                                   "momentum_z": [float(c0["momentum"][2]), float(c1["momentum"][2])]},
             "fp64_oracle_error": fp64_error_sample(device)}
