@@ -212,6 +212,18 @@ int mpm_batch_get_stream(void *batch, void **stream);
 /* Kernels launched by the batch and its scenes so far. */
 int mpm_batch_launch_count(void *batch, int64_t *launches);
 
+/* Emitter volume sampling on the device (mpm_core/geometry.py:89-151 up to the jitter): the points of the
+ * cell-centred lattice xs x ys x zs (float64, as the reference builds it: (first + k + 0.5) * spacing) inside
+ * a closed mesh by z-ray parity per (x, y) column, with the column centre nudged by nudge[2] (the reference's
+ * _RAY_NUDGE * spacing). tri: (n_tris, 3, 3) float64 vertex coordinates. Every deciding operation is the
+ * reference's, in FP64 and its order, each rounded on its own, so the same points come out in the same
+ * order (columns in increasing i * ny + j, heights increasing). Writes n_out points (x, y, z float64) to out
+ * when capacity >= n_out; call with out = NULL to learn n_out. The caller adds the reference's seeded
+ * jitter. At most 2^31 column-triangle pairs. Errors: mpm_last_error(NULL). */
+int mpm_volume_lattice(const double *tri, int64_t n_tris, const double *xs, int32_t nx, const double *ys, int32_t ny,
+                       const double *zs, int32_t nz, double spacing, const double nudge[2], int64_t first_x,
+                       int64_t first_y, int32_t device, double *out, int64_t capacity, int64_t *n_out);
+
 #ifdef __cplusplus
 }
 #endif
