@@ -228,17 +228,19 @@ def serve_trace(seconds: float, rate: float, seed: int = 0):
         t += float(rng.exponential(1.0 / rate))
         if t > seconds:
             return trace
-        d, mats, setup, before, frames, fps, max_n, tris = pour_job_spec(seed * 1000 + i)
+        d, mats, setup, before, frames, fps, max_n, tris = pour_job_spec(seed * 1000 + i, res=128, frames=16,
+                                                                         side_range=(0.25, 0.45))
         trace.append((t, BakeJob(f"job{i}", d, mats, frames, fps, setup=setup, before_frame=before,
                                  writer=_FrameSink(), max_particles=max_n, collider_triangles=tris)))
         i += 1
 
 
 def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float = 150.0) -> dict:
-    """Serving: a Poisson trace of pour jobs (96^3, pile of 28k-230k particles plus a 2 m/s disc inflow, a
-    2,048-triangle torus turning at 1 rev/s, 12 frames at 24 fps each) served by the bake server with a
-    150 GB admission budget, against the same trace served sequentially by the plain solver (each job alone,
-    in arrival order, starting when it has arrived and the one before has finished)."""
+    """Serving: a Poisson trace of pour jobs (128^3, a pile of 130k-760k particles plus a 2 m/s disc inflow, a
+    2,048-triangle torus turning at 1 rev/s, 16 frames at 24 fps each; at 4 requests per second the GPU is
+    the bottleneck) served by the bake server with a 150 GB admission budget, against the same trace served
+    sequentially by the plain solver (each job alone, in arrival order, starting when it has arrived and
+    the one before has finished)."""
     import torch
 
     from mpm_plugin_gb300.serve import BakeServer
@@ -280,17 +282,18 @@ def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float
     return {"requests": len(trace), "rate_per_s": rate, "seconds": seconds, "budget_gb": budget_gb,
             "served": served, "plain_sequential": plain,
             "ratio": served["particle_substeps_per_s"] / plain["particle_substeps_per_s"],
-            "workload": "Poisson pour jobs, 96^3, 12 frames at 24 fps, inflow + rotating 2,048-triangle torus; "
+            "workload": "Poisson pour jobs, 128^3, 16 frames at 24 fps, inflow + rotating 2,048-triangle torus; "
                         "frames handed to an in-memory sink in place of the cache writer"}
 
 
 def large_scene(res: int, pile_top: float, seed: int = 3):
     """The large inflow workload at resolution `res`: a Drucker-Prager pile (E 3.5e5, nu 0.3, 30 deg,
     rho 1600) filling (0.2-0.8)^2 x (0-pile_top) at 8 per cell, a seeded perturbed torus of 20,480 triangles
-    (R 0.2, r 0.05, friction 0.4) turning at 1 rev/s about z, and a disc inflow r = 0.05 m at 2 m/s downward.
+    (R 0.2, r 0.05, friction 0.4) turning at 1 rev/s about z, and a disc inflow r = 0.05 m at 2 m/s downward
+    (a closed 48-sided cylinder emitter, one emission substep's slab high).
     Returns (domain, materials, pile, torus mesh, pose(t), emit(solver, piece))."""
     from mpm_plugin_gb300.interface import MaterialParams
-    from scenes import domain, lattice_box, rot_x, rot_z, torus, translate
+    from scenes import cylinder, domain, lattice_box, rot_x, rot_z, torus, translate
 
     d = domain(res=res)
     mats = [MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)]
@@ -300,16 +303,25 @@ def large_scene(res: int, pile_top: float, seed: int = 3):
     def pose(t):
         return translate(0.5, 0.5, pile_top + 0.12) @ rot_z(360.0 * t) @ rot_x(90.0)
 
-    def emit(s, piece):  # one emission substep: the slab 2 m/s x 1/96 s below the disc, where no material is
-        r = np.random.default_rng(seed * 100000 + piece)
-        slab = lattice_box((0.45, 0.45, 0.9), (0.55, 0.55, 0.9 + 2.0 / 96), d.dx / 2, r)
-        slab = slab[np.hypot(slab[:, 0] - 0.5, slab[:, 1] - 0.5) <= 0.05]
-        free = ~s.is_occupied(slab)
-        p = slab[free]
-        if len(p):
-            s.add_particles(p, np.tile(np.float32([0.0, 0.0, -2.0]), (len(p), 1)), np.zeros(len(p), np.int32),
-                            np.zeros(len(p), np.int32))
-        return len(p)
+    ev, et = cylinder(0.05, 2.0 / 96, 48)  # one emission substep's slab of the disc inflow
+    ev = ev + np.float32([0.5, 0.5, 0.9])
+
+    def emit(s, piece):
+        """One emission substep as the bake runner's _emit does it for an inflow (bake.py:56-86): the
+        emitter volume sampled at spacing dx / 2 with the runner's seed list (here: seed, frame, emitter 0,
+        the substep fraction), points outside the domain dropped, points on occupied nodes dropped, the rest
+        added at 2 m/s downward. The sampling runs on the GPU (mpm_plugin_gb300.emit)."""
+        from mpm_plugin_gb300.emit import sample_mesh_volume
+
+        frame, quarter = divmod(piece, 4)
+        pts = sample_mesh_volume(ev, et, d.dx / 2, [seed, frame + 1, 0, quarter + 1, 4])
+        pts = pts[((pts >= np.asarray(d.min)) & (pts <= np.asarray(d.max))).all(1)]
+        if len(pts) and s.particle_count:
+            pts = pts[~s.is_occupied(pts)]
+        if len(pts):
+            s.add_particles(pts, np.tile(np.float32([0.0, 0.0, -2.0]), (len(pts), 1)), np.zeros(len(pts), np.int32),
+                            np.zeros(len(pts), np.int32))
+        return len(pts)
 
     return d, mats, pile, (tv, tt), pose, emit
 
@@ -690,7 +702,7 @@ def main():
     ap.add_argument("--small", type=int, default=1, help="measure the 32k-particle jelly workload (0: skip)")
     ap.add_argument("--large-frames", type=int, default=1,
                     help="24 fps frames of the 256^3 inflow workload (0: skip)")
-    ap.add_argument("--serve-seconds", type=float, default=5.0,
+    ap.add_argument("--serve-seconds", type=float, default=4.0,
                     help="seconds of Poisson bake requests (4 per second) for the serving measurement (0: skip)")
     ap.add_argument("--batched-frames", type=int, default=3,
                     help="frames of the 64-scene batched workload, plain and batched (0: skip)")

@@ -1067,8 +1067,9 @@ struct Batch {
     int64_t cta_cap = 0;
     unsigned int particle_ctas = 0;
     bool any_colliders = false;
-    std::vector<int64_t> layout;             // what the captured graph depends on
-    cudaGraphExec_t graph = nullptr;
+    std::vector<int64_t> layout;             // what the captured graphs depend on
+    cudaGraphExec_t graph = nullptr;         // one batched substep
+    cudaGraphExec_t graph_many = nullptr;    // kGraphReps batched substeps
     unsigned int* d_vmax = nullptr;          // per scene: max |v| bits
     unsigned int* h_vmax = nullptr;          // pinned
     int vmax_cap = 0;
@@ -1088,7 +1089,9 @@ int finish_batch(Batch* b, Status s) {
 
 void batch_invalidate(Batch* b) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->graph_many) cudaGraphExecDestroy(b->graph_many);
     b->graph = nullptr;
+    b->graph_many = nullptr;
     b->layout.clear();
 }
 
@@ -1145,23 +1148,25 @@ Status batch_upload(Batch* b) {
     return {};
 }
 
-Status batch_replay(Batch* b) {
+// reps (1 or kGraphReps) batched substeps in one graph launch.
+Status batch_replay(Batch* b, int reps = 1) {
     BatchLaunch bl{b->d_table, b->d_cta, b->d_cta + b->particle_ctas, (int)b->live.size(), b->particle_ctas,
                    b->any_colliders, b->shape};
-    if (!b->graph) {
+    cudaGraphExec_t& g = reps == 1 ? b->graph : b->graph_many;
+    if (!g) {
         cudaGraph_t graph;
         CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-        launch_batch_substep(b->stream, bl);
+        for (int r = 0; r < reps; ++r) launch_batch_substep(b->stream, bl);
         cudaError_t e0 = cudaGetLastError();
         cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
         CK(e0);
         CK(e);
-        e = cudaGraphInstantiate(&b->graph, graph, 0);
+        e = cudaGraphInstantiate(&g, graph, 0);
         cudaGraphDestroy(graph);
         CK(e);
     }
-    CK(cudaGraphLaunch(b->graph, b->stream));
-    b->launches += batch_substep_kernel_count(bl);
+    CK(cudaGraphLaunch(g, b->stream));
+    b->launches += (int64_t)batch_substep_kernel_count(bl) * reps;
     return {};
 }
 
@@ -1211,13 +1216,20 @@ Status batch_advance(Batch* b, const double* frame_dt, MpmAdvanceStats* stats) {
     }
     if (!b->live.empty()) {
         TRY(batch_upload(b));
-        for (int k = 0; k < max_steps; ++k) {
-            TRY(batch_replay(b));
-            if (b->sort_interval > 0 && (k + 1) % b->sort_interval == 0 && k + 1 < max_steps) {
+        for (int k = 0; k < max_steps;) {
+            // as many substeps per graph launch as fit before the next reorder is due
+            int reps = max_steps - k >= kGraphReps ? kGraphReps : 1;
+            if (b->sort_interval > 0 && reps > 1) {
+                const int to_sort = b->sort_interval - k % b->sort_interval;
+                if (to_sort < reps) reps = 1;
+            }
+            TRY(batch_replay(b, reps));
+            k += reps;
+            if (b->sort_interval > 0 && k % b->sort_interval == 0 && k < max_steps) {
                 bool any = false;
                 for (int s = 0; s < S; ++s) {
                     Handle* h = b->scenes[s];
-                    if (h->P.n == 0 || steps[s] <= k + 1) continue;  // done or empty: no later substep
+                    if (h->P.n == 0 || steps[s] <= k) continue;  // done or empty: no later substep
                     TRY(reorder_particles(h));
                     any = true;
                 }

@@ -27,6 +27,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+from mpm_plugin_gb300.interface import ParticleData
+
 PARTICLE_BYTES = 136  # arena words per particle x 4 B (x v C F Jp stress mat emitter id)
 
 
@@ -207,10 +209,17 @@ class BakeServer:
         counts = [run.solver.particle_count for run in self.runs]
         stats = self.batch.advance([1.0 / run.job.fps for run in self.runs])
         done = []
-        for run, n, st in zip(list(self.runs), counts, stats):
+        # every job's frame read starts at once (each on its own copy stream), then they are collected
+        reads = [run.solver.get_particles_async() if hasattr(run.solver, "get_particles_async") else None
+                 for run in self.runs]
+        for run, n, st, rd in zip(list(self.runs), counts, stats, reads):
             run.frame += 1
             self.report.particle_substeps += n * st.substeps
-            particles = run.solver.get_particles()
+            if rd is not None:
+                a = rd.wait()
+                particles = ParticleData(a["x"], a["v"], a["mat"], a["emitter"])
+            else:
+                particles = run.solver.get_particles()
             if not (np.isfinite(particles.positions).all() and np.isfinite(particles.velocities).all()):
                 done.append((run, f"simulation became unstable at frame {run.frame} (NaN/inf in particle positions)"))
                 continue

@@ -233,7 +233,7 @@ def rot_z(deg: float) -> np.ndarray:
     return m
 
 
-def pour_job_spec(seed: int, res: int = 96, frames: int = 12, fps: float = 24.0):
+def pour_job_spec(seed: int, res: int = 96, frames: int = 12, fps: float = 24.0, side_range=(0.2, 0.4)):
     """A granular pour (the large inflow workload's distribution at a serving size): a Drucker-Prager pile
     (E 3.5e5, nu 0.3, 30 deg, rho 1600) of seeded size, a disc inflow r = 0.05 m at 2 m/s downward whose slab
     of one frame is added where no material is, and a seeded torus collider (2,048 triangles, friction 0.4)
@@ -244,7 +244,7 @@ def pour_job_spec(seed: int, res: int = 96, frames: int = 12, fps: float = 24.0)
     rng = np.random.default_rng(seed)
     d = domain(res=res)
     mat = MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)
-    side = float(rng.uniform(0.2, 0.4))
+    side = float(rng.uniform(*side_range))
     pile = lattice_box((0.5 - side / 2, 0.5 - side / 2, 0.0), (0.5 + side / 2, 0.5 + side / 2, side / 2), d.dx / 2,
                        rng)
     tv, tt = torus(0.18, 0.04, 64, 16, seed=seed, jitter=0.05)
@@ -269,3 +269,17 @@ def pour_job_spec(seed: int, res: int = 96, frames: int = 12, fps: float = 24.0)
 
     slab_n = int(np.pi * 0.05 ** 2 * 2.0 / fps * 8 * res ** 3) + 1
     return d, [mat], setup, before_frame, frames, fps, len(pile) + frames * slab_n, len(tt)
+
+
+def cylinder(radius: float, height: float, segments: int = 32):
+    """Closed cylinder around the z axis from z = 0 to height (4 * segments triangles, outward winding)."""
+    a = 2 * np.pi * np.arange(segments) / segments
+    ring = np.stack([radius * np.cos(a), radius * np.sin(a)], -1)
+    verts = np.concatenate([np.c_[ring, np.zeros(segments)], np.c_[ring, np.full(segments, height)],
+                            [[0.0, 0.0, 0.0], [0.0, 0.0, height]]])
+    bc, tc = 2 * segments, 2 * segments + 1
+    tris = []
+    for k in range(segments):
+        k1 = (k + 1) % segments
+        tris += [[k, k1, segments + k1], [k, segments + k1, segments + k], [bc, k1, k], [tc, segments + k, segments + k1]]
+    return verts.astype(np.float32), np.array(tris, np.int32)
