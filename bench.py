@@ -66,28 +66,37 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs."""
+    """nvidia-smi samples of SM clock and throttle reasons while the timed region runs (every 25 ms; only
+    the samples whose timestamps fall inside the region count)."""
 
-    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
-              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
-              "clocks_event_reasons.sw_power_cap")
+    FIELDS = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
 
     def __enter__(self):
+        import datetime
+
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "25"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)  # the sampler is running before the region starts
         except Exception:
             self.proc = None
+        self.t0 = datetime.datetime.now()
         return self
 
     def __exit__(self, *exc):
+        import datetime
+
+        self.t1 = datetime.datetime.now()
         self.out = ""
         if self.proc:
+            time.sleep(0.05)
             self.proc.terminate()
             try:
                 self.out, _ = self.proc.communicate(timeout=5)
@@ -95,18 +104,23 @@ class Clocks:
                 self.proc.kill()
 
     def summary(self) -> dict:
+        import datetime
+
         sm, mx, reasons = [], [], set()
         names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         for line in (self.out or "").splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) < 8:
+            if len(f) < 9:
                 continue
             try:
-                sm.append(float(f[0]))
-                mx.append(float(f[1]))
+                ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f")
+                if not (self.t0 <= ts <= self.t1):
+                    continue
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
             except ValueError:
                 continue
-            for name, val in zip(names, f[4:8]):
+            for name, val in zip(names, f[5:9]):
                 if val.lower() in ("active", "1", "yes"):
                     reasons.add(name)
         if not sm:
@@ -694,7 +708,7 @@ def run_gpu(args, world, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
