@@ -1,6 +1,7 @@
-// Host side of the C-ABI in include/mpm_gb300.h: device memory, host-side constants, collider BVHs, the
-// substep launch sequence (captured once into a CUDA graph and replayed per substep), CFL time stepping,
-// removal of escaped particles and state I/O.
+// Host side of the C-ABI in include/mpm_gb300.h: device memory, host-side constants, collider BVHs and
+// narrow-band voxel grids, the substep launch sequence (captured into CUDA graphs of one or eight substeps
+// and replayed), CFL time stepping, the periodic reorder, removal of escaped particles, state I/O
+// (synchronous and overlapped), deterministic mode, and batches of scenes.
 //
 // The host constants follow mpm_core/backends/warp/solver.py:37-71 in float64 and are rounded to FP32
 // when stored for the kernels, as the reference's launches do.

@@ -1,5 +1,6 @@
 // One MLS-MPM substep, item by item: the collider pose of the substep, P2G of one particle, the grid update
-// of one node and G2P of one particle. The kernels in mpm_kernels.cu call these per thread; the same
+// of one node, collider contact of one node or particle, and G2P of one particle. The kernels in
+// mpm_substep_kernels.cuh call these per thread (or per warp for shared contact queries); the same
 // functions compile for the host, so the CPU tests run exactly this code against the oracle.
 #pragma once
 

@@ -1,8 +1,8 @@
 // The kernels of one substep, written once for two ways of naming the scenes they work on:
 //   OneScene    - a single scene whose arguments are kernel parameters (the plain solver);
 //   SceneTable  - a device table of scenes (a batch). Particle kernels take one scene per CTA (a per-CTA
-//                 scene index), the kernels over work lists walk every scene's list in turn, and a scene
-//                 whose advance is done (StepParams::active == 0) is skipped by all of them.
+//                 scene index), the kernels over work lists share out the flattened (scene, item) list of
+//                 all scenes, and a scene whose advance is done (StepParams::active == 0) is skipped by all.
 // One substep = step_begin -> clear -> P2G -> grid update -> collider contact -> G2P -> particle projection
 // (warp/solver.py:187-212 for the order).
 #pragma once
