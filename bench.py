@@ -414,41 +414,53 @@ def run_large(device: str, frames: int) -> dict:
 
 def fp64_error_sample(device: str, substeps: int = 100) -> dict:
     """The large workload's physics at 48^3 (pile, turning torus; about 22k particles), 100 substeps at
-    dt = 2e-4 on the GPU (FP32) and on the FP64 oracle: relative error of x, v and of the invariants."""
+    dt = 2e-4 on the GPU (FP32) and on the FP64 oracle: relative error of x, v and of the invariants, for the
+    default build and with the Drucker-Prager clamp redone in FP64 (MPM_OPT_FP64_CLAMP)."""
+    from mpm_plugin_gb300 import _abi
     from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
     from oracle.oracle import OracleSolver
 
     d, mats, pile, (tv, tt), pose, _ = large_scene(48, 0.1)
-    g = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+    gs = [Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device) for _ in range(2)]
+    gs[1].set_option(_abi.OPT_FP64_CLAMP, 1)
     o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f64", threads=os.cpu_count() or 1)
     z = np.zeros(len(pile), np.int32)
-    g.add_particles(pile, np.zeros_like(pile), z, z)
-    o.add_particles(pile, np.zeros_like(pile), z, z)
-    g.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
-    o.set_colliders([(tv, tt, True, 0.4)])
     xf0, xf1 = pose(0.0), pose(1 / 24)
-    g.set_collider_transforms(xf0[None], xf1[None])
+    for g in gs:
+        g.add_particles(pile, np.zeros_like(pile), z, z)
+        g.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
+        g.set_collider_transforms(xf0[None], xf1[None])
+    o.add_particles(pile, np.zeros_like(pile), z, z)
+    o.set_colliders([(tv, tt, True, 0.4)])
     o.set_collider_transforms(xf0[None], xf1[None])
     o.frame_dt = 1 / 24
     t0 = time.perf_counter()
     for k in range(substeps):
         sk = (k + 1) / substeps
-        g.substep(2e-4, sk, 1 / 24)
+        for g in gs:
+            g.substep(2e-4, sk, 1 / 24)
         o.substep(2e-4, sk)
-    a, b = g.save_state(), o.save_state()
-    g.close()
+    b = o.save_state()
+    states = [g.save_state() for g in gs]
+    for g in gs:
+        g.close()
     pm = float(np.float32(1600.0) * np.float32(d.dx ** 3 / 8))
 
     def inv(st):
         x, v = st["x"].astype(np.float64), st["v"].astype(np.float64)
         return (pm * v).sum(0), (x.mean(0)), 0.5 * pm * (v * v).sum()
 
-    (pa, ca, ka), (pb, cb, kb) = inv(a), inv(b)
     rel = lambda u, w: float(np.linalg.norm(u - w) / max(np.linalg.norm(w), 1e-30))
-    return {"particles": len(pile), "substeps": substeps, "dt": 2e-4, "x": rel(a["x"], b["x"]),
-            "v": rel(a["v"], b["v"]), "momentum": rel(pa, pb), "com": rel(ca, cb), "ke": abs(ka - kb) / kb,
-            "oracle_seconds": time.perf_counter() - t0}
+    pb, cb, kb = inv(b)
+
+    def errors(a):
+        pa, ca, ka = inv(a)
+        return {"x": rel(a["x"], b["x"]), "v": rel(a["v"], b["v"]), "F": rel(a["F"], b["F"]),
+                "momentum": rel(pa, pb), "com": rel(ca, cb), "ke": abs(ka - kb) / kb}
+
+    return {"particles": len(pile), "substeps": substeps, "dt": 2e-4, **errors(states[0]),
+            "fp64_clamp": errors(states[1]), "oracle_seconds": time.perf_counter() - t0}
 
 
 def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict:

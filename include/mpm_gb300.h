@@ -127,8 +127,11 @@ enum {
                                   1216 = 8 per SM of a GB300) */
     MPM_OPT_P2G_GROUP = 7,     /* P2G sums same-cell lanes within aligned groups of this many lanes before one
                                   reduction each: 1, 2, 4, 8, 16 or 32 (default) */
-    MPM_OPT_PDL = 8            /* 1 (default): the substep kernels use programmatic dependent launch, so each
+    MPM_OPT_PDL = 8,           /* 1 (default): the substep kernels use programmatic dependent launch, so each
                                   kernel's launch overlaps the tail of the one before; 0: plain stream order */
+    MPM_OPT_FP64_CLAMP = 9     /* 1: a Drucker-Prager or snow particle whose return mapping clamps is redone in
+                                  FP64 (SVD, projection, hardening, stress); 0 (default): FP32, with the FP64
+                                  redo only for SVDs that did not converge */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

@@ -145,6 +145,7 @@ struct Handle {
     int64_t since_sort = 0;
 
     LaunchShape shape;                      // autotuned launch choices
+    bool fp64_clamp = false;                // Drucker-Prager / snow return mapping in FP64 at an active clamp
     bool deterministic = false;
     unsigned long long* d_fixed = nullptr;  // deterministic mode: fixed-point node sums (4 per node)
     unsigned int* d_poison = nullptr;       // deterministic mode: non-finite marks (1 per node)
@@ -352,6 +353,7 @@ SubstepArgs substep_args(Handle* h) {
     a.poison = h->deterministic ? h->d_poison : nullptr;
     a.fixed_exp = h->fixed_exp;
     a.p2g_group = h->shape.p2g_group;
+    a.fp64_clamp = h->fp64_clamp ? 1 : 0;
     return a;
 }
 
@@ -458,8 +460,8 @@ Status run_substep(Handle* h, int reps = 1) {
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
                                      (int64_t)h->shape.list_ctas,
-                                     (((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
-                                             64 + reps};
+                                     ((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
+                                              2 + (h->fp64_clamp ? 1 : 0)) * 64 + reps};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -1491,6 +1493,10 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             return MPM_OK;
         case MPM_OPT_PDL:
             h->shape.pdl = value != 0;
+            return MPM_OK;
+        case MPM_OPT_FP64_CLAMP:
+            h->fp64_clamp = value != 0;
+            invalidate_graph(h);  // the flag is a kernel argument of the captured graphs
             return MPM_OK;
         case MPM_OPT_P2G_GROUP:
             if (value < 1 || value > 32 || (value & (value - 1)))

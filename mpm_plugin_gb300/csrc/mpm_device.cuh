@@ -11,6 +11,11 @@
 
 // The math below also compiles for the host (tests check the SVD's accuracy on the CPU).
 #define MPM_HD __host__ __device__ __forceinline__
+#ifdef __CUDACC__
+#define MPM_HD_NOINLINE __host__ __device__ __noinline__
+#else
+#define MPM_HD_NOINLINE __attribute__((noinline))
+#endif
 
 namespace mpm {
 
@@ -248,11 +253,27 @@ MPM_HD void bspline_weights(float fx, float w[3]) {
 //   fixed-corotated (kernels.py:30-38): 2 mu (F - R) F^T + lam J (J - 1) I = U diag(2 mu (s-1) s + lam J (J-1)) U^T
 //   Hencky / St. Venant-Kirchhoff (kernels.py:51-60): U diag(2 mu eps + lam tr eps) U^T, eps = log max(s, 1e-4)
 // ---------------------------------------------------------------------------------------------------------
-MPM_HD float jm1(const float d[3]) {  // J - 1 = prod(1 + d) - 1, expanded so small strains keep their digits
+// Elementary functions of either precision (the float versions are the single-precision calls).
+MPM_HD float log1p_t(float x) { return log1pf(x); }
+MPM_HD double log1p_t(double x) { return log1p(x); }
+MPM_HD float expm1_t(float x) { return expm1f(x); }
+MPM_HD double expm1_t(double x) { return expm1(x); }
+MPM_HD float log_t(float x) { return logf(x); }
+MPM_HD double log_t(double x) { return log(x); }
+MPM_HD float exp_t(float x) { return expf(x); }
+MPM_HD double exp_t(double x) { return exp(x); }
+MPM_HD float min_t(float a, float b) { return fminf(a, b); }
+MPM_HD double min_t(double a, double b) { return fmin(a, b); }
+MPM_HD float max_t(float a, float b) { return fmaxf(a, b); }
+MPM_HD double max_t(double a, double b) { return fmax(a, b); }
+
+template <typename T>
+MPM_HD T jm1(const T d[3]) {  // J - 1 = prod(1 + d) - 1, expanded so small strains keep their digits
     return d[0] + d[1] + d[2] + (d[0] * d[1] + d[0] * d[2] + d[1] * d[2]) + d[0] * d[1] * d[2];
 }
 
-MPM_HD void sym_from_diag(const float U[3][3], const float g[3], float tau[3][3]) {
+template <typename T>
+MPM_HD void sym_from_diag(const T U[3][3], const T g[3], T tau[3][3]) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -261,22 +282,25 @@ MPM_HD void sym_from_diag(const float U[3][3], const float g[3], float tau[3][3]
 
 // Principal Kirchhoff stresses of the fixed-corotated energy (kernels.py:30-38) from the singular values sig
 // and their deviations d = sig - 1: 2 mu (sig - 1) sig + lam (J - 1) J.
-MPM_HD void corotated_principal(float mu, float lam, const float sig[3], const float d[3], float g[3]) {
-    float Jm1 = jm1(d);
-    float iso = lam * (1.0f + Jm1) * Jm1;
+template <typename T>
+MPM_HD void corotated_principal(T mu, T lam, const T sig[3], const T d[3], T g[3]) {
+    T Jm1 = jm1(d);
+    T iso = lam * (T(1) + Jm1) * Jm1;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) g[i] = 2.0f * mu * d[i] * sig[i] + iso;
+    for (int i = 0; i < 3; ++i) g[i] = T(2) * mu * d[i] * sig[i] + iso;
 }
 
-MPM_HD float safe_log_dev(float s, float d) {  // log(max(s, 1e-4)) from d = s - 1 (kernels.py:41-43)
-    return s > 1.0e-4f ? log1pf(d) : logf(1.0e-4f);
+template <typename T>
+MPM_HD T safe_log_dev(T s, T d) {  // log(max(s, 1e-4)) from d = s - 1 (kernels.py:41-43)
+    return s > T(1.0e-4f) ? log1p_t(d) : log_t(T(1.0e-4f));
 }
 
 // Principal Kirchhoff stresses of the Hencky (logarithmic) energy (kernels.py:51-60): 2 mu e + lam tr(e).
-MPM_HD void hencky_principal(float mu, float lam, const float sig[3], const float d[3], float g[3]) {
-    float e0 = safe_log_dev(sig[0], d[0]), e1 = safe_log_dev(sig[1], d[1]), e2 = safe_log_dev(sig[2], d[2]);
-    float tr = e0 + e1 + e2;
-    float two_mu = 2.0f * mu;
+template <typename T>
+MPM_HD void hencky_principal(T mu, T lam, const T sig[3], const T d[3], T g[3]) {
+    T e0 = safe_log_dev(sig[0], d[0]), e1 = safe_log_dev(sig[1], d[1]), e2 = safe_log_dev(sig[2], d[2]);
+    T tr = e0 + e1 + e2;
+    T two_mu = T(2) * mu;
     g[0] = two_mu * e0 + lam * tr;
     g[1] = two_mu * e1 + lam * tr;
     g[2] = two_mu * e2 + lam * tr;
@@ -302,50 +326,52 @@ MPM_HD void hencky_tau(const float F[3][3], float mu, float lam, float tau[3][3]
 // change of the singular values, delta = new - old, computed without cancellation; the caller applies
 // F <- F + U diag(delta) V^T, which equals U diag(new) V^T exactly when the SVD is exact and leaves F
 // untouched (no reconstruction round-off) when nothing is projected. Returns false when delta == 0.
+// Written for either precision: FP32 for the bulk, FP64 for the optional redo at an active clamp.
 // ---------------------------------------------------------------------------------------------------------
-MPM_HD bool project_von_mises(const float sig[3], const float d[3], float mu, float yield_stress, float delta[3]) {
-    float e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
-    float third = (e[0] + e[1] + e[2]) / 3.0f;
-    float dev[3] = {e[0] - third, e[1] - third, e[2] - third};
-    float n = sqrtf(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
-    float limit = yield_stress / (2.0f * mu);
+template <typename T>
+MPM_HD bool project_von_mises(const T sig[3], const T d[3], T mu, T yield_stress, T delta[3]) {
+    T e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
+    T third = (e[0] + e[1] + e[2]) / T(3);
+    T dev[3] = {e[0] - third, e[1] - third, e[2] - third};
+    T n = sqrt_t(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
+    T limit = yield_stress / (T(2) * mu);
     if (!(n > limit)) return false;
-    float f = limit / n;
+    T f = limit / n;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) delta[i] = expm1f(third + dev[i] * f) - d[i];
+    for (int i = 0; i < 3; ++i) delta[i] = expm1_t(third + dev[i] * f) - d[i];
     return true;
 }
 
-MPM_HD bool project_drucker_prager(const float sig[3], const float d[3], float mu, float lam, float alpha,
-                                   float delta[3]) {
-    float e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
-    float tr = e[0] + e[1] + e[2];
-    if (tr >= 0.0f) {  // separation: stress-free, singular values back to 1
+template <typename T>
+MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T alpha, T delta[3]) {
+    T e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
+    T tr = e[0] + e[1] + e[2];
+    if (tr >= T(0)) {  // separation: stress-free, singular values back to 1
 #pragma unroll
         for (int i = 0; i < 3; ++i) delta[i] = -d[i];
         return true;
     }
-    float third = tr / 3.0f;
-    float dev[3] = {e[0] - third, e[1] - third, e[2] - third};
-    float n = sqrtf(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
-    if (n < 1.0e-10f) return false;
-    float dgamma = n + (3.0f * lam + 2.0f * mu) / (2.0f * mu) * tr * alpha;
-    if (dgamma <= 0.0f) return false;
-    float f = dgamma / n;
+    T third = tr / T(3);
+    T dev[3] = {e[0] - third, e[1] - third, e[2] - third};
+    T n = sqrt_t(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
+    if (n < T(1.0e-10f)) return false;
+    T dgamma = n + (T(3) * lam + T(2) * mu) / (T(2) * mu) * tr * alpha;
+    if (dgamma <= T(0)) return false;
+    T f = dgamma / n;
 #pragma unroll
-    for (int i = 0; i < 3; ++i) delta[i] = expm1f(e[i] - dev[i] * f) - d[i];
+    for (int i = 0; i < 3; ++i) delta[i] = expm1_t(e[i] - dev[i] * f) - d[i];
     return true;
 }
 
-MPM_HD bool project_snow(const float sig[3], const float d[3], float clamp_lo, float clamp_hi, float delta[3],
-                         float* jp_ratio) {
+template <typename T>
+MPM_HD bool project_snow(const T sig[3], const T d[3], T clamp_lo, T clamp_hi, T delta[3], T* jp_ratio) {
     bool any = false;
-    float num = 1.0f, den = 1.0f;
+    T num = T(1), den = T(1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        float ns = fminf(fmaxf(sig[i], clamp_lo), clamp_hi);
-        delta[i] = ns == sig[i] ? 0.0f : (ns - 1.0f) - d[i];
-        any |= delta[i] != 0.0f;
+        T ns = min_t(max_t(sig[i], clamp_lo), clamp_hi);
+        delta[i] = ns == sig[i] ? T(0) : (ns - T(1)) - d[i];
+        any |= delta[i] != T(0);
         num *= sig[i];
         den *= ns;
     }

@@ -364,9 +364,72 @@ MPM_HD float4 load_node(const float4* p) {
 
 // G2P of one particle gathering node velocities from `src` (src(i, j, k) -> float4); the new position goes
 // to nx_out.
+// FP64 redo of a Drucker-Prager or snow particle whose FP32 projection was active (the option to keep the
+// return mapping at the clamp in double precision): the trial F rebuilt in FP64 from the stored F and the
+// new C (both still in memory), then the SVD (eight double sweeps), the return mapping, the projected F, the
+// snow hardening and the stress in FP64, rounded to FP32 only when stored.
+// Kept out of line so that the FP32 path's register allocation does not carry the FP64 working set.
+static MPM_HD_NOINLINE void plastic_redo_fp64(const Particles& P, int64_t p, const Material& m, float dt, float jp_old,
+                                              float Fn_out[3][3], float* jp_out, float t_out[6]) {
+    float F[3][3], C[3][3];
+    load_mat3(P.F, p, F);
+    load_mat3(P.C, p, C);
+    double A[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            A[i][j] = ((i == 0 ? 1.0 : 0.0) + (double)dt * C[i][0]) * F[0][j] +
+                      ((i == 1 ? 1.0 : 0.0) + (double)dt * C[i][1]) * F[1][j] +
+                      ((i == 2 ? 1.0 : 0.0) + (double)dt * C[i][2]) * F[2][j];  // (I + dt C) F
+    double U[3][3], sig[3], d[3], V[3][3], delta[3];
+    svd3_dev_core<double, 8>(A, U, sig, d, V);
+    double jp = jp_old;
+    bool moved;
+    if (m.model == 2) {
+        moved = project_drucker_prager<double>(sig, d, m.mu, m.lam, m.alpha, delta);
+    } else {
+        double ratio;
+        moved = project_snow<double>(sig, d, m.clamp_lo, m.clamp_hi, delta, &ratio);
+        jp = jp * ratio;
+    }
+    if (moved) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                A[i][j] += U[i][0] * delta[0] * V[j][0] + U[i][1] * delta[1] * V[j][1] + U[i][2] * delta[2] * V[j][2];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            sig[i] += delta[i];
+            d[i] += delta[i];
+        }
+    }
+    double gp[3], tau[3][3];
+    if (m.model == 2) {
+        hencky_principal<double>(m.mu, m.lam, sig, d, gp);
+    } else {
+        const double h = min_t(exp_t((double)m.hardening * (1.0 - jp)), (double)m.max_hardening);
+        corotated_principal<double>(m.mu * h, m.lam * h, sig, d, gp);
+    }
+    sym_from_diag<double>(U, gp, tau);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Fn_out[i][j] = (float)A[i][j];
+    *jp_out = (float)jp;
+    t_out[0] = (float)tau[0][0];
+    t_out[1] = (float)tau[1][1];
+    t_out[2] = (float)tau[2][2];
+    t_out[3] = (float)tau[0][1];
+    t_out[4] = (float)tau[0][2];
+    t_out[5] = (float)tau[1][2];
+}
+
 template <class Source>
 MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
-                              float dt, const Source& src, unsigned int* fp64, float nx_out[3]) {
+                              float dt, const Source& src, unsigned int* fp64, float nx_out[3],
+                              bool fp64_clamp = false) {
     float xo[3];
     int base[3];
     float fx[3], w[3][3];
@@ -427,7 +490,9 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     const Material m = mats[P.mat[p]];
     float U[3][3], sig[3], d[3], V[3][3];
     svd3(Fn, U, sig, d, V, fp64);
-    float jp = P.Jp[p];
+    const float jp_old = P.Jp[p];
+    float jp = jp_old;
+    bool redo = false;  // FP64 redo at an active Drucker-Prager or snow clamp
     if (m.model != 0) {
         float delta[3];
         bool moved;
@@ -439,8 +504,8 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
             float ratio;
             moved = project_snow(sig, d, m.clamp_lo, m.clamp_hi, delta, &ratio);
             jp = jp * ratio;
-            P.Jp[p] = jp;
         }
+        redo = fp64_clamp && moved && m.model >= 2;
         if (moved) {  // F = U diag(new) V^T, applied as F + U diag(new - old) V^T
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -454,9 +519,13 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
             }
         }
     }
-    store_mat3(P.F, p, Fn);
     float t[6];
-    tau_from_svd(m, jp, U, sig, d, t);
+    if (redo)
+        plastic_redo_fp64(P, p, m, dt, jp_old, Fn, &jp, t);  // reads F and C before F is overwritten
+    else
+        tau_from_svd(m, jp, U, sig, d, t);
+    store_mat3(P.F, p, Fn);
+    if (m.model == 3) P.Jp[p] = jp;
 #pragma unroll
     for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
 
@@ -475,9 +544,9 @@ struct GlobalSource {
 };
 
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3]) {
+                         const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false) {
     GlobalSource src{&g, grid};
-    g2p_particle_from(P, p, mats, g, dt, src, fp64, nx_out);
+    g2p_particle_from(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     const int64_t p = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x + threadIdx.x;
     if (p >= a.n) return;
     float nx[3];
-    g2p_particle(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx);
+    g2p_particle(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx, a.fp64_clamp != 0);
     if (a.cd.n_col > 0) {
         ColliderData cd = a.cd;
         cd.poses += a.sp->pose_base;

@@ -127,6 +127,42 @@ def test_one_substep_matches_oracle(scene):
         assert e <= 1e-5, (k, e)
 
 
+def test_fp64_clamp_is_closer_to_the_fp64_oracle():
+    """Sand (Drucker-Prager) and snow particles at an active clamp redone in FP64 (MPM_OPT_FP64_CLAMP): one
+    substep stays within 1e-5 of the FP32 oracle and its F, Jp and x are no further from the FP64 oracle than
+    the FP32 build's."""
+    from mpm_plugin_gb300 import _abi
+
+    d = domain(res=32)
+    mats = [preset("sand_dry"), preset("snow_packed")]
+    groups = [(box_particles((0.1 + 0.4 * i, 0.3, 0.05), (0.45 + 0.4 * i, 0.6, 0.4), d.dx, seed=i), i, (0, 0, 0))
+              for i in range(2)]
+    gs = [gpu_solver(d, mats), gpu_solver(d, mats)]
+    gs[1].set_option(_abi.OPT_FP64_CLAMP, 1)
+    o32, o64 = _oracle(d, mats), _oracle(d, mats, precision="f64")
+    for pos, m, vel in groups:
+        add(gs[0], pos, m, m, vel)
+    state = perturbed_state(gs[0].save_state(), seed=5)
+    for s in (*gs, o32, o64):
+        s.load_state(state)
+    for s in gs:
+        s.substep(2e-4, 1.0, 1 / 24)
+    for o in (o32, o64):
+        o.frame_dt = 1 / 24
+        o.substep(2e-4, 1.0)
+    plain, redo = gs[0].save_state(), gs[1].save_state()
+    r32, r64 = o32.save_state(), o64.save_state()
+    snow_clamped = (r64["mat"] == 1) & (r64["Jp"] != state["Jp"])  # snow's Jp changes only at the clamp
+    assert snow_clamped.sum() > 100
+    for k in ("x", "v", "F", "Jp"):
+        assert rel_err(redo[k], r32[k]) <= 1e-5, k
+    e_plain = {k: rel_err(plain[k], r64[k]) for k in ("x", "F", "Jp")}
+    e_redo = {k: rel_err(redo[k], r64[k]) for k in ("x", "F", "Jp")}
+    print({k: f"{e_plain[k]:.2e} -> {e_redo[k]:.2e}" for k in e_plain})
+    for k in e_plain:
+        assert e_redo[k] <= 1.05 * e_plain[k] + 1e-9, (k, e_plain[k], e_redo[k])
+
+
 def _invariants(s: dict, pmass: np.ndarray) -> dict:
     x, v = s["x"].astype(np.float64), s["v"].astype(np.float64)
     m = pmass.astype(np.float64)
