@@ -129,9 +129,12 @@ enum {
                                   reduction each: 1, 2, 4, 8, 16 or 32 (default) */
     MPM_OPT_PDL = 8,           /* 1 (default): the substep kernels use programmatic dependent launch, so each
                                   kernel's launch overlaps the tail of the one before; 0: plain stream order */
-    MPM_OPT_FP64_CLAMP = 9     /* 1: a Drucker-Prager or snow particle whose return mapping clamps is redone in
+    MPM_OPT_FP64_CLAMP = 9,    /* 1: a Drucker-Prager or snow particle whose return mapping clamps is redone in
                                   FP64 (SVD, projection, hardening, stress); 0 (default): FP32, with the FP64
                                   redo only for SVDs that did not converge */
+    MPM_OPT_P2G_TILE = 10      /* 1: P2G sums each CTA's contributions in shared-memory tiles of the nodes its
+                                  particles touch, then adds them to the grid; 0 (default): warp segments
+                                  (shuffle sums of same-cell lanes) only. Deterministic mode uses segments */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 
@@ -209,7 +212,8 @@ int mpm_batch_size(void *batch, int32_t *n);
 /* One frame of every scene, in the order they were added: frame_dt[i] for scene i (its advance(frame_dt),
  * mpm_core/solver.py:67-68), stats[i] as mpm_advance returns them. */
 int mpm_batch_advance(void *batch, const double *frame_dt, MpmAdvanceStats *stats);
-/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP, MPM_OPT_PDL for the batch */
+/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP, MPM_OPT_PDL, MPM_OPT_P2G_TILE
+   for the batch */
 int mpm_batch_set_option(void *batch, int32_t option, int64_t value);
 int mpm_batch_get_stream(void *batch, void **stream);
 /* Kernels launched by the batch and its scenes so far. */

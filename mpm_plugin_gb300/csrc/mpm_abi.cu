@@ -460,8 +460,8 @@ Status run_substep(Handle* h, int reps = 1) {
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
                                      (int64_t)h->shape.list_ctas,
-                                     ((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
-                                              2 + (h->fp64_clamp ? 1 : 0)) * 64 + reps};
+                                     (((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
+                                               2 + (h->fp64_clamp ? 1 : 0)) * 2 + h->shape.p2g_tile) * 64 + reps};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -893,6 +893,7 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     *out = h;
     h->device = device;
     DeviceGuard guard(device);
+    CK(prepare_substep_kernels());
     CK(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
     h->stream = h->own_stream;
     h->dom = *dom;
@@ -1494,6 +1495,9 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
         case MPM_OPT_PDL:
             h->shape.pdl = value != 0;
             return MPM_OK;
+        case MPM_OPT_P2G_TILE:
+            h->shape.p2g_tile = value != 0;
+            return MPM_OK;
         case MPM_OPT_FP64_CLAMP:
             h->fp64_clamp = value != 0;
             invalidate_graph(h);  // the flag is a kernel argument of the captured graphs
@@ -1678,6 +1682,8 @@ int mpm_batch_add(void* batch, void* handle) {
     Handle* h = static_cast<Handle*>(handle);
     if (!h) return finish_batch(b, {MPM_ERR_ARGUMENT, "null handle"});
     DeviceGuard guard(h->device);
+    if (cudaError_t e = prepare_batch_kernels(); e != cudaSuccess)
+        return finish_batch(b, {MPM_ERR_CUDA, cudaGetErrorString(e)});
     return finish_batch(b, batch_add(b, h));
 }
 
@@ -1721,6 +1727,11 @@ int mpm_batch_set_option(void* batch, int32_t option, int64_t value) {
     }
     if (option == MPM_OPT_PDL) {
         b->shape.pdl = value != 0;
+        batch_invalidate(b);
+        return MPM_OK;
+    }
+    if (option == MPM_OPT_P2G_TILE) {
+        b->shape.p2g_tile = value != 0;
         batch_invalidate(b);
         return MPM_OK;
     }

@@ -13,7 +13,12 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
     const bool pdl = b.shape.pdl != 0;
     launch_step_kernel(k_step_begin<SceneTable>, 1, 128, st, pdl, sc);
     launch_step_kernel(k_clear_blocks<SceneTable>, list_ctas, 256, st, pdl, sc);
-    if (b.particle_ctas > 0) launch_step_kernel(k_p2g_scatter<SceneTable>, b.particle_ctas, 256, st, pdl, sc);
+    if (b.particle_ctas > 0) {  // a deterministic scene takes the warp-segment path inside k_p2g_tile
+        if (b.shape.p2g_tile)
+            launch_step_kernel_smem(k_p2g_tile<SceneTable>, b.particle_ctas, 256, kP2gTileBytes, st, pdl, sc);
+        else
+            launch_step_kernel(k_p2g_scatter<SceneTable>, b.particle_ctas, 256, st, pdl, sc);
+    }
     launch_step_kernel(k_grid_update<SceneTable>, list_ctas, 256, st, pdl, sc);
     if (b.any_colliders) launch_step_kernel(k_grid_colliders<SceneTable>, list_ctas, 128, st, pdl, sc);
     if (b.particle_ctas > 0) {
@@ -23,6 +28,10 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
             launch_step_kernel(k_g2p<SceneTable, 3>, b.particle_ctas, 256, st, pdl, sc);
     }
     if (b.any_colliders) launch_step_kernel(k_project_particles<SceneTable>, list_ctas, 128, st, pdl, sc);
+}
+
+cudaError_t prepare_batch_kernels() {
+    return cudaFuncSetAttribute(k_p2g_tile<SceneTable>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2gTileBytes);
 }
 
 int batch_substep_kernel_count(const BatchLaunch& b) {

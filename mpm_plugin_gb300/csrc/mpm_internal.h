@@ -33,17 +33,18 @@ struct LaunchShape {
     int g2p_variant = 0;
     int p2g_group = 32;  // lanes of the aligned groups P2G sums within (a power of two, 1 .. 32)
     int pdl = 1;         // 1: the substep kernels launch with programmatic dependent launch
+    int p2g_tile = 0;    // 1: P2G through shared-memory tiles per CTA (k_p2g_tile); 0: warp segments only
 };
 
 // Launch of a substep kernel: with shape.pdl the launch carries the programmatic-stream-serialization
 // attribute (the kernel's launch may overlap the previous kernel's tail; the kernel waits for it itself).
 template <typename... KArgs, typename... Args>
-inline void launch_step_kernel(void (*kernel)(KArgs...), unsigned int grid, unsigned int block, cudaStream_t st,
-                               bool pdl, Args... args) {
+inline void launch_step_kernel_smem(void (*kernel)(KArgs...), unsigned int grid, unsigned int block, size_t smem,
+                                    cudaStream_t st, bool pdl, Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -52,6 +53,15 @@ inline void launch_step_kernel(void (*kernel)(KArgs...), unsigned int grid, unsi
     cfg.numAttrs = pdl ? 1 : 0;
     cudaLaunchKernelEx(&cfg, kernel, args...);
 }
+template <typename... KArgs, typename... Args>
+inline void launch_step_kernel(void (*kernel)(KArgs...), unsigned int grid, unsigned int block, cudaStream_t st,
+                               bool pdl, Args... args) {
+    launch_step_kernel_smem(kernel, grid, block, 0, st, pdl, args...);
+}
+// Function attributes the substep kernels need (the tiled P2G's dynamic shared memory above 48 KB); called
+// once per solver and batch, outside stream capture.
+cudaError_t prepare_substep_kernels();
+cudaError_t prepare_batch_kernels();
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing);
 int substep_kernel_count(const SubstepArgs& a);
 

@@ -460,7 +460,12 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
     launch_step_kernel(k_step_begin<OneScene>, 1, 1, st, pdl, sc);
     launch_step_kernel(k_clear_blocks<OneScene>, list_ctas, 256, st, pdl, sc);
     mark(1);
-    if (a.n > 0) launch_step_kernel(k_p2g_scatter<OneScene>, blocks_for(a.n, 256), 256, st, pdl, sc);
+    if (a.n > 0) {
+        if (shape.p2g_tile && !a.fixed)
+            launch_step_kernel_smem(k_p2g_tile<OneScene>, blocks_for(a.n, 256), 256, kP2gTileBytes, st, pdl, sc);
+        else
+            launch_step_kernel(k_p2g_scatter<OneScene>, blocks_for(a.n, 256), 256, st, pdl, sc);
+    }
     mark(2);
     launch_step_kernel(k_grid_update<OneScene>, list_ctas, 256, st, pdl, sc);
     if (a.cd.n_col > 0) launch_step_kernel(k_grid_colliders<OneScene>, list_ctas, 128, st, pdl, sc);
@@ -506,6 +511,10 @@ void launch_sdf_classify(cudaStream_t st, const ColliderDev& col, const BvhNode*
 void launch_sdf_fill(cudaStream_t st, const ColliderDev& col, const BvhNode* nodes, const MeshTri* tris, int64_t n_vox,
                      int max_cand, int2* cells, const int32_t* starts, int32_t* cand) {
     k_sdf_fill<<<blocks_for(n_vox, 128), 128, 0, st>>>(col, nodes, tris, n_vox, max_cand, cells, starts, cand);
+}
+
+cudaError_t prepare_substep_kernels() {
+    return cudaFuncSetAttribute(k_p2g_tile<OneScene>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2gTileBytes);
 }
 
 int substep_kernel_count(const SubstepArgs& a) {

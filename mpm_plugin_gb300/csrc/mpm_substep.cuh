@@ -168,12 +168,36 @@ MPM_HD void particle_stress(const Particles& P, int64_t p, const Material* __res
     for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
 }
 
+// Node index of the stencil nodes base + (i, j, k): the blocked layout's index is a sum of one term per
+// axis (node_index), so the 27 indices are x[i] + y[j] + z[k] from nine per-axis terms.
+struct StencilIndex {
+    int64_t x[3];
+    int y[3], z[3];
+    MPM_HD int64_t operator()(int i, int j, int k) const { return x[i] + (int64_t)(y[j] + z[k]); }
+};
+
+MPM_HD StencilIndex stencil_index(const GridDesc& g, const int base[3]) {
+    StencilIndex s;
+    const int64_t slab = (int64_t)g.nb[1] * g.nb[2] * 64;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int i = base[0] + d, j = base[1] + d, k = base[2] + d;
+        s.x[d] = (int64_t)(i >> 2) * slab + (i & 3) * 16;
+        s.y[d] = (j >> 2) * g.nb[2] * 64 + (j & 3) * 4;
+        s.z[d] = (k >> 2) * 64 + (k & 3);
+    }
+    return s;
+}
+
 // Per-particle terms of P2G (kernels.py:93-140): stencil base and weights, p_mass v and the affine matrix
 // A = -dt p_vol 4 inv_dx^2 tau + p_mass C. tau is the particle's stored Kirchhoff stress, computed from F at
-// the end of the previous G2P (or when the particle entered), so P2G itself decomposes nothing.
+// the end of the previous G2P (or when the particle entered), so P2G itself decomposes nothing. The
+// contribution to stencil node (i, j, k) is w (p_mass v + A dpos) with dpos = ((i, j, k) - fx) dx; written as
+// w (u0 + dA (i, j, k)) with dA = A dx and u0 = p_mass v - dA fx, the per-node work is a few multiply-adds by
+// small integers along the stencil.
 struct P2gTerms {
     int base[3];
-    float fx[3], w[3][3], mv[3], A[3][3], pm;
+    float w[3][3], u0[3], dA[3][3], pm;
 };
 
 // False when the stencil leaves the grid (the particle scatters nothing).
@@ -184,28 +208,35 @@ MPM_HD bool p2g_terms(const Particles& P, int64_t p, const Material* __restrict_
     const float tau[3][3] = {{t0, t3, t4}, {t3, t1, t5}, {t4, t5, t2}};
     t.pm = mats[P.mat[p]].p_mass;
     const float k_stress = -dt * g.p_vol * 4.0f * g.inv_dx * g.inv_dx;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) t.A[i][j] = k_stress * tau[i][j] + t.pm * P.C[i * 3 + j][p];
     bool inside = true;
+    float fx[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         float xp = (P.x[a][p] - g.origin[a]) * g.inv_dx;
-        inside &= stencil_axis(xp, g.dims[a], &t.base[a], &t.fx[a]);
-        bspline_weights(t.fx[a], t.w[a]);
-        t.mv[a] = t.pm * P.v[a][p];
+        inside &= stencil_axis(xp, g.dims[a], &t.base[a], &fx[a]);
+        bspline_weights(fx[a], t.w[a]);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t.dA[i][j] = (k_stress * tau[i][j] + t.pm * P.C[i * 3 + j][p]) * g.dx;
+        t.u0[i] = t.pm * P.v[i][p] - (t.dA[i][0] * fx[0] + t.dA[i][1] * fx[1] + t.dA[i][2] * fx[2]);
     }
     return inside;
 }
 
-// Momentum (x, y, z) and mass the particle adds to stencil node (i, j, k), i, j, k in 0..2:
-// w (p_mass v + A (x_i - x_p)) and w p_mass.
-MPM_HD void p2g_node(const P2gTerms& t, const GridDesc& g, int i, int j, int k, float out[4]) {
-    float wt = t.w[0][i] * t.w[1][j] * t.w[2][k];
-    float dpos[3] = {((float)i - t.fx[0]) * g.dx, ((float)j - t.fx[1]) * g.dx, ((float)k - t.fx[2]) * g.dx};
+// Momentum (x, y, z) and mass the particle adds to stencil node (i, j, k), i, j, k in 0..2. In unrolled
+// loops the partial sums along i and j are common to the later nodes.
+MPM_HD void p2g_node(const P2gTerms& t, int i, int j, int k, float out[4]) {
+    const float wt = (t.w[0][i] * t.w[1][j]) * t.w[2][k];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) out[a] = wt * (t.mv[a] + (t.A[a][0] * dpos[0] + t.A[a][1] * dpos[1] + t.A[a][2] * dpos[2]));
+    for (int a = 0; a < 3; ++a) {
+        float u = t.u0[a];
+        if (i) u = fmaf(t.dA[a][0], (float)i, u);
+        if (j) u = fmaf(t.dA[a][1], (float)j, u);
+        if (k) u = fmaf(t.dA[a][2], (float)k, u);
+        out[a] = wt * u;
+    }
     out[3] = wt * t.pm;
 }
 
@@ -234,7 +265,7 @@ MPM_HD bool p2g_particle_into(const Particles& P, int64_t p, const Material* __r
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 float val[4];
-                p2g_node(t, g, i, j, k, val);
+                p2g_node(t, i, j, k, val);
                 sink.add(t.base[0] + i, t.base[1] + j, t.base[2] + k, val[0], val[1], val[2], val[3]);
             }
     return true;
@@ -362,8 +393,6 @@ MPM_HD float4 load_node(const float4* p) {
 #endif
 }
 
-// G2P of one particle gathering node velocities from `src` (src(i, j, k) -> float4); the new position goes
-// to nx_out.
 // FP64 redo of a Drucker-Prager or snow particle whose FP32 projection was active (the option to keep the
 // return mapping at the clamp in double precision): the trial F rebuilt in FP64 from the stored F and the
 // new C (both still in memory), then the SVD (eight double sweeps), the return mapping, the projected F, the
@@ -426,6 +455,8 @@ static MPM_HD_NOINLINE void plastic_redo_fp64(const Particles& P, int64_t p, con
     t_out[5] = (float)tau[1][2];
 }
 
+// G2P of one particle gathering node velocities from `src` (src(node index) -> float4); the new position goes
+// to nx_out.
 template <class Source>
 MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
                               float dt, const Source& src, unsigned int* fp64, float nx_out[3],
@@ -441,27 +472,50 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
         inside &= stencil_axis(xp, g.dims[a], &base[a], &fx[a]);
         bspline_weights(fx[a], w[a]);
     }
-    float nv[3] = {0.f, 0.f, 0.f}, nC[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-    const float cscale = 4.0f * g.inv_dx * g.inv_dx;
-    if (inside)
+    // v = sum w gv and C = 4 inv_dx^2 sum w gv (x) dpos (kernels.py:214-227). With dpos = ((i, j, k) - fx) dx,
+    // sum w gv dpos_c = dx (S_c - fx_c v) where S_c = sum w gv idx_c; the sums are taken along k, then j, then
+    // i, so each node costs six multiply-adds (w gv and idx_k w gv) instead of twenty-one.
+    float nv[3] = {0.f, 0.f, 0.f}, S[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    if (inside) {
+        const StencilIndex at = stencil_index(g, base);
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 3; ++i) {
+            float Q[3] = {0.f, 0.f, 0.f}, Qj[3] = {0.f, 0.f, 0.f}, Qk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int j = 0; j < 3; ++j)
+            for (int j = 0; j < 3; ++j) {
+                float R[3] = {0.f, 0.f, 0.f}, Rk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                float wt = w[0][i] * w[1][j] * w[2][k];
-                float dpos[3] = {((float)i - fx[0]) * g.dx, ((float)j - fx[1]) * g.dx, ((float)k - fx[2]) * g.dx};
-                float4 gv = src(base[0] + i, base[1] + j, base[2] + k);
-                float gva[3] = {gv.x, gv.y, gv.z};
-                float cw = cscale * wt;
+                for (int k = 0; k < 3; ++k) {
+                    const float4 gv = src(at(i, j, k));
+                    const float gva[3] = {gv.x, gv.y, gv.z};
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        R[a] = fmaf(w[2][k], gva[a], R[a]);
+                        if (k) Rk[a] = fmaf((float)k * w[2][k], gva[a], Rk[a]);
+                    }
+                }
 #pragma unroll
                 for (int a = 0; a < 3; ++a) {
-                    nv[a] += wt * gva[a];
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) nC[a][c] += cw * (gva[a] * dpos[c]);
+                    Q[a] = fmaf(w[1][j], R[a], Q[a]);
+                    if (j) Qj[a] = fmaf((float)j * w[1][j], R[a], Qj[a]);
+                    Qk[a] = fmaf(w[1][j], Rk[a], Qk[a]);
                 }
             }
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                nv[a] = fmaf(w[0][i], Q[a], nv[a]);
+                if (i) S[a][0] = fmaf((float)i * w[0][i], Q[a], S[a][0]);
+                S[a][1] = fmaf(w[0][i], Qj[a], S[a][1]);
+                S[a][2] = fmaf(w[0][i], Qk[a], S[a][2]);
+            }
+        }
+    }
+    const float cscale = 4.0f * g.inv_dx * g.inv_dx * g.dx;
+    float nC[3][3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) nC[a][c] = cscale * (S[a][c] - fx[c] * nv[a]);
     float nx[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
@@ -540,7 +594,7 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
 struct GlobalSource {
     const GridDesc* g;
     const float4* grid;
-    MPM_HD float4 operator()(int i, int j, int k) const { return load_node(&grid[node_index(*g, i, j, k)]); }
+    MPM_HD float4 operator()(int64_t node) const { return load_node(&grid[node]); }
 };
 
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,

@@ -7,6 +7,8 @@
 // (warp/solver.py:187-212 for the order).
 #pragma once
 
+#include <climits>
+
 #include "mpm_substep.cuh"
 
 namespace mpm {
@@ -160,7 +162,7 @@ __device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTe
     for (int n = 0; n < 27; ++n) {
         const int i = n / 9, j = (n / 3) % 3, k = n % 3;
         float val[4] = {0.f, 0.f, 0.f, 0.f};
-        if (valid) p2g_node(t, g, i, j, k, val);
+        if (valid) p2g_node(t, i, j, k, val);
         long long q[4];
         bool bad = false;
 #pragma unroll
@@ -217,20 +219,9 @@ __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
 // reduction per node instead of eight. Runs are also cut at aligned groups of p2g_group lanes: fewer shuffle
 // rounds for more reductions (the autotuner picks the group). Lanes past the end or with a stencil outside
 // the grid are single-lane segments that add nothing. The segment's first lane lists the blocks it touches.
-template <class Scenes>
-__global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
-    pdl_begin();
-    const int s = sc.scene_of_cta(blockIdx.x);
-    const SubstepArgs a = sc.get(s);
-    if (!sc.active(a)) return;
-    const int64_t first = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x;
-    const int64_t p = first + threadIdx.x;
+__device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, const P2gTerms& t, bool valid) {
     const int lane = (int)(threadIdx.x & 31u);
-    if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end
     const GridDesc& g = a.g;
-    const Particles P = particles_of(a);
-    P2gTerms t;
-    const bool valid = p < a.n && p2g_terms(P, p, a.mats, g, a.sp->dt, t);
     const int64_t key = valid ? node_index(g, t.base[0], t.base[1], t.base[2]) : -1 - (int64_t)lane;
     const int64_t key_prev = __shfl_up_sync(0xffffffffu, key, 1);
     const int64_t key_next = __shfl_down_sync(0xffffffffu, key, 1);
@@ -256,7 +247,7 @@ __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 float val[4] = {0.f, 0.f, 0.f, 0.f};
-                if (valid) p2g_node(t, g, i, j, k, val);
+                if (valid) p2g_node(t, i, j, k, val);
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
                     if (d <= span) {  // warp-uniform
@@ -271,6 +262,120 @@ __global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
                     grid_add(&a.grid[node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k)], val[0], val[1],
                              val[2], val[3]);
             }
+}
+
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
+    pdl_begin();
+    const int s = sc.scene_of_cta(blockIdx.x);
+    const SubstepArgs a = sc.get(s);
+    if (!sc.active(a)) return;
+    const int64_t first = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x;
+    const int64_t p = first + threadIdx.x;
+    if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end
+    const Particles P = particles_of(a);
+    P2gTerms t;
+    const bool valid = p < a.n && p2g_terms(P, p, a.mats, a.g, a.sp->dt, t);
+    p2g_warp_segments(a, t, valid);
+}
+
+// P2G through shared-memory tiles. The CTA's 256 particles (a contiguous range of the particle order) are
+// taken with a stride of 8 inside the range (lane l of warp w takes particle 8 l + w), so the lanes of a warp
+// sit in different cells whether the order is by cell (about 8 particles per cell) or the sampler's lattice
+// order. The CTA's stencils are bounded by a box of nodes; when it holds at most kP2gTileNodes nodes, each
+// warp adds its lanes' contributions into its own copy of the box with plain shared-memory read-add-writes
+// (no atomics): at one stencil offset, lanes with different stencil bases write different nodes, and lanes
+// that share a base take turns (rounds by their rank among the lanes with that base), with __syncwarp
+// ordering each step. The warps' copies are then summed per node and every node that received anything is
+// added to the grid with one 16-byte reduction (its grid block listed): a few reductions per box node
+// instead of ~4.7 per particle, and no shuffle sums. A CTA whose box is larger (scattered particles) or a
+// deterministic-mode scene takes the warp-segment path.
+constexpr int kP2gTileNodes = 432;  // per warp: 8 copies x 432 nodes x 16 B = 55,296 B of shared memory
+constexpr size_t kP2gTileBytes = (size_t)8 * kP2gTileNodes * sizeof(float4);
+
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_p2g_tile(Scenes sc) {
+    pdl_begin();
+    extern __shared__ float4 tiles[];  // 8 warp copies of the box, node-major, `nodes` apart
+    __shared__ int box[6];             // min x, y, z and max x, y, z of the stencil bases
+    const int s = sc.scene_of_cta(blockIdx.x);
+    const SubstepArgs a = sc.get(s);
+    if (!sc.active(a)) return;
+    const int64_t first = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x;
+    if (first >= a.n) return;  // CTA-uniform
+    const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t p = first + lane * 8 + warp;
+    const GridDesc& g = a.g;
+    const Particles P = particles_of(a);
+    P2gTerms t;
+    const bool valid = p < a.n && p2g_terms(P, p, a.mats, g, a.sp->dt, t);
+    if (tid < 6) box[tid] = tid < 3 ? INT_MAX : INT_MIN;
+    __syncthreads();
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int lo = __reduce_min_sync(0xffffffffu, valid ? t.base[d] : INT_MAX);
+        const int hi = __reduce_max_sync(0xffffffffu, valid ? t.base[d] : INT_MIN);
+        if (lane == 0 && lo <= hi) {
+            atomicMin(&box[d], lo);
+            atomicMax(&box[3 + d], hi);
+        }
+    }
+    __syncthreads();
+    const int lo0 = box[0], lo1 = box[1], lo2 = box[2];
+    if (lo0 > box[3]) return;  // no particle of the CTA scatters (CTA-uniform)
+    const int e1 = box[4] - lo1 + 3, e2 = box[5] - lo2 + 3;
+    const int nodes = (box[3] - lo0 + 3) * e1 * e2;
+    if (a.fixed || nodes > kP2gTileNodes) {  // CTA-uniform
+        p2g_warp_segments(a, t, valid);
+        return;
+    }
+    for (int q = tid; q < 8 * nodes; q += 256) tiles[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int o = valid ? ((t.base[0] - lo0) * e1 + (t.base[1] - lo1)) * e2 + (t.base[2] - lo2) : 0;
+    const unsigned int peers = __match_any_sync(0xffffffffu, valid ? o : -1 - lane);
+    const int rank = __popc(peers & ((1u << lane) - 1u));  // lanes before this one with the same base
+    const int rounds = (int)__reduce_max_sync(0xffffffffu, (unsigned int)rank) + 1;
+    float4* mine = tiles + warp * nodes;
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float val[4] = {0.f, 0.f, 0.f, 0.f};
+                if (valid) p2g_node(t, i, j, k, val);
+                float4* cell = mine + o + (i * e1 + j) * e2 + k;
+                for (int r = 0; r < rounds; ++r) {  // warp-uniform; one round unless lanes share a base
+                    if (valid && rank == r) {
+                        float4 c = *cell;
+                        c.x += val[0];
+                        c.y += val[1];
+                        c.z += val[2];
+                        c.w += val[3];
+                        *cell = c;
+                    }
+                    __syncwarp();
+                }
+            }
+    __syncthreads();
+    const unsigned int cur = a.sp->seq & 1u;
+    for (int q = tid; q < nodes; q += 256) {
+        float4 v = tiles[q];
+#pragma unroll
+        for (int w = 1; w < 8; ++w) {
+            const float4 u = tiles[w * nodes + q];
+            v.x += u.x;
+            v.y += u.y;
+            v.z += u.z;
+            v.w += u.w;
+        }
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {  // true for NaN too
+            const int qk = q % e2, qij = q / e2;
+            const int64_t node = node_index(g, lo0 + qij / e1, lo1 + qij % e1, lo2 + qk);
+            grid_add(&a.grid[node], v.x, v.y, v.z, v.w);
+            mark_block(node >> 6, a.wl.block_flag, active_blocks(a.wl, cur), &a.wl.counts[cur]);
+        }
+    }
 }
 
 // Grid update (normalise, gravity, walls) over the active blocks, four 4x4x4 blocks per 256-thread CTA;

@@ -6,7 +6,8 @@ Knobs (C options of include/mpm_gb300.h):
   g2p_variant        G2P build: 0 capped at 80 registers (3 CTAs of 256 per SM), 1 uncapped;
   list_ctas_per_sm   CTAs per SM of the kernels that walk the active-block and candidate lists;
   p2g_group          P2G sums same-cell lanes within aligned groups of this many lanes (1 .. 32);
-  pdl                programmatic dependent launch of the substep kernels (1) or plain stream order (0).
+  pdl                programmatic dependent launch of the substep kernels (1) or plain stream order (0);
+  p2g_tile           P2G through a shared-memory tile per CTA (1) or warp segments only (0).
 
 Search: coordinate descent from the defaults, one knob at a time over its candidates with the others fixed,
 keeping a change only when it is at least 2 % faster. A configuration is timed by the CUDA events the
@@ -28,10 +29,10 @@ from pathlib import Path
 
 from mpm_plugin_gb300 import _abi
 
-DEFAULTS = {"sort_interval": 4, "g2p_variant": 0, "list_ctas_per_sm": 8, "p2g_group": 32, "pdl": 1}
+DEFAULTS = {"sort_interval": 4, "g2p_variant": 0, "list_ctas_per_sm": 8, "p2g_group": 32, "pdl": 1, "p2g_tile": 0}
 CANDIDATES = {"sort_interval": (0, 2, 4, 8, 16), "g2p_variant": (0, 1), "list_ctas_per_sm": (4, 8, 16),
-              "p2g_group": (1, 4, 8, 32), "pdl": (0, 1)}
-KNOB_ORDER = ("g2p_variant", "sort_interval", "p2g_group", "list_ctas_per_sm", "pdl")
+              "p2g_group": (1, 4, 8, 32), "pdl": (0, 1), "p2g_tile": (0, 1)}
+KNOB_ORDER = ("g2p_variant", "p2g_tile", "sort_interval", "p2g_group", "list_ctas_per_sm", "pdl")
 MIN_GAIN = 0.02
 
 
@@ -76,6 +77,7 @@ def apply(target, cfg: dict, sms: int) -> None:
     target.set_option(_abi.OPT_LIST_CTAS, int(cfg["list_ctas_per_sm"]) * sms)
     target.set_option(_abi.OPT_P2G_GROUP, int(cfg.get("p2g_group", 32)))
     target.set_option(_abi.OPT_PDL, int(cfg.get("pdl", 1)))
+    target.set_option(_abi.OPT_P2G_TILE, int(cfg.get("p2g_tile", 0)))
 
 
 def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, min_gain=MIN_GAIN):
