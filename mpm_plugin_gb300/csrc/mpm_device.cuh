@@ -72,15 +72,32 @@ MPM_HD double rsqrt_t<double>(double x) { return 1.0 / sqrt(x); }
 template <typename T>
 MPM_HD T sqrt_t(T x) { return sqrt(x); }
 
+// Quotient and square root inside a Jacobi rotation. The rotation stays orthogonal whatever the rounding of
+// its angle (c = 1 / sqrt(1 + t^2), s = t c), so FP32 takes the hardware approximations (2 ulp) there;
+// FP64 keeps IEEE operations.
+template <typename T>
+MPM_HD T rot_div(T a, T b) { return a / b; }
+template <typename T>
+MPM_HD T rot_sqrt(T x) { return sqrt_t(x); }  // x >= 1
+#ifdef __CUDA_ARCH__
+template <>
+MPM_HD float rot_div<float>(float a, float b) { return __fdividef(a, b); }
+template <>
+MPM_HD float rot_sqrt<float>(float x) { return x * rsqrtf(x); }
+#endif
+
 template <typename T>
 MPM_HD void jacobi_rotate(T S[3][3], T V[3][3], int p, int q) {
     const int r = 3 - p - q;
     T apq = S[p][q];
-    if (apq == T(0)) return;
-    T zeta = (S[q][q] - S[p][p]) / (T(2) * apq);
+    // an off-diagonal this small is already negligible against the 4e-6 convergence bound (and would
+    // overflow the quotient); NaN passes on to the convergence check
+    if (fabs(apq) < T(1e-30)) return;
+    T zeta = rot_div<T>(S[q][q] - S[p][p], T(2) * apq);
     T az = fabs(zeta);
     // t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)); for huge |zeta| the square would overflow, t -> 1/(2 zeta)
-    T t = az > T(1e18) ? T(0.5) / zeta : copysign(T(1), zeta) / (az + sqrt_t(T(1) + zeta * zeta));
+    T t = az > T(1e18) ? rot_div<T>(T(0.5), zeta)
+                       : rot_div<T>(copysign(T(1), zeta), az + rot_sqrt<T>(T(1) + zeta * zeta));
     T c = rsqrt_t(T(1) + t * t);
     T s = t * c;
     S[p][p] -= t * apq;

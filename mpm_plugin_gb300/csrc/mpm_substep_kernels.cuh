@@ -212,6 +212,33 @@ __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
     }
 }
 
+// The 27 x 4 contributions of each lane summed over its segment in kRounds shuffle rounds (after round r a
+// lane holds the sum of the next 2^r lanes of its segment); the segment's first lane adds each node's sums to
+// the grid. kRounds is fixed per warp, so the rounds carry no per-node branches.
+template <int kRounds>
+__device__ __forceinline__ void p2g_segment_sums(const SubstepArgs& a, const P2gTerms& t, bool valid, bool leader,
+                                                 int tail, const StencilIndex& at) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float val[4] = {0.f, 0.f, 0.f, 0.f};
+                if (valid) p2g_node(t, i, j, k, val);
+#pragma unroll
+                for (int r = 0; r < kRounds; ++r) {
+                    const int d = 1 << r;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float o = __shfl_down_sync(0xffffffffu, val[c], d);
+                        if (d <= tail) val[c] += o;
+                    }
+                }
+                if (leader) grid_add(&a.grid[at(i, j, k)], val[0], val[1], val[2], val[3]);
+            }
+}
+
 // P2G with warp-level aggregation: lanes whose stencils start at the same grid node (neighbours in the
 // particle order after the reorder by grid node) form a segment; each of the 27 x 4 contributions is summed
 // over the segment with shuffles (after round r a lane holds the sum of the next 2^r lanes of its segment)
@@ -240,28 +267,19 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, const P2
         p2g_fixed_warp(a, t, valid, leader, tail, span);
         return;
     }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                float val[4] = {0.f, 0.f, 0.f, 0.f};
-                if (valid) p2g_node(t, i, j, k, val);
-#pragma unroll
-                for (int d = 1; d < 32; d <<= 1) {
-                    if (d <= span) {  // warp-uniform
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            const float o = __shfl_down_sync(0xffffffffu, val[c], d);
-                            if (d <= tail) val[c] += o;
-                        }
-                    }
-                }
-                if (leader)
-                    grid_add(&a.grid[node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k)], val[0], val[1],
-                             val[2], val[3]);
-            }
+    const StencilIndex at = stencil_index(g, t.base);
+    // shuffle rounds needed by the longest segment of the warp: 0, 1, 2, 3 or 5 (4 takes 5)
+    const int rounds = span == 0 ? 0 : 32 - __clz(span);
+    if (rounds == 0)
+        p2g_segment_sums<0>(a, t, valid, leader, tail, at);
+    else if (rounds == 1)
+        p2g_segment_sums<1>(a, t, valid, leader, tail, at);
+    else if (rounds == 2)
+        p2g_segment_sums<2>(a, t, valid, leader, tail, at);
+    else if (rounds == 3)
+        p2g_segment_sums<3>(a, t, valid, leader, tail, at);
+    else
+        p2g_segment_sums<5>(a, t, valid, leader, tail, at);
 }
 
 template <class Scenes>
@@ -485,8 +503,9 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
 
 // G2P; particles that end inside a collider's margin box are listed for k_project_particles. kMinCtas = 3
 // caps it at 80 registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra
-// resident warps outweighed the few spilled values on the mixed workload (10 % faster than kMinCtas = 1,
-// 120 registers). Both are built; the autotuner picks one per workload.
+// resident warps outweighed the few spilled values on the mixed workload (10 % faster than kMinCtas = 1).
+// Caps of 128 and 64 registers were slower on the mixed and the 256^3 workloads (measured on a GB300). Both
+// builds are kept; the autotuner picks one per workload.
 template <class Scenes, int kMinCtas>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     pdl_begin();

@@ -41,13 +41,15 @@ def test_tune_solver_restores_state_and_caches(tmp_path):
     assert rel_err(s.save_state()["x"], ref.save_state()["x"]) <= 1e-4
 
 
-@pytest.mark.parametrize("variant,ctas_per_sm,group,pdl", [(0, 4, 1, 0), (1, 16, 4, 1), (1, 8, 32, 0), (0, 16, 8, 1)])
-def test_every_launch_choice_gives_the_same_physics(variant, ctas_per_sm, group, pdl):
+@pytest.mark.parametrize("variant,ctas_per_sm,group,pdl,tile", [(0, 4, 1, 0, 0), (1, 16, 4, 1, 0), (1, 8, 32, 0, 1),
+                                                              (0, 16, 8, 1, 1), (0, 8, 32, 1, 0), (1, 4, 8, 0, 1)])
+def test_every_launch_choice_gives_the_same_physics(variant, ctas_per_sm, group, pdl, tile):
     from mpm_plugin_gb300 import _abi
 
     s, ref = _solver(), _solver()
     ref.set_option(_abi.OPT_PDL, 0)
     s.set_option(_abi.OPT_PDL, pdl)
+    s.set_option(_abi.OPT_P2G_TILE, tile)
     s.set_option(_abi.OPT_G2P_VARIANT, variant)
     s.set_option(_abi.OPT_LIST_CTAS, ctas_per_sm * 152)
     s.set_option(_abi.OPT_P2G_GROUP, group)
