@@ -356,7 +356,7 @@ def run_large(device: str, frames: int) -> dict:
     s.add_particles(pile, np.zeros_like(pile), np.zeros(len(pile), np.int32), np.zeros(len(pile), np.int32))
     s.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
     s.set_collider_transforms(pose(0.0)[None], pose(0.0)[None])
-    tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=6)
+    tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=12)
     n0 = s.particle_count
     c0 = s.conservation()
     t_adv = t_emit = t_read = 0.0
@@ -582,7 +582,7 @@ def run_gpu(args, world, rank, local):
 
     from mpm_plugin_gb300 import tune
 
-    tuned = tune.tune_solver(solver, DT, FRAME_DT, substeps=10)  # launch choices for this GPU and workload
+    tuned = tune.tune_solver(solver, DT, FRAME_DT, substeps=50)  # launch choices for this GPU and workload
     for _ in range(args.warmup):
         solver.substep(DT, 1.0, FRAME_DT)
     solver.synchronize()
@@ -629,7 +629,7 @@ def run_gpu(args, world, rank, local):
     fp64_lanes = solver.fp64_lanes()
     solver.close()
     solver, xf = make_gpu_solver(device)
-    tune.tune_solver(solver, DT, FRAME_DT, substeps=10)  # the cached choice
+    tune.tune_solver(solver, DT, FRAME_DT, substeps=50)  # the cached choice
     e2e_frames, frame_ms, substeps = max(2, args.e2e_frames), [], 0
     h2d = 2 * 64  # the collider's start and end world matrices
     d2h = n * (12 + 12 + 36 + 36 + 4 + 4 + 4)  # the full state (x v C F Jp mat emitter) covers get_particles too

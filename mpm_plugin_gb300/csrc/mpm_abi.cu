@@ -1071,6 +1071,7 @@ struct Batch {
     int64_t cta_cap = 0;
     unsigned int particle_ctas = 0;
     bool any_colliders = false;
+    bool any_fp64_clamp = false;
     std::vector<int64_t> layout;             // what the captured graphs depend on
     cudaGraphExec_t graph = nullptr;         // one batched substep
     cudaGraphExec_t graph_many = nullptr;    // kGraphReps batched substeps
@@ -1115,7 +1116,7 @@ Status batch_upload(Batch* b) {
     std::vector<SubstepArgs> table(n);
     std::vector<int64_t> layout{n};
     int64_t ctas = 0;
-    bool cols = false;
+    bool cols = false, clamp = false;
     for (int s = 0; s < n; ++s) {
         Handle* h = b->live[s];
         table[s] = substep_args(h);
@@ -1123,8 +1124,10 @@ Status batch_upload(Batch* b) {
         layout.push_back(h->P.cap);
         ctas += (h->P.cap + 255) / 256;
         cols = cols || h->n_col > 0;
+        clamp = clamp || h->fp64_clamp;
     }
     layout.push_back(cols ? 1 : 0);
+    layout.push_back(clamp ? 1 : 0);
     if (layout != b->layout) {
         CK(cudaStreamSynchronize(b->stream));
         batch_invalidate(b);
@@ -1145,6 +1148,7 @@ Status batch_upload(Batch* b) {
         CK(cudaMemcpyAsync(b->d_cta, cta.data(), sizeof(int32_t) * cta.size(), cudaMemcpyHostToDevice, b->stream));
         b->particle_ctas = (unsigned int)ctas;
         b->any_colliders = cols;
+        b->any_fp64_clamp = clamp;
         b->layout = layout;
     }
     // a pageable source is staged by the driver before the call returns, so `table` may go out of scope
@@ -1155,7 +1159,7 @@ Status batch_upload(Batch* b) {
 // reps (1 or kGraphReps) batched substeps in one graph launch.
 Status batch_replay(Batch* b, int reps = 1) {
     BatchLaunch bl{b->d_table, b->d_cta, b->d_cta + b->particle_ctas, (int)b->live.size(), b->particle_ctas,
-                   b->any_colliders, b->shape};
+                   b->any_colliders, b->any_fp64_clamp, b->shape};
     cudaGraphExec_t& g = reps == 1 ? b->graph : b->graph_many;
     if (!g) {
         cudaGraph_t graph;

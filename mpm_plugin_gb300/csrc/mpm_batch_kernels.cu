@@ -22,7 +22,9 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
     launch_step_kernel(k_grid_update<SceneTable>, list_ctas, 256, st, pdl, sc);
     if (b.any_colliders) launch_step_kernel(k_grid_colliders<SceneTable>, list_ctas, 128, st, pdl, sc);
     if (b.particle_ctas > 0) {
-        if (b.shape.g2p_variant == 1)
+        if (b.any_fp64_clamp)
+            launch_step_kernel(k_g2p<SceneTable, 1, true>, b.particle_ctas, 256, st, pdl, sc);
+        else if (b.shape.g2p_variant == 1)
             launch_step_kernel(k_g2p<SceneTable, 1>, b.particle_ctas, 256, st, pdl, sc);
         else
             launch_step_kernel(k_g2p<SceneTable, 3>, b.particle_ctas, 256, st, pdl, sc);

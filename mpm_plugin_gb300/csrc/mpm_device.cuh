@@ -11,11 +11,6 @@
 
 // The math below also compiles for the host (tests check the SVD's accuracy on the CPU).
 #define MPM_HD __host__ __device__ __forceinline__
-#ifdef __CUDACC__
-#define MPM_HD_NOINLINE __host__ __device__ __noinline__
-#else
-#define MPM_HD_NOINLINE __attribute__((noinline))
-#endif
 
 namespace mpm {
 

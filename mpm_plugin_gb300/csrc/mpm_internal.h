@@ -75,6 +75,7 @@ struct BatchLaunch {
     int n_scenes;
     unsigned int particle_ctas;
     bool any_colliders;
+    bool any_fp64_clamp;  // some scene redoes the plastic clamp in FP64 (the G2P build with the redo)
     LaunchShape shape;
 };
 void launch_batch_substep(cudaStream_t st, const BatchLaunch& b);

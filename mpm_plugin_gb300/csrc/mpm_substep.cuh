@@ -397,9 +397,10 @@ MPM_HD float4 load_node(const float4* p) {
 // return mapping at the clamp in double precision): the trial F rebuilt in FP64 from the stored F and the
 // new C (both still in memory), then the SVD (eight double sweeps), the return mapping, the projected F, the
 // snow hardening and the stress in FP64, rounded to FP32 only when stored.
-// Kept out of line so that the FP32 path's register allocation does not carry the FP64 working set.
-static MPM_HD_NOINLINE void plastic_redo_fp64(const Particles& P, int64_t p, const Material& m, float dt, float jp_old,
-                                              float Fn_out[3][3], float* jp_out, float t_out[6]) {
+// Only the G2P build for the option contains it, so the default build's registers never carry the FP64
+// working set (an out-of-line call in the one build made the default G2P 28 % slower, measured).
+MPM_HD void plastic_redo_fp64(const Particles& P, int64_t p, const Material& m, float dt, float jp_old,
+                              float Fn_out[3][3], float* jp_out, float t_out[6]) {
     float F[3][3], C[3][3];
     load_mat3(P.F, p, F);
     load_mat3(P.C, p, C);
@@ -456,8 +457,9 @@ static MPM_HD_NOINLINE void plastic_redo_fp64(const Particles& P, int64_t p, con
 }
 
 // G2P of one particle gathering node velocities from `src` (src(node index) -> float4); the new position goes
-// to nx_out.
-template <class Source>
+// to nx_out. kFp64Clamp builds in the FP64 redo at an active Drucker-Prager or snow clamp, taken where
+// fp64_clamp is set.
+template <class Source, bool kFp64Clamp = false>
 MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
                               float dt, const Source& src, unsigned int* fp64, float nx_out[3],
                               bool fp64_clamp = false) {
@@ -559,7 +561,7 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
             moved = project_snow(sig, d, m.clamp_lo, m.clamp_hi, delta, &ratio);
             jp = jp * ratio;
         }
-        redo = fp64_clamp && moved && m.model >= 2;
+        redo = kFp64Clamp && fp64_clamp && moved && m.model >= 2;
         if (moved) {  // F = U diag(new) V^T, applied as F + U diag(new - old) V^T
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -574,10 +576,14 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
         }
     }
     float t[6];
-    if (redo)
-        plastic_redo_fp64(P, p, m, dt, jp_old, Fn, &jp, t);  // reads F and C before F is overwritten
-    else
+    if constexpr (kFp64Clamp) {
+        if (redo)
+            plastic_redo_fp64(P, p, m, dt, jp_old, Fn, &jp, t);  // reads F and C before F is overwritten
+        else
+            tau_from_svd(m, jp, U, sig, d, t);
+    } else {
         tau_from_svd(m, jp, U, sig, d, t);
+    }
     store_mat3(P.F, p, Fn);
     if (m.model == 3) P.Jp[p] = jp;
 #pragma unroll
@@ -597,10 +603,11 @@ struct GlobalSource {
     MPM_HD float4 operator()(int64_t node) const { return load_node(&grid[node]); }
 };
 
+template <bool kFp64Clamp = false>
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
                          const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false) {
     GlobalSource src{&g, grid};
-    g2p_particle_from(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp);
+    g2p_particle_from<GlobalSource, kFp64Clamp>(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

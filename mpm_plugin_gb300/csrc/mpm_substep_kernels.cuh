@@ -505,8 +505,9 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
 // caps it at 80 registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra
 // resident warps outweighed the few spilled values on the mixed workload (10 % faster than kMinCtas = 1).
 // Caps of 128 and 64 registers were slower on the mixed and the 256^3 workloads (measured on a GB300). Both
-// builds are kept; the autotuner picks one per workload.
-template <class Scenes, int kMinCtas>
+// builds are kept; the autotuner picks one per workload. kFp64Clamp: the build with the FP64 redo at the
+// Drucker-Prager and snow clamp (MPM_OPT_FP64_CLAMP), launched only when a scene has the option set.
+template <class Scenes, int kMinCtas, bool kFp64Clamp = false>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     pdl_begin();
     const int s = sc.scene_of_cta(blockIdx.x);
@@ -515,7 +516,7 @@ __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     const int64_t p = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x + threadIdx.x;
     if (p >= a.n) return;
     float nx[3];
-    g2p_particle(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx, a.fp64_clamp != 0);
+    g2p_particle<kFp64Clamp>(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx, a.fp64_clamp != 0);
     if (a.cd.n_col > 0) {
         ColliderData cd = a.cd;
         cd.poses += a.sp->pose_base;
