@@ -224,7 +224,8 @@ void invalidate_graph(Handle* h) {
 
 Status ensure_capacity(Handle* h, int64_t need) {
     if (need <= h->P.cap) return {};
-    int64_t cap = std::max<int64_t>({need, 2 * h->P.cap, 4096});
+    // a multiple of 256 entries: every plane starts 1 KB-aligned
+    int64_t cap = (std::max<int64_t>({need, 2 * h->P.cap, 4096}) + 255) / 256 * 256;
     void* fresh = nullptr;
     if (cudaMalloc(&fresh, (size_t)cap * kFields * 4) != cudaSuccess) {
         cudaGetLastError();

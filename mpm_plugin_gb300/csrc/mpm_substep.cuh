@@ -118,6 +118,15 @@ MPM_HD void store_mat3(float* const* dst, int64_t p, const float M[3][3]) {
         for (int j = 0; j < 3; ++j) dst[i * 3 + j][p] = M[i][j];
 }
 
+// Asks for the line holding *addr in L1 without waiting for it (a hint: no register, no fault on any address).
+MPM_HD void prefetch_l1(const void* addr) {
+#ifdef __CUDA_ARCH__
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(addr));
+#else
+    (void)addr;
+#endif
+}
+
 // Adds grid block b to the active list of this substep unless it is there already.
 MPM_HD void mark_block(int64_t b, unsigned int* __restrict__ flags, int32_t* __restrict__ list,
                        unsigned int* __restrict__ count) {
@@ -200,29 +209,44 @@ struct P2gTerms {
     float w[3][3], u0[3], dA[3][3], pm;
 };
 
+// The fields P2G reads, straight from the particle arrays (GlobalFields) or from a CTA's staged copy.
+struct GlobalFields {
+    const Particles& P;
+    int64_t p;
+    MPM_HD float x(int a) const { return P.x[a][p]; }
+    MPM_HD float v(int a) const { return P.v[a][p]; }
+    MPM_HD float C(int e) const { return P.C[e][p]; }
+    MPM_HD float tau(int e) const { return P.tau[e][p]; }
+    MPM_HD int mat() const { return P.mat[p]; }
+};
+
 // False when the stencil leaves the grid (the particle scatters nothing).
-MPM_HD bool p2g_terms(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                      P2gTerms& t) {
-    const float t0 = P.tau[0][p], t1 = P.tau[1][p], t2 = P.tau[2][p], t3 = P.tau[3][p], t4 = P.tau[4][p],
-                t5 = P.tau[5][p];
+template <class Fields>
+MPM_HD bool p2g_terms_of(const Fields& f, const Material* __restrict__ mats, const GridDesc& g, float dt, P2gTerms& t) {
+    const float t0 = f.tau(0), t1 = f.tau(1), t2 = f.tau(2), t3 = f.tau(3), t4 = f.tau(4), t5 = f.tau(5);
     const float tau[3][3] = {{t0, t3, t4}, {t3, t1, t5}, {t4, t5, t2}};
-    t.pm = mats[P.mat[p]].p_mass;
+    t.pm = mats[f.mat()].p_mass;
     const float k_stress = -dt * g.p_vol * 4.0f * g.inv_dx * g.inv_dx;
     bool inside = true;
     float fx[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float xp = (P.x[a][p] - g.origin[a]) * g.inv_dx;
+        float xp = (f.x(a) - g.origin[a]) * g.inv_dx;
         inside &= stencil_axis(xp, g.dims[a], &t.base[a], &fx[a]);
         bspline_weights(fx[a], t.w[a]);
     }
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
 #pragma unroll
-        for (int j = 0; j < 3; ++j) t.dA[i][j] = (k_stress * tau[i][j] + t.pm * P.C[i * 3 + j][p]) * g.dx;
-        t.u0[i] = t.pm * P.v[i][p] - (t.dA[i][0] * fx[0] + t.dA[i][1] * fx[1] + t.dA[i][2] * fx[2]);
+        for (int j = 0; j < 3; ++j) t.dA[i][j] = (k_stress * tau[i][j] + t.pm * f.C(i * 3 + j)) * g.dx;
+        t.u0[i] = t.pm * f.v(i) - (t.dA[i][0] * fx[0] + t.dA[i][1] * fx[1] + t.dA[i][2] * fx[2]);
     }
     return inside;
+}
+
+MPM_HD bool p2g_terms(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
+                      P2gTerms& t) {
+    return p2g_terms_of(GlobalFields{P, p}, mats, g, dt, t);
 }
 
 // Momentum (x, y, z) and mass the particle adds to stencil node (i, j, k), i, j, k in 0..2. In unrolled
@@ -463,6 +487,12 @@ template <class Source, bool kFp64Clamp = false>
 MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
                               float dt, const Source& src, unsigned int* fp64, float nx_out[3],
                               bool fp64_clamp = false) {
+    // F, Jp and mat are read after the gather and the C store; their lines are requested now so that the
+    // memory latency overlaps the gather
+#pragma unroll
+    for (int e = 0; e < 9; ++e) prefetch_l1(&P.F[e][p]);
+    prefetch_l1(&P.Jp[p]);
+    prefetch_l1(&P.mat[p]);
     float xo[3];
     int base[3];
     float fx[3], w[3][3];
