@@ -64,6 +64,8 @@ class Gb300Batch:
         if n == 0:
             return []
         fdt = np.broadcast_to(np.asarray(frame_dt, np.float64), (n,)).copy()
+        for s in self._scenes:
+            s._mutated()
         stats = (_abi.MpmAdvanceStats * n)()
         self._check(self._lib.mpm_batch_advance(self._b, fdt.ctypes.data_as(C.c_void_p), stats))
         return [AdvanceStats(int(st.substeps), float(st.dt), int(st.removed)) for st in stats]

@@ -213,6 +213,37 @@ def test_state_roundtrip_and_order():
         np.testing.assert_array_equal(s2[k], p2[k])
 
 
+def test_frame_reads_share_one_state_read():
+    """frame_reads (the bake entry point's solvers): get_particles reads the whole state and the save_state
+    right after it returns that read; any advance in between makes save_state read afresh."""
+    from mpm_plugin_gb300.solver import Gb300Solver
+
+    d = domain(res=32)
+    pos = box_particles((0.4, 0.4, 0.3), (0.6, 0.6, 0.5), d.dx)
+    a = Gb300Solver(d, [preset("jelly")], (0.0, 0.0, -9.81), 8, device="cuda:0", frame_reads=True)
+    b = gpu_solver(d, [preset("jelly")])
+    for s in (a, b):
+        add(s, pos)
+        s.advance(1 / 96)
+    pa, pb = a.get_particles(), b.get_particles()
+    fresh = a._save_state()
+    for u, w, k in ((pa.positions, pb.positions, "x"), (pa.velocities, pb.velocities, "v"),
+                    (pa.material_ids, pb.material_ids, "mat"), (pa.emitter_ids, pb.emitter_ids, "emitter")):
+        assert u.dtype == w.dtype and u.shape == w.shape
+        np.testing.assert_array_equal(u, fresh[k])
+    sa = a.save_state()
+    assert sa["x"] is pa.positions  # the same read
+    for k in fresh:
+        np.testing.assert_array_equal(sa[k], fresh[k])
+    a.get_particles()
+    a.advance(1 / 96)
+    sa = a.save_state()
+    assert np.abs(sa["x"] - pa.positions).max() > 0  # not the kept read
+    fresh = a._save_state()
+    for k in fresh:
+        np.testing.assert_array_equal(sa[k], fresh[k])
+
+
 @pytest.mark.parametrize("res", [64, 160])
 def test_reorder_keeps_every_particle(res):
     """The reorder by grid node after every substep (counting sort over all grid nodes, 1,158 scan tiles at
