@@ -231,6 +231,32 @@ int mpm_volume_lattice(const double *tri, int64_t n_tris, const double *xs, int3
                        const double *zs, int32_t nz, double spacing, const double nudge[2], int64_t first_x,
                        int64_t first_y, int32_t device, double *out, int64_t capacity, int64_t *n_out);
 
+/* ---- Surfacing (replaces the GPU part of mpm_surface/field.py:35-142, surface_particles) ----------------
+ * A surfacer owns a stream and the device buffers of its last build. mpm_surface_build splats the n
+ * particles (x, v: (n, 3) float32 host arrays) onto a dims[0] x dims[1] x dims[2] node grid at `origin`
+ * (float32, the field.py origin rounded) with spacing `cell` (inv_cell = the host's 1 / cell rounded to
+ * float32): cubic B-spline kernel of radius h, density and momentum summed (field.py:35-57); velocity =
+ * momentum / density where density > 0, density scaled by inv_rest (field.py:60-66); then marching cubes at
+ * `iso` (a node is inside when its density is above iso; the case table is built from the cube's geometry,
+ * mpm_mc_table), one vertex per crossing grid edge in node order then axis order, triangles in cell order,
+ * wound outward; each vertex's velocity sampled trilinearly (field.py:69-89). n_verts and n_tris receive the
+ * counts; mpm_surface_read copies verts ((n_verts, 3) float32 in grid index units), tris ((n_tris, 3) int32)
+ * and vel ((n_verts, 3) float32) to host memory. Errors: mpm_surface_last_error(surfacer). */
+int mpm_surface_create(int32_t device, void **surfacer);
+int mpm_surface_destroy(void *surfacer);
+const char *mpm_surface_last_error(void *surfacer);
+int mpm_surface_build(void *surfacer, int64_t n, const float *x, const float *v, const float origin[3],
+                      const int32_t dims[3], float cell, float inv_cell, float h, float inv_rest, float iso,
+                      int64_t *n_verts, int64_t *n_tris);
+int mpm_surface_read(void *surfacer, float *verts, int32_t *tris, float *vel);
+/* The last build's fields, for checking: density (dims, float32, normalised) and field (dims x 4 float32:
+ * velocity xyz where the raw density is positive, else the zero momentum, and the raw density). */
+int mpm_surface_read_field(void *surfacer, float *density, float *field);
+/* The marching-cubes case table the surfacer uses (host only): ntri[256] triangle counts, edges[256 * 36]
+ * edge ids (triangle t of case m at edges[m * 36 + 3 t .. + 2]; corner c = x + 2 y + 4 z, edge e = 4 a + s
+ * along axis a from the corner whose other coordinates, in cyclic axis order, are the bits of s). */
+int mpm_mc_table(int8_t *ntri, int8_t *edges);
+
 #ifdef __cplusplus
 }
 #endif

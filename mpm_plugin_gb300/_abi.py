@@ -27,7 +27,9 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_volume_lattice", "mpm_read_begin", "mpm_read_wait", "mpm_host_alloc",
            "mpm_host_free", "mpm_conservation", "mpm_device_bytes", "mpm_batch_create", "mpm_batch_destroy",
            "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
-           "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count")
+           "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count", "mpm_surface_create",
+           "mpm_surface_destroy", "mpm_surface_last_error", "mpm_surface_build", "mpm_surface_read", "mpm_surface_read_field",
+           "mpm_mc_table")
 
 
 class MpmDomainDesc(C.Structure):
@@ -104,6 +106,13 @@ def lib() -> C.CDLL:
         "mpm_batch_set_option": [P, I32, I64],
         "mpm_batch_get_stream": [P, C.POINTER(P)],
         "mpm_batch_launch_count": [P, C.POINTER(I64)],
+        "mpm_surface_create": [I32, C.POINTER(P)],
+        "mpm_surface_destroy": [P],
+        "mpm_surface_build": [P, I64, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                              C.POINTER(I64), C.POINTER(I64)],
+        "mpm_surface_read": [P, P, P, P],
+        "mpm_surface_read_field": [P, P, P],
+        "mpm_mc_table": [P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -113,6 +122,8 @@ def lib() -> C.CDLL:
     L.mpm_last_error.restype = C.c_char_p
     L.mpm_batch_last_error.argtypes = [P]
     L.mpm_batch_last_error.restype = C.c_char_p
+    L.mpm_surface_last_error.argtypes = [P]
+    L.mpm_surface_last_error.restype = C.c_char_p
     _lib = L
     return L
 

@@ -17,7 +17,7 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = BUILD / "libmpm_gb300.so"
-SOURCES = ["mpm_kernels.cu", "mpm_batch_kernels.cu", "mpm_abi.cu", "mpm_noalloc.cu", "mpm_emit.cu"]
+SOURCES = ["mpm_kernels.cu", "mpm_batch_kernels.cu", "mpm_abi.cu", "mpm_noalloc.cu", "mpm_emit.cu", "mpm_surface.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
