@@ -463,6 +463,50 @@ def fp64_error_sample(device: str, substeps: int = 100) -> dict:
             "fp64_clamp": errors(states[1]), "oracle_seconds": time.perf_counter() - t0}
 
 
+def run_surface(device: str, repeats: int = 3) -> dict:
+    """Surfacing (mpm_plugin_gb300.surface, the drop-in for mpm_surface/field.py) of two particle sets with
+    the default settings (detail 1, smoothing 2, iso 0.35): the 256^3 pour's pile (7.45M particles at the
+    8-per-cell spacing dx / 2) and a seeded Gaussian blob of 1M particles at spacing 0.004. Each call is timed
+    end to end through surface_particles (host set-up, copies in, splat, normalisation, marching cubes,
+    vertex velocities, copies out), median of `repeats` after one untimed call. The CPU restatement's splat
+    alone (oracle.surface, float64 numpy per particle) is timed on 2,000 particles of the blob beside it."""
+    import torch
+
+    from mpm_plugin_gb300.surface import SurfaceSettings, surface_particles
+    from oracle import surface as S
+
+    d, _, pile, _, _, _ = large_scene(256, 0.155)
+    rng = np.random.default_rng(5)
+    sets = {"pour_pile_256": (pile.astype(np.float32), rng.normal(0, 0.1, pile.shape).astype(np.float32), d.dx / 2),
+            "blob_1m": ((rng.normal(0, 0.05, (1_000_000, 3)) + 0.5).astype(np.float32),
+                        rng.normal(0, 1.0, (1_000_000, 3)).astype(np.float32), 0.004)}
+    out = {}
+    for name, (x, v, spacing) in sets.items():
+        st = SurfaceSettings()
+        surface_particles(x, v, spacing, st, device=device)
+        ts = []
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mesh = surface_particles(x, v, spacing, st, device=device)
+            ts.append(time.perf_counter() - t0)
+        t = float(np.median(ts))
+        cell = spacing / st.detail
+        pad = 2.0 * spacing * st.smoothing + 2.0 * cell
+        dims = [int(np.ceil(e / cell)) + 1 for e in x.max(0) + pad - (x.min(0).astype(np.float64) - pad)]
+        out[name] = {"particles": len(x), "field_nodes": int(np.prod(dims)), "verts": len(mesh.verts),
+                     "tris": len(mesh.tris), "ms": 1e3 * t, "particles_per_s": len(x) / t}
+    x, v, spacing = sets["blob_1m"]
+    sample = x[:2000]
+    origin, dims, cell, h = S.grid_params(x, spacing, 1.0, 2.0)
+    t0 = time.perf_counter()
+    S.splat(sample, v[:2000], np.float32(origin), np.float32(1.0 / cell), np.float32(cell), np.float32(h), dims)
+    el = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": len(sample) / el, "unit": "particles/s (splat only)", "cores": 1,
+                           "kind": "port", "sample": f"{len(sample)} particles of blob_1m, {el:.1f} s"}
+    return out
+
+
 def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict:
     """The small plain workload: a fixed-corotated jelly cube of side 0.25 centred at (0.5, 0.6, 0.5) in a
     1 m box at 64^3, 8 particles per cell from a seeded stratified jitter (32,768 particles), E 1e5, nu 0.3,
@@ -686,6 +730,7 @@ def run_gpu(args, world, rank, local):
     serving = run_serving(device, args.serve_seconds) if args.serve_seconds > 0 else None
     large = run_large(device, args.large_frames) if args.large_frames > 0 else None
     small = run_small(device) if args.small else None
+    surface = run_surface(device) if args.surface and rank == 0 else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -716,6 +761,7 @@ def run_gpu(args, world, rank, local):
         "serving": serving,
         "large": large,
         "small": small,
+        "surface": surface,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -737,6 +783,7 @@ def main():
                     help="seconds of Poisson bake requests (4 per second) for the serving measurement (0: skip)")
     ap.add_argument("--batched-frames", type=int, default=3,
                     help="frames of the 64-scene batched workload, plain and batched (0: skip)")
+    ap.add_argument("--surface", type=int, default=1, help="measure the surfacer (0: skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
