@@ -232,8 +232,11 @@ int mpm_volume_lattice(const double *tri, int64_t n_tris, const double *xs, int3
                        int64_t first_y, int32_t device, double *out, int64_t capacity, int64_t *n_out);
 
 /* ---- Surfacing (replaces the GPU part of mpm_surface/field.py:35-142, surface_particles) ----------------
- * A surfacer owns a stream and the device buffers of its last build. mpm_surface_build splats the n
- * particles (x, v: (n, 3) float32 host arrays) onto a dims[0] x dims[1] x dims[2] node grid at `origin`
+ * A surfacer owns a stream and device buffers that grow as needed and stay from frame to frame.
+ * mpm_surface_upload copies the n > 0 particles (x, v: (n, 3) float32 host arrays) to the device and returns
+ * the per-axis minimum and maximum of x (NaN on an axis holding a NaN, as numpy's min and max), from which
+ * the caller sets up the field grid (field.py:112-117). mpm_surface_build then splats the uploaded
+ * particles onto a dims[0] x dims[1] x dims[2] node grid (fewer than 2^31 nodes) at `origin`
  * (float32, the field.py origin rounded) with spacing `cell` (inv_cell = the host's 1 / cell rounded to
  * float32): cubic B-spline kernel of radius h, density and momentum summed (field.py:35-57); velocity =
  * momentum / density where density > 0, density scaled by inv_rest (field.py:60-66); then marching cubes at
@@ -245,9 +248,9 @@ int mpm_volume_lattice(const double *tri, int64_t n_tris, const double *xs, int3
 int mpm_surface_create(int32_t device, void **surfacer);
 int mpm_surface_destroy(void *surfacer);
 const char *mpm_surface_last_error(void *surfacer);
-int mpm_surface_build(void *surfacer, int64_t n, const float *x, const float *v, const float origin[3],
-                      const int32_t dims[3], float cell, float inv_cell, float h, float inv_rest, float iso,
-                      int64_t *n_verts, int64_t *n_tris);
+int mpm_surface_upload(void *surfacer, int64_t n, const float *x, const float *v, float lo[3], float hi[3]);
+int mpm_surface_build(void *surfacer, const float origin[3], const int32_t dims[3], float cell, float inv_cell,
+                      float h, float inv_rest, float iso, int64_t *n_verts, int64_t *n_tris);
 int mpm_surface_read(void *surfacer, float *verts, int32_t *tris, float *vel);
 /* The last build's fields, for checking: density (dims, float32, normalised) and field (dims x 4 float32:
  * velocity xyz where the raw density is positive, else the zero momentum, and the raw density). */

@@ -28,7 +28,7 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_host_free", "mpm_conservation", "mpm_device_bytes", "mpm_batch_create", "mpm_batch_destroy",
            "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
            "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count", "mpm_surface_create",
-           "mpm_surface_destroy", "mpm_surface_last_error", "mpm_surface_build", "mpm_surface_read", "mpm_surface_read_field",
+           "mpm_surface_destroy", "mpm_surface_upload", "mpm_surface_last_error", "mpm_surface_build", "mpm_surface_read", "mpm_surface_read_field",
            "mpm_mc_table")
 
 
@@ -108,8 +108,9 @@ def lib() -> C.CDLL:
         "mpm_batch_launch_count": [P, C.POINTER(I64)],
         "mpm_surface_create": [I32, C.POINTER(P)],
         "mpm_surface_destroy": [P],
-        "mpm_surface_build": [P, I64, P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
-                              C.POINTER(I64), C.POINTER(I64)],
+        "mpm_surface_upload": [P, I64, P, P, P, P],
+        "mpm_surface_build": [P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.POINTER(I64),
+                              C.POINTER(I64)],
         "mpm_surface_read": [P, P, P, P],
         "mpm_surface_read_field": [P, P, P],
         "mpm_mc_table": [P, P],

@@ -4,7 +4,10 @@
 // (momentum xyz, density) for the splat, then velocity xyz in place and the normalised density alongside.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <climits>
 #include <cmath>
+#include <cstring>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -202,34 +205,84 @@ __global__ void k_surf_tris(SurfGrid G, const uint8_t* __restrict__ cube, const 
     }
 }
 
+// Per-axis bounds of the particle positions: min and max as order-preserving integers, and a flag per axis
+// for a NaN (numpy's min and max return NaN then, and so does mpm_surface_upload).
+__device__ __forceinline__ int ordered_int(float f) {
+    const int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7fffffff;
+}
+__device__ __forceinline__ float from_ordered_int(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7fffffff); }
+
+__global__ void k_surf_bounds(int64_t n, const float* __restrict__ x, int* __restrict__ out) {
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+    unsigned int nan = 0;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float f = x[3 * p + a];
+            if (f != f) {
+                nan |= 1u << a;
+            } else {
+                const int o = ordered_int(f);
+                lo[a] = min(lo[a], o);
+                hi[a] = max(hi[a], o);
+            }
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = __reduce_min_sync(0xffffffffu, lo[a]);
+        hi[a] = __reduce_max_sync(0xffffffffu, hi[a]);
+    }
+    nan = __reduce_or_sync(0xffffffffu, nan);
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&out[a], lo[a]);
+            atomicMax(&out[3 + a], hi[a]);
+        }
+        if (nan) atomicOr(&out[6], (int)nan);
+    }
+}
+
 namespace {
+
+// Device buffers that only grow, kept from frame to frame.
+struct Pool {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        const size_t want = need + need / 4 + 256;
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const { return static_cast<T*>(p); }
+};
 
 struct Surfacer {
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
-    std::vector<void*> bufs;  // device buffers of the last build
-    float* d_verts = nullptr;
-    float* d_vvel = nullptr;
-    int32_t* d_tris = nullptr;
-    float* d_dens = nullptr;     // normalised density of the last build
-    float4* d_field = nullptr;   // velocity (xyz) and raw density (w) of the last build
-    int64_t n_verts = 0, n_tris = 0, n_nodes = 0;
+    Pool x, v, acc, dens, bits, cube, cnt, voff, tcnt, toff, tile, small, verts, vvel, tris;
+    int64_t n = 0, n_nodes = 0, n_verts = 0, n_tris = 0;
+    bool built = false;
     void release() {
-        for (void* p : bufs) cudaFree(p);
-        bufs.clear();
-        d_verts = d_vvel = d_dens = nullptr;
-        d_tris = nullptr;
-        d_field = nullptr;
-        n_verts = n_tris = n_nodes = 0;
-    }
-    template <class T>
-    cudaError_t alloc(T** p, size_t count) {
-        void* q = nullptr;
-        cudaError_t e = cudaMalloc(&q, count * sizeof(T) + 16);
-        if (e == cudaSuccess) bufs.push_back(q);
-        *p = static_cast<T*>(q);
-        return e;
+        for (Pool* q : {&x, &v, &acc, &dens, &bits, &cube, &cnt, &voff, &tcnt, &toff, &tile, &small, &verts, &vvel,
+                        &tris})
+            q->release();
+        n = n_nodes = n_verts = n_tris = 0;
+        built = false;
     }
 };
 
@@ -241,6 +294,15 @@ int surf_fail(Surfacer* s, int code, const std::string& msg) {
 }
 
 unsigned int blocks_of(int64_t n) { return (unsigned int)((n + 255) / 256); }
+
+struct DeviceScope {
+    int prev = 0;
+    explicit DeviceScope(int d) {
+        cudaGetDevice(&prev);
+        cudaSetDevice(d);
+    }
+    ~DeviceScope() { cudaSetDevice(prev); }
+};
 
 }  // namespace
 }  // namespace mpm
@@ -262,23 +324,23 @@ int mpm_mc_table(int8_t* ntri, int8_t* edges) {
 int mpm_surface_create(int32_t device, void** surfacer) {
     if (!surfacer) return MPM_ERR_ARGUMENT;
     *surfacer = nullptr;
-    int prev = 0;
-    cudaGetDevice(&prev);
-    if (cudaSetDevice(device) != cudaSuccess) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count) {
         cudaGetLastError();
         return MPM_ERR_CUDA;
     }
+    DeviceScope scope(device);
     Surfacer* s = new Surfacer();
     s->device = device;
     cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess && device >= 0 && device < 64 && !g_table_ready[device]) {
+    if (e == cudaSuccess && device < 64 && !g_table_ready[device]) {
         const McTable t = build_mc_table();
         e = cudaMemcpyToSymbol(c_mc_ntri, t.ntri, sizeof(t.ntri));
         if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_mc_edge, t.edge, sizeof(t.edge));
         if (e == cudaSuccess) g_table_ready[device] = true;
     }
-    cudaSetDevice(prev);
     if (e != cudaSuccess) {
+        cudaGetLastError();
         if (s->stream) cudaStreamDestroy(s->stream);
         delete s;
         return MPM_ERR_CUDA;
@@ -290,12 +352,10 @@ int mpm_surface_create(int32_t device, void** surfacer) {
 int mpm_surface_destroy(void* surfacer) {
     Surfacer* s = static_cast<Surfacer*>(surfacer);
     if (!s) return MPM_OK;
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(s->device);
+    DeviceScope scope(s->device);
+    cudaStreamSynchronize(s->stream);
     s->release();
     if (s->stream) cudaStreamDestroy(s->stream);
-    cudaSetDevice(prev);
     delete s;
     return MPM_OK;
 }
@@ -304,44 +364,80 @@ const char* mpm_surface_last_error(void* surfacer) {
     return surfacer ? static_cast<Surfacer*>(surfacer)->err.c_str() : "";
 }
 
-int mpm_surface_build(void* surfacer, int64_t n, const float* x, const float* v, const float origin[3],
-                      const int32_t dims[3], float cell, float inv_cell, float h, float inv_rest, float iso,
-                      int64_t* n_verts, int64_t* n_tris) {
+int mpm_surface_upload(void* surfacer, int64_t n, const float* x, const float* v, float lo[3], float hi[3]) {
     Surfacer* s = static_cast<Surfacer*>(surfacer);
     if (!s) return MPM_ERR_ARGUMENT;
-    if (n < 0 || (n > 0 && (!x || !v)) || !origin || !dims || !n_verts || !n_tris)
-        return surf_fail(s, MPM_ERR_ARGUMENT, "bad surfacing arguments");
+    if (n <= 0 || !x || !v || !lo || !hi) return surf_fail(s, MPM_ERR_ARGUMENT, "bad particle arrays");
+    DeviceScope scope(s->device);
+    cudaStream_t st = s->stream;
+    s->built = false;
+    const size_t bytes = sizeof(float) * 3 * (size_t)n;
+    int h_b[7];
+    cudaError_t e = s->x.ensure(bytes);
+    if (e == cudaSuccess) e = s->v.ensure(bytes);
+    if (e == cudaSuccess) e = s->small.ensure(64);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->x.p, x, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(s->v.p, v, bytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        const int init[7] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0};
+        e = cudaMemcpyAsync(s->small.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) {
+        const unsigned int blocks = (unsigned int)std::min<int64_t>(blocks_of(n), 152 * 8);
+        k_surf_bounds<<<blocks, 256, 0, st>>>(n, s->x.as<float>(), s->small.as<int>());
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_b, s->small.p, sizeof(h_b), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        s->n = 0;
+        return surf_fail(s, e == cudaErrorMemoryAllocation ? MPM_ERR_MEMORY : MPM_ERR_CUDA,
+                         std::string("surface upload: ") + cudaGetErrorString(e));
+    }
+    s->n = n;
+    for (int a = 0; a < 3; ++a) {
+        const bool nan = (h_b[6] >> a) & 1;
+        int l = h_b[a], u = h_b[3 + a];  // order-preserving integers back to float bits
+        l = l >= 0 ? l : l ^ 0x7fffffff;
+        u = u >= 0 ? u : u ^ 0x7fffffff;
+        std::memcpy(&lo[a], &l, 4);
+        std::memcpy(&hi[a], &u, 4);
+        if (nan) lo[a] = hi[a] = std::nanf("");
+    }
+    return MPM_OK;
+}
+
+int mpm_surface_build(void* surfacer, const float origin[3], const int32_t dims[3], float cell, float inv_cell,
+                      float h, float inv_rest, float iso, int64_t* n_verts, int64_t* n_tris) {
+    Surfacer* s = static_cast<Surfacer*>(surfacer);
+    if (!s) return MPM_ERR_ARGUMENT;
+    if (!origin || !dims || !n_verts || !n_tris) return surf_fail(s, MPM_ERR_ARGUMENT, "bad surfacing arguments");
+    if (s->n <= 0) return surf_fail(s, MPM_ERR_ARGUMENT, "no particles uploaded");
     if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2) return surf_fail(s, MPM_ERR_VALUE, "field grid under 2 nodes");
     if (!(cell > 0.0f) || !(h > 0.0f)) return surf_fail(s, MPM_ERR_VALUE, "cell and kernel radius must be positive");
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(s->device);
-    s->release();
+    DeviceScope scope(s->device);
+    s->built = false;
     const SurfGrid G{dims[0], dims[1], dims[2]};
     const int64_t N = (int64_t)dims[0] * dims[1] * dims[2];
+    if (N >= (int64_t)1 << 31) return surf_fail(s, MPM_ERR_VALUE, "field grid of 2^31 nodes or more");
     auto run = [&]() -> cudaError_t {
         cudaStream_t st = s->stream;
-        float4* acc;
-        float *dens, *px, *pv;
-        uint8_t *bits, *cube;
-        int32_t *cnt, *voff, *tcnt, *toff, *tile, *tot;
         cudaError_t e;
-        if ((e = s->alloc(&acc, N)) || (e = s->alloc(&dens, N)) || (e = s->alloc(&bits, N)) ||
-            (e = s->alloc(&cube, N)) || (e = s->alloc(&cnt, N)) || (e = s->alloc(&voff, N)) ||
-            (e = s->alloc(&tcnt, N)) || (e = s->alloc(&toff, N)) || (e = s->alloc(&tile, scan_tile_count(N) + 1)) ||
-            (e = s->alloc(&tot, 2)) || (e = s->alloc(&px, 3 * (size_t)(n > 0 ? n : 1))) ||
-            (e = s->alloc(&pv, 3 * (size_t)(n > 0 ? n : 1))))
+        if ((e = s->acc.ensure(sizeof(float4) * N)) || (e = s->dens.ensure(sizeof(float) * N)) ||
+            (e = s->bits.ensure(N)) || (e = s->cube.ensure(N)) || (e = s->cnt.ensure(sizeof(int32_t) * N)) ||
+            (e = s->voff.ensure(sizeof(int32_t) * N)) || (e = s->tcnt.ensure(sizeof(int32_t) * N)) ||
+            (e = s->toff.ensure(sizeof(int32_t) * N)) ||
+            (e = s->tile.ensure(sizeof(int32_t) * (scan_tile_count(N) + 1))) || (e = s->small.ensure(64)))
             return e;
-        s->d_dens = dens;
-        s->d_field = acc;
-        s->n_nodes = N;
+        float4* acc = s->acc.as<float4>();
+        float* dens = s->dens.as<float>();
+        uint8_t *bits = s->bits.as<uint8_t>(), *cube = s->cube.as<uint8_t>();
+        int32_t *cnt = s->cnt.as<int32_t>(), *voff = s->voff.as<int32_t>(), *tcnt = s->tcnt.as<int32_t>(),
+                *toff = s->toff.as<int32_t>(), *tile = s->tile.as<int32_t>(), *tot = s->small.as<int32_t>() + 8;
         if ((e = cudaMemsetAsync(acc, 0, sizeof(float4) * (size_t)N, st))) return e;
-        if (n > 0) {
-            if ((e = cudaMemcpyAsync(px, x, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, st))) return e;
-            if ((e = cudaMemcpyAsync(pv, v, sizeof(float) * 3 * (size_t)n, cudaMemcpyHostToDevice, st))) return e;
-            k_surf_splat<<<blocks_of(n), 256, 0, st>>>(n, px, pv, origin[0], origin[1], origin[2], inv_cell,
-                                                      cell, h, G, acc);
-        }
+        k_surf_splat<<<blocks_of(s->n), 256, 0, st>>>(s->n, s->x.as<float>(), s->v.as<float>(), origin[0], origin[1],
+                                                     origin[2], inv_cell, cell, h, G, acc);
         k_surf_normalize<<<blocks_of(N), 256, 0, st>>>(N, acc, dens, inv_rest);
         k_surf_edges<<<blocks_of(N), 256, 0, st>>>(G, dens, iso, bits, cnt);
         launch_exclusive_scan(st, cnt, N, voff, tile, tot);
@@ -350,26 +446,27 @@ int mpm_surface_build(void* surfacer, int64_t n, const float* x, const float* v,
         int32_t h_tot[2] = {0, 0};
         if ((e = cudaMemcpyAsync(h_tot, tot, sizeof(h_tot), cudaMemcpyDeviceToHost, st))) return e;
         if ((e = cudaStreamSynchronize(st))) return e;
+        s->n_nodes = N;
         s->n_verts = h_tot[0];
         s->n_tris = h_tot[1];
-        if ((e = s->alloc(&s->d_verts, 3 * (size_t)(s->n_verts > 0 ? s->n_verts : 1))) ||
-            (e = s->alloc(&s->d_vvel, 3 * (size_t)(s->n_verts > 0 ? s->n_verts : 1))) ||
-            (e = s->alloc(&s->d_tris, 3 * (size_t)(s->n_tris > 0 ? s->n_tris : 1))))
+        if ((e = s->verts.ensure(sizeof(float) * 3 * (size_t)(s->n_verts + 1))) ||
+            (e = s->vvel.ensure(sizeof(float) * 3 * (size_t)(s->n_verts + 1))) ||
+            (e = s->tris.ensure(sizeof(int32_t) * 3 * (size_t)(s->n_tris + 1))))
             return e;
         if (s->n_verts > 0)
-            k_surf_verts<<<blocks_of(N), 256, 0, st>>>(G, dens, acc, iso, bits, voff, s->d_verts, s->d_vvel);
-        if (s->n_tris > 0) k_surf_tris<<<blocks_of(N), 256, 0, st>>>(G, cube, toff, bits, voff, s->d_tris);
+            k_surf_verts<<<blocks_of(N), 256, 0, st>>>(G, dens, acc, iso, bits, voff, s->verts.as<float>(),
+                                                      s->vvel.as<float>());
+        if (s->n_tris > 0) k_surf_tris<<<blocks_of(N), 256, 0, st>>>(G, cube, toff, bits, voff, s->tris.as<int32_t>());
         if ((e = cudaGetLastError())) return e;
         return cudaStreamSynchronize(st);
     };
     const cudaError_t e = run();
-    cudaSetDevice(prev);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        s->release();
         return surf_fail(s, e == cudaErrorMemoryAllocation ? MPM_ERR_MEMORY : MPM_ERR_CUDA,
                          std::string("surfacing: ") + cudaGetErrorString(e));
     }
+    s->built = true;
     *n_verts = s->n_verts;
     *n_tris = s->n_tris;
     return MPM_OK;
@@ -378,24 +475,22 @@ int mpm_surface_build(void* surfacer, int64_t n, const float* x, const float* v,
 int mpm_surface_read(void* surfacer, float* verts, int32_t* tris, float* vel) {
     Surfacer* s = static_cast<Surfacer*>(surfacer);
     if (!s) return MPM_ERR_ARGUMENT;
+    if (!s->built) return surf_fail(s, MPM_ERR_ARGUMENT, "nothing built");
     if ((s->n_verts > 0 && (!verts || !vel)) || (s->n_tris > 0 && !tris))
         return surf_fail(s, MPM_ERR_ARGUMENT, "null output");
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(s->device);
+    DeviceScope scope(s->device);
     cudaError_t e = cudaSuccess;
     if (s->n_verts > 0) {
-        e = cudaMemcpyAsync(verts, s->d_verts, sizeof(float) * 3 * (size_t)s->n_verts, cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(verts, s->verts.p, sizeof(float) * 3 * (size_t)s->n_verts, cudaMemcpyDeviceToHost,
                             s->stream);
         if (e == cudaSuccess)
-            e = cudaMemcpyAsync(vel, s->d_vvel, sizeof(float) * 3 * (size_t)s->n_verts, cudaMemcpyDeviceToHost,
+            e = cudaMemcpyAsync(vel, s->vvel.p, sizeof(float) * 3 * (size_t)s->n_verts, cudaMemcpyDeviceToHost,
                                 s->stream);
     }
     if (e == cudaSuccess && s->n_tris > 0)
-        e = cudaMemcpyAsync(tris, s->d_tris, sizeof(int32_t) * 3 * (size_t)s->n_tris, cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(tris, s->tris.p, sizeof(int32_t) * 3 * (size_t)s->n_tris, cudaMemcpyDeviceToHost,
                             s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaSetDevice(prev);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return surf_fail(s, MPM_ERR_CUDA, std::string("surface read: ") + cudaGetErrorString(e));
@@ -406,17 +501,14 @@ int mpm_surface_read(void* surfacer, float* verts, int32_t* tris, float* vel) {
 int mpm_surface_read_field(void* surfacer, float* density, float* field) {
     Surfacer* s = static_cast<Surfacer*>(surfacer);
     if (!s) return MPM_ERR_ARGUMENT;
-    if (!s->d_dens || !density || !field) return surf_fail(s, MPM_ERR_ARGUMENT, "no field to read");
-    int prev = 0;
-    cudaGetDevice(&prev);
-    cudaSetDevice(s->device);
-    cudaError_t e = cudaMemcpyAsync(density, s->d_dens, sizeof(float) * (size_t)s->n_nodes, cudaMemcpyDeviceToHost,
+    if (!s->built || !density || !field) return surf_fail(s, MPM_ERR_ARGUMENT, "no field to read");
+    DeviceScope scope(s->device);
+    cudaError_t e = cudaMemcpyAsync(density, s->dens.p, sizeof(float) * (size_t)s->n_nodes, cudaMemcpyDeviceToHost,
                                     s->stream);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(field, s->d_field, sizeof(float4) * (size_t)s->n_nodes, cudaMemcpyDeviceToHost,
+        e = cudaMemcpyAsync(field, s->acc.p, sizeof(float4) * (size_t)s->n_nodes, cudaMemcpyDeviceToHost,
                             s->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
-    cudaSetDevice(prev);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return surf_fail(s, MPM_ERR_CUDA, std::string("field read: ") + cudaGetErrorString(e));

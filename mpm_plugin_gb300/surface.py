@@ -121,16 +121,23 @@ class Surfacer:
                 raise ValueError(msg)
             raise RuntimeError(msg)
 
-    def build(self, x, v, origin, dims, cell, h, inv_rest, iso):
-        """Runs the device pipeline; returns (verts in grid index units, tris, vel)."""
+    def upload(self, x, v):
+        """Copies the particles to the device; returns their per-axis (min, max) as float32 arrays."""
         x = np.ascontiguousarray(x, np.float32).reshape(-1, 3)
         v = np.ascontiguousarray(v, np.float32).reshape(-1, 3)
+        lo, hi = np.empty(3, np.float32), np.empty(3, np.float32)
+        self._check(self._lib.mpm_surface_upload(self._s, len(x), x.ctypes.data_as(C.c_void_p),
+                                                 v.ctypes.data_as(C.c_void_p), lo.ctypes.data_as(C.c_void_p),
+                                                 hi.ctypes.data_as(C.c_void_p)))
+        return lo, hi
+
+    def build(self, origin, dims, cell, h, inv_rest, iso):
+        """Runs the device pipeline on the uploaded particles; returns (verts in grid index units, tris, vel)."""
         o = (C.c_float * 3)(*np.asarray(origin, np.float64).astype(np.float32))
         d = (C.c_int32 * 3)(*[int(a) for a in dims])
         nv, nt = C.c_int64(), C.c_int64()
-        self._check(self._lib.mpm_surface_build(
-            self._s, len(x), x.ctypes.data_as(C.c_void_p), v.ctypes.data_as(C.c_void_p), o, d, float(cell),
-            float(1.0 / cell), float(h), float(inv_rest), float(iso), C.byref(nv), C.byref(nt)))
+        self._check(self._lib.mpm_surface_build(self._s, o, d, float(cell), float(1.0 / cell), float(h),
+                                                float(inv_rest), float(iso), C.byref(nv), C.byref(nt)))
         verts = np.empty((nv.value, 3), np.float32)
         vel = np.empty((nv.value, 3), np.float32)
         tris = np.empty((nt.value, 3), np.int32)
@@ -164,22 +171,25 @@ def surface_particles(positions: np.ndarray, velocities: np.ndarray, spacing: fl
     positions = np.asarray(positions, np.float32).reshape(-1, 3)
     if len(positions) == 0:
         return SurfaceMesh.empty()
+    index = _device_index(device)
+    surfacer = _surfacer(index)
+    # the particles go to the device once; their bounds come back from there (numpy's min and max over
+    # axis 0 of an (N, 3) array take longer than the whole surfacing on the GPU)
+    lo, hi = surfacer.upload(positions, velocities)
     cell = spacing / settings.detail
     h = 2.0 * spacing * settings.smoothing
     pad = h + 2.0 * cell
-    origin = positions.min(0).astype(np.float64) - pad
-    dims = tuple(int(math.ceil(e / cell)) + 1 for e in positions.max(0) + pad - origin)
+    origin = lo.astype(np.float64) - pad
+    dims = tuple(int(math.ceil(e / cell)) + 1 for e in hi + pad - origin)
     cells = dims[0] * dims[1] * dims[2]
     needed = cells * BYTES_PER_CELL
-    index = _device_index(device)
     if max_bytes is None:
         max_bytes = int(0.7 * _free_bytes(index))
     if needed > max_bytes:
         raise ValueError(f"surfacing needs a {dims[0]}x{dims[1]}x{dims[2]} grid ({cells:,} cells, about "
                          f"{needed / 1e9:.1f} GB of GPU memory), over the budget of {max_bytes / 1e9:.1f} GB; "
                          f"lower the detail or split the emitter")
-    verts, tris, vel = _surfacer(index).build(positions, velocities, origin, dims, cell, h,
-                                              1.0 / rest_density(spacing, h), settings.iso)
+    verts, tris, vel = surfacer.build(origin, dims, cell, h, 1.0 / rest_density(spacing, h), settings.iso)
     if len(verts) == 0:
         return SurfaceMesh.empty()
     world = (origin + verts.astype(np.float64) * cell).astype(np.float32)

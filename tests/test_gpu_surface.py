@@ -60,6 +60,21 @@ def test_surface_matches_oracle(detail, smoothing, iso):
     assert volume > 0  # wound outward
 
 
+def test_budget_error_and_bounds_match_numpy():
+    from mpm_plugin_gb300.surface import SurfaceSettings, _surfacer, surface_particles
+
+    pts = np.random.default_rng(0).normal(0, 1, (100_000, 3)).astype(np.float32)
+    lo, hi = _surfacer("cuda:0").upload(pts, pts)
+    np.testing.assert_array_equal(lo, pts.min(0))
+    np.testing.assert_array_equal(hi, pts.max(0))
+    pts[7, 1] = np.nan
+    lo, hi = _surfacer("cuda:0").upload(pts, pts)
+    assert np.isnan(lo[1]) and np.isnan(hi[1]) and not np.isnan(lo[0])
+    with pytest.raises(ValueError, match="surfacing needs a"):
+        surface_particles(pts[10:110] * 0.01, pts[10:110], 0.0001, SurfaceSettings(), device="cuda:0",
+                          max_bytes=1 << 20)
+
+
 def test_large_blob_is_closed():
     from mpm_plugin_gb300.surface import SurfaceSettings, surface_particles
 
