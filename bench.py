@@ -652,8 +652,10 @@ def run_gpu(args, world, rank, local):
     ktimes = solver.kernel_times(reset=True)
     total_ms = sum(t for t, _ in ktimes.values())
 
-    # the same timed substeps in deterministic mode (fixed-point P2G)
+    # the same timed substeps in deterministic mode (fixed-point P2G), with launch choices tuned for it
     solver.set_option(_abi.OPT_DETERMINISTIC, 1)
+    det_tuned = tune.tune_solver(solver, DT, FRAME_DT, substeps=50, deterministic=True)
+    solver.set_option(_abi.OPT_KERNEL_TIMING, 1)
     for _ in range(3):
         solver.substep(DT, 1.0, FRAME_DT)
     solver.kernel_times(reset=True)
@@ -756,7 +758,8 @@ def run_gpu(args, world, rank, local):
         "fp64_svd_lanes": fp64_lanes,
         "tuned": tuned,
         "deterministic": {"value": n * args.steps / (det_ms / 1e3), "unit": UNIT,
-                          "kernels_ms_per_launch": {k: t / max(c, 1) for k, (t, c) in det_times.items()}},
+                          "kernels_ms_per_launch": {k: t / max(c, 1) for k, (t, c) in det_times.items()},
+                          "tuned": det_tuned},
         "batched": batched,
         "serving": serving,
         "large": large,
