@@ -273,10 +273,6 @@ MPM_HD void mark_stencil_blocks(const GridDesc& g, const int base[3], unsigned i
             for (int bk = b0[2]; bk <= b1[2]; ++bk)
                 mark_block(((int64_t)bi * g.nb[1] + bj) * g.nb[2] + bk, flags, list, count);
 }
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-        if (f[c] == 0u) mark_block(id[c], flags, list, count);
-}
 
 // P2G of one particle into `sink` (sink.begin(base) once, then sink.add(i, j, k, mv x, y, z, m) per node);
 // false for a particle whose stencil leaves the padded grid (it scatters nothing).
