@@ -132,9 +132,14 @@ enum {
     MPM_OPT_FP64_CLAMP = 9,    /* 1: a Drucker-Prager or snow particle whose return mapping clamps is redone in
                                   FP64 (SVD, projection, hardening, stress); 0 (default): FP32, with the FP64
                                   redo only for SVDs that did not converge */
-    MPM_OPT_P2G_TILE = 10      /* 1: P2G sums each CTA's contributions in shared-memory tiles of the nodes its
+    MPM_OPT_P2G_TILE = 10,     /* 1: P2G sums each CTA's contributions in shared-memory tiles of the nodes its
                                   particles touch, then adds them to the grid; 0 (default): warp segments
                                   (shuffle sums of same-cell lanes) only. Deterministic mode uses segments */
+    MPM_OPT_COOP = 11          /* substeps of mpm_advance / mpm_run_substeps in cooperative launches of up to 64
+                                  substeps each (the kernels' phases separated by grid-wide barriers): 0
+                                  (default) never, 1 always (without kernel timing, the FP64 clamp or the tile
+                                  P2G), 2 for scenes of up to 131,072 particles. Slower than the graphs of
+                                  separate kernels on a GB300 at the sizes measured */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 
@@ -230,6 +235,12 @@ int mpm_batch_launch_count(void *batch, int64_t *launches);
 int mpm_volume_lattice(const double *tri, int64_t n_tris, const double *xs, int32_t nx, const double *ys, int32_t ny,
                        const double *zs, int32_t nz, double spacing, const double nudge[2], int64_t first_x,
                        int64_t first_y, int32_t device, double *out, int64_t capacity, int64_t *n_out);
+
+/* The grid barrier of the cooperative substeps on its own (2 CTAs, the handle's device and stream): with
+ * stall = 1 its arrival count is preset so that no CTA completes it, and each CTA gives up after its spin
+ * limit (about a second) and sets the error flag, which *timed_out receives; with stall = 0 it completes and
+ * *timed_out is 0. For tests of the bounded wait: the context stays usable either way. */
+int mpm_coop_barrier_selftest(void *handle, int32_t stall, int32_t *timed_out);
 
 /* ---- Surfacing (replaces the GPU part of mpm_surface/field.py:35-142, surface_particles) ----------------
  * A surfacer owns a stream and device buffers that grow as needed and stay from frame to frame.

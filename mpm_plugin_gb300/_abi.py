@@ -16,7 +16,7 @@ LIB_PATH = HERE / "_build" / "libmpm_gb300.so"
 MPM_OK, MPM_ERR_VALUE, MPM_ERR_NOT_IMPLEMENTED, MPM_ERR_CUDA, MPM_ERR_ARGUMENT, MPM_ERR_MEMORY = range(6)
 MODEL_IDS = {"elastic": 0, "von_mises": 1, "drucker_prager": 2, "snow": 3}
 (OPT_USE_GRAPH, OPT_KERNEL_TIMING, OPT_SORT_INTERVAL, OPT_DETERMINISTIC, OPT_G2P_VARIANT, OPT_LIST_CTAS,
- OPT_P2G_GROUP, OPT_PDL, OPT_FP64_CLAMP, OPT_P2G_TILE) = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10
+ OPT_P2G_GROUP, OPT_PDL, OPT_FP64_CLAMP, OPT_P2G_TILE, OPT_COOP) = 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11
 KERNEL_SLOTS = ("p2g", "grid_update", "g2p", "other")
 
 # every symbol declared in include/mpm_gb300.h
@@ -24,7 +24,7 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_set_collider_transforms", "mpm_advance", "mpm_substep", "mpm_run_substeps", "mpm_particle_count", "mpm_get_particles",
            "mpm_is_occupied", "mpm_save_state", "mpm_load_state", "mpm_set_option", "mpm_get_stream",
            "mpm_synchronize", "mpm_kernel_times", "mpm_grid_dims", "mpm_read_grid", "mpm_read_collider_pose",
-           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_volume_lattice", "mpm_read_begin", "mpm_read_wait", "mpm_host_alloc",
+           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_volume_lattice", "mpm_read_begin", "mpm_read_wait", "mpm_host_alloc", "mpm_coop_barrier_selftest",
            "mpm_host_free", "mpm_conservation", "mpm_device_bytes", "mpm_batch_create", "mpm_batch_destroy",
            "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
            "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count", "mpm_surface_create",
@@ -106,6 +106,7 @@ def lib() -> C.CDLL:
         "mpm_batch_set_option": [P, I32, I64],
         "mpm_batch_get_stream": [P, C.POINTER(P)],
         "mpm_batch_launch_count": [P, C.POINTER(I64)],
+        "mpm_coop_barrier_selftest": [P, I32, C.POINTER(I32)],
         "mpm_surface_create": [I32, C.POINTER(P)],
         "mpm_surface_destroy": [P],
         "mpm_surface_upload": [P, I64, P, P, P, P],

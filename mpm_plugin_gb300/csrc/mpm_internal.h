@@ -63,6 +63,12 @@ inline void launch_step_kernel(void (*kernel)(KArgs...), unsigned int grid, unsi
 cudaError_t prepare_substep_kernels();
 cudaError_t prepare_batch_kernels();
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing);
+// reps substeps of one scene in one cooperative launch (k_substeps_coop); bar: 3 device words (barrier and
+// error flag), zeroed here. Grid: the particle chunks of 256, at most the CTAs resident at once.
+cudaError_t launch_substeps_coop(cudaStream_t st, const SubstepArgs& a, int reps, unsigned int* bar);
+// One grid barrier on 2 CTAs (cooperative); with stall no CTA completes it and both give up after the spin
+// limit. *timed_out (host) receives the error flag; synchronises the stream.
+cudaError_t barrier_selftest(cudaStream_t st, bool stall, unsigned int* bar, unsigned int* timed_out);
 int substep_kernel_count(const SubstepArgs& a);
 
 // One batched substep over a device table of scenes (mpm_batch_kernels.cu). The particle kernels run

@@ -515,6 +515,51 @@ void launch_sdf_fill(cudaStream_t st, const ColliderDev& col, const BvhNode* nod
     k_sdf_fill<<<blocks_for(n_vox, 128), 128, 0, st>>>(col, nodes, tris, n_vox, max_cand, cells, starts, cand);
 }
 
+// CTAs of the cooperative multi-substep kernel that fit on the device at once (all must be resident).
+static int coop_resident_ctas() {
+    static int cached[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 0;
+    if (!cached[dev]) {
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_substeps_coop<1>, 256, 0) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        cached[dev] = per_sm * sms;
+    }
+    return cached[dev];
+}
+
+cudaError_t launch_substeps_coop(cudaStream_t st, const SubstepArgs& a, int reps, unsigned int* bar) {
+    const int resident = coop_resident_ctas();
+    if (resident <= 0) return cudaErrorCooperativeLaunchTooLarge;
+    const int64_t chunks = std::max<int64_t>((a.n + 255) / 256, 1);
+    const unsigned int grid = (unsigned int)std::min<int64_t>(chunks, resident);
+    cudaError_t e = cudaMemsetAsync(bar, 0, 3 * sizeof(unsigned int), st);
+    if (e != cudaSuccess) return e;
+    OneScene sc{a};
+    void* args[] = {&sc, &reps, &bar};
+    return cudaLaunchCooperativeKernel((const void*)k_substeps_coop<1>, dim3(grid), dim3(256), args, 0, st);
+}
+
+// One barrier on its own, for checking the bounded wait (bar as for k_substeps_coop).
+__global__ void k_barrier_selftest(unsigned int* bar) { grid_barrier(bar, bar + 2); }
+
+cudaError_t barrier_selftest(cudaStream_t st, bool stall, unsigned int* bar, unsigned int* timed_out) {
+    // stall: the arrival count starts so high that no CTA is ever the last to arrive
+    const unsigned int init[3] = {stall ? 0x80000000u : 0u, 0u, 0u};
+    cudaError_t e = cudaMemcpyAsync(bar, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    void* args[] = {&bar};
+    if (e == cudaSuccess)
+        e = cudaLaunchCooperativeKernel((const void*)k_barrier_selftest, dim3(2), dim3(32), args, 0, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(timed_out, bar + 2, sizeof(unsigned int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e;
+}
+
 cudaError_t prepare_substep_kernels() {
     return cudaFuncSetAttribute(k_p2g_tile<OneScene>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2gTileBytes);
 }

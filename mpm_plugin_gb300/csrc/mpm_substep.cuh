@@ -627,17 +627,32 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     }
 }
 
+// Grid nodes through the read-only data path (the grid is not written while a G2P kernel runs).
 struct GlobalSource {
     const GridDesc* g;
     const float4* grid;
     MPM_HD float4 operator()(int64_t node) const { return load_node(&grid[node]); }
 };
 
-template <bool kFp64Clamp = false>
+// Grid nodes from L2 (inside a kernel that also writes the grid in an earlier phase, where the read-only
+// path could return lines of the previous substep).
+struct CoherentSource {
+    const GridDesc* g;
+    const float4* grid;
+    MPM_HD float4 operator()(int64_t node) const {
+#ifdef __CUDA_ARCH__
+        return __ldcg(&grid[node]);
+#else
+        return grid[node];
+#endif
+    }
+};
+
+template <bool kFp64Clamp = false, class Source = GlobalSource>
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         const float4* __restrict__ grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false) {
-    GlobalSource src{&g, grid};
-    g2p_particle_from<GlobalSource, kFp64Clamp>(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp);
+                         const float4* grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false) {
+    Source src{&g, grid};
+    g2p_particle_from<Source, kFp64Clamp>(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

@@ -282,19 +282,23 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, const P2
         p2g_segment_sums<5>(a, t, valid, leader, tail, at);
 }
 
-template <class Scenes>
-__global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
-    pdl_begin();
-    const int s = sc.scene_of_cta(blockIdx.x);
-    const SubstepArgs a = sc.get(s);
-    if (!sc.active(a)) return;
-    const int64_t first = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x;
+// P2G of the 256 particles from `first` (one CTA's share; the warps past the end return).
+__device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     const int64_t p = first + threadIdx.x;
     if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end
     const Particles P = particles_of(a);
     P2gTerms t;
     const bool valid = p < a.n && p2g_terms(P, p, a.mats, a.g, a.sp->dt, t);
     p2g_warp_segments(a, t, valid);
+}
+
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_p2g_scatter(Scenes sc) {
+    pdl_begin();
+    const int s = sc.scene_of_cta(blockIdx.x);
+    const SubstepArgs a = sc.get(s);
+    if (!sc.active(a)) return;
+    p2g_cta(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
 }
 
 // P2G through shared-memory tiles. The CTA's 256 particles (a contiguous range of the particle order) are
@@ -507,21 +511,27 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
 // Caps of 128 and 64 registers were slower on the mixed and the 256^3 workloads (measured on a GB300). Both
 // builds are kept; the autotuner picks one per workload. kFp64Clamp: the build with the FP64 redo at the
 // Drucker-Prager and snow clamp (MPM_OPT_FP64_CLAMP), launched only when a scene has the option set.
+template <bool kFp64Clamp = false, class Source = GlobalSource>
+__device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
+    const int64_t p = first + threadIdx.x;
+    if (p >= a.n) return;
+    float nx[3];
+    g2p_particle<kFp64Clamp, Source>(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx,
+                                     a.fp64_clamp != 0);
+    if (a.cd.n_col > 0) {
+        ColliderData cd = a.cd;
+        cd.poses += a.sp->pose_base;
+        if (near_any_collider(nx, cd)) warp_append(a.wl.part_cand, &a.wl.counts[3], (int32_t)p);
+    }
+}
+
 template <class Scenes, int kMinCtas, bool kFp64Clamp = false>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     pdl_begin();
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
     if (!sc.active(a)) return;
-    const int64_t p = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x + threadIdx.x;
-    if (p >= a.n) return;
-    float nx[3];
-    g2p_particle<kFp64Clamp>(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx, a.fp64_clamp != 0);
-    if (a.cd.n_col > 0) {
-        ColliderData cd = a.cd;
-        cd.poses += a.sp->pose_base;
-        if (near_any_collider(nx, cd)) warp_append(a.wl.part_cand, &a.wl.counts[3], (int32_t)p);
-    }
+    g2p_cta<kFp64Clamp>(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
 }
 
 // Projection of one listed particle (the same two shapes as for the nodes).
@@ -560,6 +570,89 @@ __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
                 const int s = scene_of_item(off, sc.count(), q);
                 project_candidate<false>(sc.get(s), q - off[s]);
             }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------
+// Several substeps of one scene in one cooperative launch: the phases of the kernels above, each over all
+// CTAs of the grid, separated by grid-wide barriers. A small scene's substep is then one barrier per phase
+// instead of one kernel launch per phase. Each CTA takes the same particle chunks in every phase; data
+// written by other CTAs is read after a barrier (whose fences order it) through coherent loads: the G2P
+// gather reads the grid from L2, never through the read-only path.
+// ------------------------------------------------------------------------------------------------------
+constexpr unsigned int kBarrierSpins = 1u << 22;  // polls of an L2 word: about a second
+
+// Grid-wide barrier (bar[0] arrivals, bar[1] generation). A CTA that waits longer than kBarrierSpins sets
+// *err and goes on; every CTA then leaves the kernel at its next barrier. Returns false once *err is set.
+__device__ __forceinline__ bool grid_barrier(unsigned int* bar, unsigned int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vb = bar;
+        const unsigned int gen = vb[1];
+        __threadfence();
+        if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+            bar[0] = 0u;
+            __threadfence();
+            atomicAdd(&bar[1], 1u);
+        } else {
+            unsigned int spins = 0;
+            while (vb[1] == gen) {
+                if (++spins > kBarrierSpins) {
+                    atomicOr(err, 1u);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile unsigned int*)err == 0u;
+}
+
+// reps substeps; bar: 2 barrier words and the error word, zeroed before the launch.
+template <int kMinCtas>
+__global__ void __launch_bounds__(256, kMinCtas) k_substeps_coop(OneScene sc, int reps, unsigned int* bar) {
+    const SubstepArgs a = sc.get(0);
+    unsigned int* err = bar + 2;
+    const unsigned int ncta = gridDim.x, tid = blockIdx.x * blockDim.x + threadIdx.x, threads = ncta * blockDim.x;
+    const unsigned int warp = tid >> 5, warps = threads >> 5;
+    const int64_t pctas = (a.n + 255) / 256;
+    for (int r = 0; r < reps; ++r) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) step_begin(a.sp, a.wl.counts, a.cd.n_col);
+        if (!grid_barrier(bar, err)) return;
+        {
+            const unsigned int n = a.wl.counts[(a.sp->seq - 1u) & 1u];
+            for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += ncta * 4u) clear_block(a, i);
+        }
+        if (!grid_barrier(bar, err)) return;
+        for (int64_t c = blockIdx.x; c < pctas; c += ncta) p2g_cta(a, c * 256);
+        if (!grid_barrier(bar, err)) return;
+        {
+            const unsigned int n = a.wl.counts[a.sp->seq & 1u];
+            for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += ncta * 4u)
+                grid_update_block(a, i);
+        }
+        if (!grid_barrier(bar, err)) return;
+        if (a.cd.n_col > 0) {
+            const unsigned int n = a.wl.counts[2];
+            if (n <= warps * kWarpItemsPerWarp) {
+                for (unsigned int i = warp; i < n; i += warps) grid_collider_node<true>(a, i);
+            } else {
+                for (unsigned int i = tid; i < n; i += threads) grid_collider_node<false>(a, i);
+            }
+            if (!grid_barrier(bar, err)) return;
+        }
+        for (int64_t c = blockIdx.x; c < pctas; c += ncta) g2p_cta<false, CoherentSource>(a, c * 256);
+        if (!grid_barrier(bar, err)) return;
+        if (a.cd.n_col > 0) {
+            const unsigned int n = a.wl.counts[3];
+            if (n <= warps * kWarpItemsPerWarp) {
+                for (unsigned int i = warp; i < n; i += warps) project_candidate<true>(a, i);
+            } else {
+                for (unsigned int i = tid; i < n; i += threads) project_candidate<false>(a, i);
+            }
+            if (!grid_barrier(bar, err)) return;
         }
     }
 }

@@ -133,3 +133,17 @@ def test_batch_is_bit_identical_to_alone():
         batch.advance(1 / 96)
     for a, b in zip(alone, batched):
         _bits_equal(a.save_state(), b.save_state())
+
+
+def test_cooperative_launches_are_bit_identical():
+    """Substeps in cooperative launches (the kernels' phases separated by grid-wide barriers) give the same
+    bits as the same substeps launched kernel by kernel."""
+    from mpm_plugin_gb300 import _abi
+
+    out = []
+    for coop in (0, 1):
+        s, _ = _scene()
+        s.set_option(_abi.OPT_COOP, coop)
+        s.run_substeps(2e-4, 24)
+        out.append(s.save_state())
+    _bits_equal(out[0], out[1])

@@ -363,6 +363,47 @@ def test_run_substeps_equals_substeps_one_by_one():
         assert rel_err(sa[k], sb[k]) <= 1e-5, (k, rel_err(sa[k], sb[k]))
 
 
+def test_cooperative_substeps_match_kernel_by_kernel_substeps():
+    """run_substeps in cooperative launches (forced, and with a collider) against the same substeps launched
+    kernel by kernel, and an advance through the automatic choice for a small scene."""
+    from mpm_plugin_gb300 import _abi
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+
+    d, mats, groups, (cv, ct, xf) = mix_scene(res=64)
+    out = []
+    for coop in (0, 1):
+        s = gpu_solver(d, mats)
+        for pos, m, vel in groups:
+            add(s, pos, m, m, vel)
+        s.set_colliders([ColliderGeometry(MeshData(cv, ct), True, 0.5)])
+        s.set_collider_transforms(xf[None], xf[None])
+        s.set_option(_abi.OPT_COOP, coop)
+        s.set_option(_abi.OPT_SORT_INTERVAL, 0)
+        s.run_substeps(2e-4, 1)  # one substep the same way in both (and the colliders' voxel grids built)
+        launches = s.launch_count()
+        s.run_substeps(2e-4, 12)
+        if coop:  # twelve substeps in one launch (and the collider poses of the twelve in one)
+            assert s.launch_count() - launches <= 2
+        out.append(s.save_state())
+    for k in ("x", "v", "F"):
+        assert rel_err(out[1][k], out[0][k]) <= 1e-5, (k, rel_err(out[1][k], out[0][k]))
+
+
+def test_cooperative_barrier_gives_up_and_reports():
+    """The grid barrier's bounded wait: with its arrival count preset so no CTA completes it, both CTAs give up
+    after the spin limit and set the error flag; the context stays usable."""
+    import ctypes as C
+
+    d = domain(res=32)
+    s = gpu_solver(d, [preset("jelly")])
+    add(s, box_particles((0.4, 0.4, 0.3), (0.6, 0.6, 0.5), d.dx))
+    flag = C.c_int32(-1)
+    assert s._lib.mpm_coop_barrier_selftest(s._h, 1, C.byref(flag)) == 0 and flag.value == 1
+    assert s._lib.mpm_coop_barrier_selftest(s._h, 0, C.byref(flag)) == 0 and flag.value == 0
+    st = s.advance(1 / 96)
+    assert st.substeps > 0 and np.isfinite(s.save_state()["x"]).all()
+
+
 def test_full_size_momentum_is_conserved_without_gravity_or_walls():
     """The 304k-particle mixed workload at full size, gravity off and collider off, for 200 substeps (the
     snowball in flight, no particle near a wall): P2G and G2P conserve momentum exactly in exact
