@@ -525,8 +525,11 @@ def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict
     mats = [MaterialParams("jelly_cube", "elastic", 1e5, 0.3, 1000.0)]
     pos = lattice_box((0.375, 0.475, 0.375), (0.625, 0.725, 0.625), d.dx / 2, np.random.default_rng(0))
     z = np.zeros(len(pos), np.int32)
+    from mpm_plugin_gb300 import tune
+
     g = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
     g.add_particles(pos, np.zeros_like(pos), z, z)
+    tuned = tune.tune_solver(g, 1e-4, 1e-4, substeps=50)  # launch choices for this size
     g.run_substeps(1e-4, 10)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -547,6 +550,7 @@ def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict
             "ms_per_substep": 1e3 * gpu_s / substeps,
             "timing": "host clock around one run_substeps call with device synchronisation (launch-bound at this "
                       "size: about 7 kernels per substep)",
+            "tuned": tuned,
             "cpu_baseline": {"value": n * cpu_substeps / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{cpu_substeps} substeps of the same scene"}}
 

@@ -32,7 +32,7 @@ from pathlib import Path
 from mpm_plugin_gb300 import _abi
 
 DEFAULTS = {"sort_interval": 0, "g2p_variant": 0, "list_ctas_per_sm": 8, "p2g_group": 32, "pdl": 1}
-CANDIDATES = {"sort_interval": (0, 2, 4, 8, 16), "g2p_variant": (0, 1), "list_ctas_per_sm": (4, 8, 16),
+CANDIDATES = {"sort_interval": (0, 2, 4, 8, 16), "g2p_variant": (0, 1), "list_ctas_per_sm": (2, 4, 8, 16),
               "p2g_group": (1, 4, 8, 32), "pdl": (0, 1)}
 KNOB_ORDER = ("g2p_variant", "sort_interval", "p2g_group", "list_ctas_per_sm", "pdl")
 MIN_GAIN = 0.02
