@@ -16,7 +16,6 @@
 // vertices on one face (such a triangle would be drawn again, reversed, by the neighbouring cell).
 #pragma once
 
-#include <array>
 #include <cstdint>
 
 namespace mpm {

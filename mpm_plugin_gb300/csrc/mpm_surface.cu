@@ -10,7 +10,6 @@
 #include <cstring>
 #include <cstdint>
 #include <string>
-#include <vector>
 
 #include "../../include/mpm_gb300.h"
 #include "mpm_internal.h"
