@@ -634,42 +634,49 @@ def run_gpu(args, world, rank, local):
         solver.substep(DT, 1.0, FRAME_DT)
     solver.synchronize()
 
-    # timed region: K substeps, L2 written between them. Each substep replays the captured graph, which
-    # records CUDA events on the solver's stream between its kernel groups; the substep time is the sum.
-    solver.set_option(_abi.OPT_KERNEL_TIMING, 1)
-    solver.substep(DT, 1.0, FRAME_DT)  # capture the timed graph outside the timed region
-    solver.kernel_times(reset=True)
-    launches0 = solver.launch_count()
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
+    # timed region: K substeps, L2 written between them. Each substep replays its captured graph with CUDA
+    # events recorded at the graph's two ends on the solver's stream (MPM_OPT_KERNEL_TIMING 2); the value is
+    # the sum of those substep times, so the writes between substeps are not in it.
+    def timed_substeps(mode, clocks=None):
+        """K substeps under kernel timing `mode`; returns the kernels they launched."""
+        solver.set_option(_abi.OPT_KERNEL_TIMING, mode)
+        solver.substep(DT, 1.0, FRAME_DT)  # capture the timed graph outside the timed region
+        solver.kernel_times(reset=True)
+        solver.substep_times(reset=True)
+        launches0 = solver.launch_count()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.__enter__()
         with torch.cuda.stream(stream):
             for k in range(args.steps):
                 flush.fill_(float(k))
                 solver.substep(DT, 1.0, FRAME_DT)
         torch.cuda.synchronize()
-    if world > 1:
-        torch.distributed.barrier()
-    launches = solver.launch_count() - launches0
+        if clocks:
+            clocks.__exit__(None, None, None)
+        if world > 1:
+            torch.distributed.barrier()
+        return solver.launch_count() - launches0
+
+    clk = Clocks(local)
+    launches = timed_substeps(2, clk)
+    total_ms, _ = solver.substep_times(reset=True)
+    # the same substeps with events between the kernel groups (which also break the launch chain there): the
+    # per-kernel times of the breakdown and the roofline
+    timed_substeps(1)
     ktimes = solver.kernel_times(reset=True)
-    total_ms = sum(t for t, _ in ktimes.values())
 
     # the same timed substeps in deterministic mode (fixed-point P2G), with launch choices tuned for it
     solver.set_option(_abi.OPT_DETERMINISTIC, 1)
     det_tuned = tune.tune_solver(solver, DT, FRAME_DT, substeps=50, deterministic=True)
-    solver.set_option(_abi.OPT_KERNEL_TIMING, 1)
     for _ in range(3):
         solver.substep(DT, 1.0, FRAME_DT)
-    solver.kernel_times(reset=True)
-    torch.cuda.synchronize()
-    with torch.cuda.stream(stream):
-        for k in range(args.steps):
-            flush.fill_(float(k))
-            solver.substep(DT, 1.0, FRAME_DT)
-    torch.cuda.synchronize()
+    timed_substeps(2)
+    det_ms, _ = solver.substep_times(reset=True)
+    timed_substeps(1)
     det_times = solver.kernel_times(reset=True)
-    det_ms = sum(t for t, _ in det_times.values())
     solver.set_option(_abi.OPT_DETERMINISTIC, 0)
     solver.set_option(_abi.OPT_KERNEL_TIMING, 0)
 

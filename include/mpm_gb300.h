@@ -116,7 +116,9 @@ int mpm_load_state(void *handle, int64_t n, const float *x, const float *v, cons
 enum {
     MPM_OPT_USE_GRAPH = 1,     /* 1 (default): replay a captured CUDA graph per substep */
     MPM_OPT_KERNEL_TIMING = 2, /* 1: record CUDA events between the kernel groups of every substep (event nodes
-                                  in the captured graph); each substep then waits for its own completion */
+                                  in the captured graph); 2: events at the two ends of each substep only, so
+                                  the kernels inside stay chained as untimed; each substep then waits for its
+                                  own completion */
     MPM_OPT_SORT_INTERVAL = 3, /* N (default 4): after every N substeps the particle storage is reordered into
                                   grid-block order (ids travel along, so host order is unchanged); 0: never */
     MPM_OPT_DETERMINISTIC = 4, /* 1: bit-reproducible runs. P2G and the occupancy splat sum in 64-bit fixed point
@@ -148,7 +150,8 @@ int mpm_get_stream(void *handle, void **stream);
 int mpm_synchronize(void *handle);
 
 /* Per-kernel totals since the last reset, when MPM_OPT_KERNEL_TIMING is on: names are
- * "p2g", "grid_update", "g2p", "other"; ms[i] total milliseconds and launches[i] counts. */
+ * "p2g", "grid_update", "g2p", "other" (timing 1), then "substep" (timing 2: whole substeps, reorders
+ * included); ms[i] total milliseconds and launches[i] counts, n_slots of them (at most 5). */
 int mpm_kernel_times(void *handle, int32_t n_slots, float *ms, int64_t *launches, int32_t reset);
 
 /* Read-back for checks and tooling (no reference counterpart; the reference's grid lives in Warp arrays

@@ -157,14 +157,15 @@ struct Handle {
     unsigned int* d_coop = nullptr;  // its barrier words and error flag
     bool coop_used = false;      // a cooperative launch ran since the last check of its error flag
 
-    bool timing = false;
+    int timing = 0;              // 1: events between the kernel groups; 2: events around each substep only
     cudaEvent_t tev[5] = {};     // event nodes of the timed graph
     GraphCache tgraphs;          // the substep graph with timing events
+    GraphCache bgraphs;          // the substep graph with events at its two ends
     cudaEvent_t perm_ev[2] = {};
     std::vector<cudaEvent_t> ev_pool;
     std::vector<std::vector<cudaEvent_t>> ev_pending;  // per substep: 4 events around p2g / grid / g2p
-    double t_ms[4] = {0, 0, 0, 0};
-    int64_t t_launches[4] = {0, 0, 0, 0};
+    double t_ms[5] = {0, 0, 0, 0, 0};  // p2g, grid, g2p, other; [4]: whole substeps (timing 2)
+    int64_t t_launches[5] = {0, 0, 0, 0, 0};
 
     std::string err;
 };
@@ -223,6 +224,7 @@ Particles bind_arena(void* base, int64_t cap, int64_t n) {
 void invalidate_graph(Handle* h) {
     h->graphs.clear();
     h->tgraphs.clear();
+    h->bgraphs.clear();
 }
 
 Status ensure_capacity(Handle* h, int64_t need) {
@@ -423,7 +425,7 @@ Status reorder_particles(Handle* h) {
         CK(cudaEventSynchronize(h->perm_ev[1]));
         float t = 0;
         cudaEventElapsedTime(&t, h->perm_ev[0], h->perm_ev[1]);
-        h->t_ms[3] += t;
+        h->t_ms[h->timing == 2 ? 4 : 3] += t;
     }
     std::swap(h->arena, h->spare_arena);
     h->P = dst;
@@ -476,6 +478,34 @@ Status run_substep(Handle* h, int reps = 1) {
             launch_substep(h->stream, a, h->shape, nullptr, false);
         }
         CK(cudaGetLastError());
+        return {};
+    }
+    if (h->timing == 2) {  // events at the substep graph's two ends: the substep's device time, with the
+                           // kernels inside chained as in the untimed graph
+        if (!h->tev[0])
+            for (auto& e : h->tev) CK(cudaEventCreate(&e));
+        cudaGraphExec_t g = h->bgraphs.find(key);
+        if (!g) {
+            cudaGraph_t graph;
+            CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            cudaEventRecordWithFlags(h->tev[0], h->stream, cudaEventRecordExternal);
+            launch_substep(h->stream, a, h->shape, nullptr, true);
+            cudaEventRecordWithFlags(h->tev[4], h->stream, cudaEventRecordExternal);
+            cudaError_t e0 = cudaGetLastError();
+            cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+            CK(e0);
+            CK(e);
+            e = cudaGraphInstantiate(&g, graph, 0);
+            cudaGraphDestroy(graph);
+            CK(e);
+            h->bgraphs.put(h->bgraphs.victim(), key, g);
+        }
+        CK(cudaGraphLaunch(g, h->stream));
+        CK(cudaEventSynchronize(h->tev[4]));
+        float t = 0;
+        cudaEventElapsedTime(&t, h->tev[0], h->tev[4]);
+        h->t_ms[4] += t;
+        h->t_launches[4] += 1;
         return {};
     }
     if (h->timing) {  // the same graph with event nodes; read them before the next replay overwrites them
@@ -1551,7 +1581,8 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             if (!h->use_graph) invalidate_graph(h);
             return MPM_OK;
         case MPM_OPT_KERNEL_TIMING:
-            h->timing = value != 0;
+            if (value < 0 || value > 2) return finish(h, {MPM_ERR_VALUE, "kernel timing must be 0, 1 or 2"});
+            h->timing = (int)value;
             return MPM_OK;
         case MPM_OPT_DETERMINISTIC:
             return finish(h, set_deterministic(h, value != 0));
@@ -1615,12 +1646,12 @@ int mpm_kernel_times(void* handle, int32_t n_slots, float* ms, int64_t* launches
         for (auto x : ev) h->ev_pool.push_back(x);
     }
     h->ev_pending.clear();
-    for (int i = 0; i < n_slots && i < 4; ++i) {
+    for (int i = 0; i < n_slots && i < 5; ++i) {
         if (ms) ms[i] = (float)h->t_ms[i];
         if (launches) launches[i] = h->t_launches[i];
     }
     if (reset)
-        for (int i = 0; i < 4; ++i) { h->t_ms[i] = 0; h->t_launches[i] = 0; }
+        for (int i = 0; i < 5; ++i) { h->t_ms[i] = 0; h->t_launches[i] = 0; }
     return MPM_OK;
 }
 

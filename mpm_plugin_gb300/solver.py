@@ -286,10 +286,18 @@ class Gb300Solver(Solver):
         return s.value or 0
 
     def kernel_times(self, reset: bool = False) -> dict[str, tuple[float, int]]:
-        ms = (C.c_float * 4)()
-        n = (C.c_int64 * 4)()
-        self._check(self._lib.mpm_kernel_times(self._h, 4, ms, n, int(reset)))
-        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_abi.KERNEL_SLOTS)}
+        """Per-group (milliseconds, count) under OPT_KERNEL_TIMING 1."""
+        return {k: v for k, v in self._times(reset).items() if k != "substep"}
+
+    def substep_times(self, reset: bool = False) -> tuple[float, int]:
+        """(milliseconds, substeps) of whole substeps under OPT_KERNEL_TIMING 2."""
+        return self._times(reset)["substep"]
+
+    def _times(self, reset: bool) -> dict[str, tuple[float, int]]:
+        ms = (C.c_float * 5)()
+        n = (C.c_int64 * 5)()
+        self._check(self._lib.mpm_kernel_times(self._h, 5, ms, n, int(reset)))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_abi.KERNEL_SLOTS + ("substep",))}
 
     def read_grid(self) -> np.ndarray:
         """(dims..., 4) float32: node velocity (momentum where the mass is 0) and mass after the last substep."""

@@ -12,9 +12,9 @@ The shared-memory tile P2G (MPM_OPT_P2G_TILE) is not searched: it was slower tha
 unsorted mixed workload and on the 256^3 pour, and in a short tuning window it could look faster.
 
 Search: coordinate descent from the defaults, one knob at a time over its candidates with the others fixed,
-keeping a change only when it is at least 2 % faster. A configuration is timed by the CUDA events the
-solver records between its kernel groups (MPM_OPT_KERNEL_TIMING) over `substeps` substeps after 3 warm-up
-substeps. The solver's state is saved before and loaded back after, so tuning does not advance the bake
+keeping a change only when it is at least 2 % faster. A configuration is timed by CUDA events the solver
+records at the two ends of each substep (MPM_OPT_KERNEL_TIMING 2, so the kernels inside stay chained as
+untimed) over `substeps` substeps after 3 warm-up substeps. The solver's state is saved before and loaded back after, so tuning does not advance the bake
 (a load recomputes the stored stress from F, a last-bit change).
 
 Cache: JSON at $MPM_GB300_TUNE_CACHE or ~/.cache/mpm_plugin_gb300/autotune.json, keyed by the GPU (name,
@@ -106,11 +106,11 @@ def _time_solver(solver, cfg, sms, dt, frame_dt, substeps):
     apply(solver, cfg, sms)
     for _ in range(3):
         solver.substep(dt, 1.0, frame_dt)
-    solver.set_option(_abi.OPT_KERNEL_TIMING, 1)
-    solver.kernel_times(reset=True)
+    solver.set_option(_abi.OPT_KERNEL_TIMING, 2)  # events at the two ends of each substep
+    solver.substep_times(reset=True)
     for _ in range(substeps):
         solver.substep(dt, 1.0, frame_dt)
-    ms = sum(t for t, _ in solver.kernel_times(reset=True).values())
+    ms, _ = solver.substep_times(reset=True)
     solver.set_option(_abi.OPT_KERNEL_TIMING, 0)
     return ms / 1e3 / substeps
 

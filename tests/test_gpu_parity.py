@@ -423,3 +423,28 @@ def test_full_size_momentum_is_conserved_without_gravity_or_walls():
     assert c1["mass"] == c0["mass"]
     scale = c0["mass"] * 3.0  # total mass x the fastest initial speed
     assert np.linalg.norm(c1["momentum"] - c0["momentum"]) <= 1e-5 * scale, (c0["momentum"], c1["momentum"])
+
+
+def test_whole_substep_timing():
+    """MPM_OPT_KERNEL_TIMING 2 times whole substeps (events at the graph's two ends), 1 the kernel groups;
+    neither changes the physics."""
+    from mpm_plugin_gb300 import _abi
+
+    d = domain(res=32)
+    states, totals = [], []
+    for mode in (0, 1, 2):
+        s = gpu_solver(d, [preset("jelly")])
+        add(s, box_particles((0.4, 0.4, 0.3), (0.6, 0.6, 0.5), d.dx, seed=3))
+        s.set_option(_abi.OPT_KERNEL_TIMING, mode)
+        for _ in range(5):
+            s.substep(2e-4, 1.0, 1 / 24)
+        groups = s.kernel_times()
+        ms, count = s.substep_times(reset=True)  # (a reset clears both)
+        if mode == 2:
+            assert count == 5 and ms > 0 and all(c == 0 for _, c in groups.values())
+        if mode == 1:
+            assert count == 0 and groups["g2p"][1] == 5 and groups["p2g"][0] > 0
+        states.append(s.save_state())
+    for st in states[1:]:
+        for k in ("x", "v", "F"):
+            assert rel_err(st[k], states[0][k]) <= 1e-5
