@@ -425,13 +425,40 @@ def test_full_size_momentum_is_conserved_without_gravity_or_walls():
     assert np.linalg.norm(c1["momentum"] - c0["momentum"]) <= 1e-5 * scale, (c0["momentum"], c1["momentum"])
 
 
+def test_pour_size_momentum_is_conserved():
+    """The 256^3 pour's pile at its full size (7.45M particles, Drucker-Prager), lifted off the floor, gravity
+    off, no collider, with a seeded swirl of velocities: 20 substeps conserve mass exactly and momentum up to
+    float rounding (size-independent checks at the large workload's size)."""
+    from mpm_plugin_gb300.interface import MaterialParams
+    from mpm_plugin_gb300.solver import Gb300Solver
+    from scenes import lattice_box
+
+    d = domain(res=256)
+    mats = [MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)]
+    pile = lattice_box((0.2, 0.2, 0.2), (0.8, 0.8, 0.355), d.dx / 2, np.random.default_rng(3))
+    rng = np.random.default_rng(4)
+    c = pile.mean(0)
+    vel = (np.cross(np.float32([0.0, 0.0, 1.0]), pile - c) + rng.normal(0, 0.1, pile.shape)).astype(np.float32)
+    g = Gb300Solver(d, mats, (0.0, 0.0, 0.0), 8, device="cuda:0")
+    z = np.zeros(len(pile), np.int32)
+    g.add_particles(pile, vel, z, z)
+    assert g.particle_count > 7_000_000
+    c0 = g.conservation()
+    g.run_substeps(1e-4, 20)
+    c1 = g.conservation()
+    assert c1["mass"] == c0["mass"]
+    scale = c0["mass"] * float(np.abs(vel).max())
+    assert np.linalg.norm(c1["momentum"] - c0["momentum"]) <= 1e-5 * scale, (c0["momentum"], c1["momentum"])
+    g.close()
+
+
 def test_whole_substep_timing():
     """MPM_OPT_KERNEL_TIMING 2 times whole substeps (events at the graph's two ends), 1 the kernel groups;
     neither changes the physics."""
     from mpm_plugin_gb300 import _abi
 
     d = domain(res=32)
-    states, totals = [], []
+    states = []
     for mode in (0, 1, 2):
         s = gpu_solver(d, [preset("jelly")])
         add(s, box_particles((0.4, 0.4, 0.3), (0.6, 0.6, 0.5), d.dx, seed=3))
