@@ -586,6 +586,13 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
         for (int a = 0; a < 3; ++a) nx[a] = fminf(fmaxf(nx[a], g.clamp_lo[a]), g.clamp_hi[a]);
     }
     store_mat3(P.C, p, nC);
+    // x and v are final here: stored now, so their registers are free through the SVD
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        P.x[a][p] = nx[a];
+        P.v[a][p] = nv[a];
+        nx_out[a] = nx[a];
+    }
 
     float F[3][3], Fn[3][3];
     load_mat3(P.F, p, F);
@@ -643,13 +650,6 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     if (m.model == 3) P.Jp[p] = jp;
 #pragma unroll
     for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
-
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        P.x[a][p] = nx[a];
-        P.v[a][p] = nv[a];
-        nx_out[a] = nx[a];
-    }
 }
 
 // Grid nodes through the read-only data path (the grid is not written while a G2P kernel runs).
