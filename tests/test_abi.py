@@ -70,3 +70,29 @@ def test_create_without_gpu_reports_cuda_error():
     g = (ctypes.c_double * 3)(0, 0, -9.81)
     assert L.mpm_create(ctypes.byref(d), m, 1, g, 8, 0, ctypes.byref(h)) == _abi.MPM_ERR_NOT_IMPLEMENTED
     assert b"not supported" in L.mpm_last_error(None)
+
+
+def test_surfacer_entry_points_validate_before_the_device():
+    """Surfacer calls with a null surfacer or null outputs fail with an argument error; without a GPU the
+    creation fails with a CUDA error rather than crashing."""
+    import ctypes as C
+
+    from mpm_plugin_gb300 import _abi
+
+    lib = _abi.lib()
+    lo, hi = (C.c_float * 3)(), (C.c_float * 3)()
+    assert lib.mpm_surface_upload(None, 10, None, None, lo, hi) == _abi.MPM_ERR_ARGUMENT
+    nv, nt = C.c_int64(), C.c_int64()
+    o, d = (C.c_float * 3)(), (C.c_int32 * 3)(4, 4, 4)
+    assert lib.mpm_surface_build(None, o, d, 1.0, 1.0, 1.0, 1.0, 0.5, C.byref(nv), C.byref(nt)) == \
+        _abi.MPM_ERR_ARGUMENT
+    assert lib.mpm_surface_read(None, None, None, None) == _abi.MPM_ERR_ARGUMENT
+    assert lib.mpm_surface_destroy(None) == _abi.MPM_OK
+    assert lib.mpm_mc_table(None, None) == _abi.MPM_ERR_ARGUMENT
+    s = C.c_void_p()
+    import torch
+
+    if not torch.cuda.is_available():
+        assert lib.mpm_surface_create(0, C.byref(s)) == _abi.MPM_ERR_CUDA and not s.value
+    flag = C.c_int32()
+    assert lib.mpm_coop_barrier_selftest(None, 1, C.byref(flag)) == _abi.MPM_ERR_ARGUMENT
