@@ -137,11 +137,18 @@ enum {
     MPM_OPT_P2G_TILE = 10,     /* 1: P2G sums each CTA's contributions in shared-memory tiles of the nodes its
                                   particles touch, then adds them to the grid; 0 (default): warp segments
                                   (shuffle sums of same-cell lanes) only. Deterministic mode uses segments */
-    MPM_OPT_COOP = 11          /* substeps of mpm_advance / mpm_run_substeps in cooperative launches of up to 64
+    MPM_OPT_COOP = 11,         /* substeps of mpm_advance / mpm_run_substeps in cooperative launches of up to 64
                                   substeps each (the kernels' phases separated by grid-wide barriers): 0
                                   (default) never, 1 always (without kernel timing, the FP64 clamp or the tile
                                   P2G), 2 for scenes of up to 131,072 particles. Slower than the graphs of
                                   separate kernels on a GB300 at the sizes measured */
+    MPM_OPT_FUSED_P2G = 12     /* 1: two grids that alternate between substeps; G2P adds each particle it has
+                                  updated to the next substep's grid right away (and the collider projection
+                                  the particles it moved), so the next substep's P2G reads no particle state.
+                                  Within mpm_advance / mpm_run_substeps, and between mpm_substep calls with the
+                                  same dt (a scatter for a call that does not follow is dropped). Not in
+                                  deterministic mode, with the FP64 clamp or in a batch (those run one grid).
+                                  Costs a second grid of device memory. 0 (default) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

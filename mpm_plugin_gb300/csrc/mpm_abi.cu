@@ -98,6 +98,12 @@ struct Handle {
 
     float4* grid = nullptr;
     int64_t grid_nodes = 0;
+    // Two-grid mode (MPM_OPT_FUSED_P2G): the second grid, and the state of the grids on the device
+    float4* grid2 = nullptr;
+    bool fused_p2g = false;    // the option
+    bool two_live = false;     // the substeps so far ran in two-grid mode (lists and flags refer to both grids)
+    bool pending = false;      // the last explicit substep scattered into the next one's grid, for dt pending_dt
+    float pending_dt = 0.f;
     float* vol = nullptr;              // occupancy scratch, one float per node
 
     StepParams* d_sp = nullptr;
@@ -300,11 +306,37 @@ Status set_deterministic(Handle* h, bool on) {
     return {};
 }
 
+Status prepare_grids(Handle* h, bool two, bool keep_pending);
+
+// MPM_OPT_FUSED_P2G: the second grid is allocated on the way in and freed on the way out; the grids are
+// brought into the new mode before the next substep (prepare_grids).
+Status set_fused_p2g(Handle* h, bool on) {
+    if (on == h->fused_p2g) return {};
+    CK(cudaStreamSynchronize(h->stream));
+    invalidate_graph(h);  // the second grid is a kernel argument of the captured graphs
+    if (on && !h->grid2) {
+        if (cudaMalloc(&h->grid2, (size_t)h->grid_nodes * sizeof(float4)) != cudaSuccess) {
+            cudaGetLastError();
+            h->grid2 = nullptr;
+            return {MPM_ERR_MEMORY, "device allocation of the second grid failed"};
+        }
+        CK(cudaMemset(h->grid2, 0, (size_t)h->grid_nodes * sizeof(float4)));
+    }
+    h->fused_p2g = on;
+    if (!on) {
+        TRY(prepare_grids(h, false, false));  // before the second grid goes: nothing may refer to it
+        CK(cudaStreamSynchronize(h->stream));
+        cudaFree(h->grid2);
+        h->grid2 = nullptr;
+    }
+    return {};
+}
+
 // Device memory the handle holds now (the allocations it made, by their sizes).
 int64_t handle_device_bytes(const Handle* h) {
     const int64_t nblk = (int64_t)h->g.nb[0] * h->g.nb[1] * h->g.nb[2];
     int64_t b = (int64_t)h->P.cap * kFields * 4 * (h->spare_arena ? 2 : 1);
-    b += h->grid_nodes * 16 + (h->vol ? h->grid_nodes * 4 : 0) + (h->d_fixed ? h->grid_nodes * 36 : 0);
+    b += h->grid_nodes * (h->grid2 ? 32 : 16) + (h->vol ? h->grid_nodes * 4 : 0) + (h->d_fixed ? h->grid_nodes * 36 : 0);
     b += nblk * 12 + h->grid_nodes * 4 + h->part_cand_cap * 4 + 16;                      // work lists
     b += h->ss_cap * 12 + (h->grid_nodes + 1) * 8 + (h->ss_scan_cap + 2) * 4;           // sort
     b += h->keep_cap * 16 + (h->scan_cap + 2) * 4;                                       // removal
@@ -337,6 +369,32 @@ cudaEvent_t take_event(Handle* h) {
     return e;
 }
 
+// Two-grid mode for this handle's next substeps: the option, and neither deterministic mode (fixed-point
+// node sums) nor the FP64 clamp build (a G2P build of its own).
+bool two_grids(const Handle* h) {
+    return h->fused_p2g && h->grid2 && !h->deterministic && !h->fp64_clamp;
+}
+
+// Puts the grids into the state the next substeps expect. Nothing changes while the mode stays and a pending
+// scatter is kept; otherwise both grids, the block flags and the active lists start empty (a scatter made
+// for a substep that does not follow is dropped). Stream-ordered: no synchronisation.
+Status prepare_grids(Handle* h, bool two, bool keep_pending) {
+    if (two == h->two_live && (!h->pending || keep_pending)) return {};
+    const int64_t nblk = (int64_t)h->g.nb[0] * h->g.nb[1] * h->g.nb[2];
+    CK(cudaMemsetAsync(h->grid, 0, (size_t)h->grid_nodes * sizeof(float4), h->stream));
+    if (h->grid2) CK(cudaMemsetAsync(h->grid2, 0, (size_t)h->grid_nodes * sizeof(float4), h->stream));
+    CK(cudaMemsetAsync(h->wl.block_flag, 0, sizeof(unsigned int) * (size_t)nblk, h->stream));
+    CK(cudaMemsetAsync(h->wl.counts, 0, sizeof(unsigned int) * 2, h->stream));
+    h->two_live = two;
+    h->pending = false;
+    return {};
+}
+
+// Drops a scatter made for an explicit substep that may not follow (the particles are about to change).
+Status drop_pending(Handle* h) {
+    return h->pending ? prepare_grids(h, h->two_live, false) : Status{};
+}
+
 SubstepArgs substep_args(Handle* h) {
     SubstepArgs a{};
     a.arena = static_cast<float*>(h->arena);
@@ -346,6 +404,7 @@ SubstepArgs substep_args(Handle* h) {
     a.g = h->g;
     a.sp = h->d_sp;
     a.grid = h->grid;
+    a.grid2 = two_grids(h) ? h->grid2 : nullptr;
     a.fp64 = h->d_counters + 1;
     a.wl = h->wl;
     a.cd.cols = h->d_cols;
@@ -466,8 +525,9 @@ Status run_substep(Handle* h, int reps = 1) {
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
                                      (int64_t)h->shape.list_ctas,
-                                     (((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
-                                               2 + (h->fp64_clamp ? 1 : 0)) * 2 + h->shape.p2g_tile) * 64 + reps};
+                                     ((((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
+                                                2 + (h->fp64_clamp ? 1 : 0)) * 2 + h->shape.p2g_tile) * 2 +
+                                              (a.grid2 ? 1 : 0)) * 64 + reps};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -551,14 +611,17 @@ constexpr int64_t kCoopAutoMaxParticles = 131072;
 constexpr int kCoopMaxReps = 64;  // substeps per cooperative launch (a launch stays in the milliseconds)
 
 bool coop_eligible(const Handle* h, int count) {
-    if (h->coop == 0 || count < 2 || h->timing || !h->use_graph || h->fp64_clamp || h->shape.p2g_tile) return false;
+    if (h->coop == 0 || count < 2 || h->timing || !h->use_graph || h->fp64_clamp || h->shape.p2g_tile ||
+        two_grids(h))
+        return false;
     return h->coop == 1 || h->P.n <= kCoopAutoMaxParticles;
 }
 
 // reps substeps in one cooperative launch.
 Status run_coop(Handle* h, int reps) {
     TRY(ensure_part_cand(h));
-    const SubstepArgs a = substep_args(h);
+    SubstepArgs a = substep_args(h);
+    a.grid2 = nullptr;  // one grid (coop_eligible excludes two-grid mode)
     CK(launch_substeps_coop(h->stream, a, reps, h->d_coop));
     h->launches += 1;
     h->coop_used = true;
@@ -701,13 +764,17 @@ Status prepare_poses(Handle* h, int steps, double s, double frame_dt) {
     return {};
 }
 
-Status set_step(Handle* h, double dt, double s, double frame_dt, int steps) {
+// skip_first / speculate: StepParams (two-grid mode, explicit substeps).
+Status set_step(Handle* h, double dt, double s, double frame_dt, int steps, bool skip_first = false,
+                bool speculate = false) {
     StepParams sp{};
     sp.dt = (float)dt;
     sp.s = (float)s;
     sp.inv_frame_dt = (float)(1.0 / frame_dt);
     sp.k = -1;
     sp.steps = steps;
+    sp.skip_first = skip_first ? 1 : 0;
+    sp.speculate = speculate ? 1 : 0;
     // only the fields before `seq`: the substep counter keeps running across calls. A pageable source is
     // staged by the driver before this call returns, so `sp` may go out of scope.
     CK(cudaMemcpyAsync(h->d_sp, &sp, offsetof(StepParams, seq), cudaMemcpyHostToDevice, h->stream));
@@ -813,6 +880,7 @@ Status do_advance(Handle* h, double frame_dt, MpmAdvanceStats* stats) {
     int steps = 0;
     double dt = 0.0;
     choose_dt(h, h->h_counters[0], frame_dt, &dt, &steps);
+    TRY(prepare_grids(h, two_grids(h), false));
     TRY(set_step(h, dt, 0.0, frame_dt, steps));
     TRY(ensure_sdf(h));
     TRY(prepare_poses(h, steps, 0.0, frame_dt));
@@ -1048,6 +1116,7 @@ void destroy(Handle* h) {
     cudaFree(h->arena);
     cudaFree(h->spare_arena);
     cudaFree(h->grid);
+    cudaFree(h->grid2);
     cudaFree(h->vol);
     cudaFree(h->d_mats);
     cudaFree(h->d_sp);
@@ -1201,7 +1270,9 @@ Status batch_upload(Batch* b) {
     bool cols = false, clamp = false;
     for (int s = 0; s < n; ++s) {
         Handle* h = b->live[s];
+        TRY(prepare_grids(h, false, false));  // a batch runs its scenes in one-grid mode
         table[s] = substep_args(h);
+        table[s].grid2 = nullptr;
         table[s].p2g_group = b->shape.p2g_group;
         layout.push_back(h->P.cap);
         ctas += (h->P.cap + 255) / 256;
@@ -1429,6 +1500,7 @@ int mpm_add_particles(void* handle, int64_t n, const float* x, const float* v, c
     if (n < 0 || !x || !v || !material_ids || !emitter_ids) return finish(h, {MPM_ERR_ARGUMENT, "bad particle arrays"});
     auto run = [&]() -> Status {
         TRY(check_mats(h, n, material_ids));
+        TRY(drop_pending(h));
         TRY(ensure_capacity(h, h->P.n + n));
         TRY(upload_particles(h, h->P.n, n, x, v, nullptr, nullptr, nullptr, material_ids, emitter_ids));
         CK(cudaStreamSynchronize(h->stream));
@@ -1462,10 +1534,18 @@ int mpm_substep(void* handle, double dt, double s, double frame_dt) {
     auto run = [&]() -> Status {
         if (h->P.n == 0) return {};
         h->frame_dt = frame_dt;
-        TRY(set_step(h, dt, s, frame_dt, 0));
+        // two-grid mode: the previous explicit substep scattered for this one if it had the same dt; this
+        // one scatters for the next in turn (dropped if the next call is not a substep with this dt)
+        const bool two = two_grids(h);
+        const bool keep = two && h->two_live && h->pending && (float)dt == h->pending_dt;
+        TRY(prepare_grids(h, two, keep));
+        TRY(set_step(h, dt, s, frame_dt, 0, keep, two));
         TRY(ensure_sdf(h));
         TRY(prepare_poses(h, 0, s, frame_dt));
-        return substep_and_sort(h);
+        TRY(substep_and_sort(h));
+        h->pending = two;
+        h->pending_dt = (float)dt;
+        return {};
     };
     return finish(h, run());
 }
@@ -1490,6 +1570,7 @@ int mpm_run_substeps(void* handle, double dt, int32_t count, double frame_dt) {
     auto run = [&]() -> Status {
         if (h->P.n == 0 || count == 0) return {};
         h->frame_dt = frame_dt;
+        TRY(prepare_grids(h, two_grids(h), false));
         TRY(set_step(h, dt, 0.0, frame_dt, count));
         TRY(ensure_sdf(h));
         TRY(prepare_poses(h, count, 0.0, frame_dt));
@@ -1525,6 +1606,7 @@ int mpm_load_state(void* handle, int64_t n, const float* x, const float* v, cons
         return finish(h, {MPM_ERR_ARGUMENT, "bad state arrays"});
     auto run = [&]() -> Status {
         TRY(check_mats(h, n, mat));
+        TRY(drop_pending(h));
         CK(cudaStreamSynchronize(h->stream));
         h->P.n = 0;
         TRY(ensure_capacity(h, n));
@@ -1618,6 +1700,8 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             h->sort_interval = (int)value;
             h->since_sort = 0;
             return MPM_OK;
+        case MPM_OPT_FUSED_P2G:
+            return finish(h, set_fused_p2g(h, value != 0));
         default:
             return finish(h, {MPM_ERR_VALUE, "unknown option"});
     }
@@ -1668,7 +1752,14 @@ int mpm_read_grid(void* handle, float* out) {
     auto run = [&]() -> Status {
         size_t bytes = (size_t)h->dims[0] * h->dims[1] * h->dims[2] * sizeof(float4);
         TRY(ensure_stage(h, bytes));
-        launch_grid_unblock(h->stream, h->g, h->grid, static_cast<float4*>(h->stage));
+        const float4* grid = h->grid;
+        if (h->two_live) {  // the grid of the last substep
+            StepParams sp;
+            CK(cudaMemcpyAsync(&sp, h->d_sp, sizeof sp, cudaMemcpyDeviceToHost, h->stream));
+            CK(cudaStreamSynchronize(h->stream));
+            if (sp.seq & 1u) grid = h->grid2;
+        }
+        launch_grid_unblock(h->stream, h->g, grid, static_cast<float4*>(h->stage));
         CK(cudaGetLastError());
         CK(cudaMemcpyAsync(out, h->stage, bytes, cudaMemcpyDeviceToHost, h->stream));
         CK(cudaStreamSynchronize(h->stream));

@@ -471,7 +471,11 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
     if (a.cd.n_col > 0) launch_step_kernel(k_grid_colliders<OneScene>, list_ctas, 128, st, pdl, sc);
     mark(3);
     if (a.n > 0) {
-        if (a.fp64_clamp)
+        if (a.grid2 && shape.g2p_variant == 1)  // two-grid mode (never with the FP64 clamp build)
+            launch_step_kernel(k_g2p<OneScene, 1, false, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
+        else if (a.grid2)
+            launch_step_kernel(k_g2p<OneScene, 3, false, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
+        else if (a.fp64_clamp)
             launch_step_kernel(k_g2p<OneScene, 1, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
         else if (shape.g2p_variant == 1)
             launch_step_kernel(k_g2p<OneScene, 1>, blocks_for(a.n, 256), 256, st, pdl, sc);

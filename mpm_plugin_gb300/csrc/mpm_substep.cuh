@@ -218,6 +218,29 @@ struct GlobalFields {
     MPM_HD int mat() const { return P.mat[p]; }
 };
 
+// A value this thread stored earlier in the same kernel, read again from L2 (so the compiler does not keep
+// the stored value live in a register across the code in between).
+MPM_HD float reload(const float* addr) {
+#ifdef __CUDA_ARCH__
+    return __ldcg(addr);
+#else
+    return *addr;
+#endif
+}
+
+// The fields of a particle G2P has just written, for the scatter into the next substep's grid: x, v and C
+// read back, the stress from the registers it was computed in.
+struct ScatterFields {
+    const Particles& P;
+    int64_t p;
+    const float* t;
+    MPM_HD float x(int a) const { return reload(&P.x[a][p]); }
+    MPM_HD float v(int a) const { return reload(&P.v[a][p]); }
+    MPM_HD float C(int e) const { return reload(&P.C[e][p]); }
+    MPM_HD float tau(int e) const { return t[e]; }
+    MPM_HD int mat() const { return P.mat[p]; }
+};
+
 // False when the stencil leaves the grid (the particle scatters nothing).
 template <class Fields>
 MPM_HD bool p2g_terms_of(const Fields& f, const Material* __restrict__ mats, const GridDesc& g, float dt, P2gTerms& t) {
@@ -506,12 +529,12 @@ MPM_HD void plastic_redo_fp64(const Particles& P, int64_t p, const Material& m, 
 }
 
 // G2P of one particle gathering node velocities from `src` (src(node index) -> float4); the new position goes
-// to nx_out. kFp64Clamp builds in the FP64 redo at an active Drucker-Prager or snow clamp, taken where
-// fp64_clamp is set.
+// to nx_out and, when tau_out is given, the stress stored for the next P2G to tau_out as well. kFp64Clamp
+// builds in the FP64 redo at an active Drucker-Prager or snow clamp, taken where fp64_clamp is set.
 template <class Source, bool kFp64Clamp = false>
 MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
                               float dt, const Source& src, unsigned int* fp64, float nx_out[3],
-                              bool fp64_clamp = false) {
+                              bool fp64_clamp = false, float* tau_out = nullptr) {
     // F, Jp and mat are read after the gather and the C store; their lines are requested now so that the
     // memory latency overlaps the gather
 #pragma unroll
@@ -649,7 +672,10 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     store_mat3(P.F, p, Fn);
     if (m.model == 3) P.Jp[p] = jp;
 #pragma unroll
-    for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
+    for (int e = 0; e < 6; ++e) {
+        P.tau[e][p] = t[e];
+        if (tau_out) tau_out[e] = t[e];
+    }
 }
 
 // Grid nodes through the read-only data path (the grid is not written while a G2P kernel runs).
@@ -675,9 +701,10 @@ struct CoherentSource {
 
 template <bool kFp64Clamp = false, class Source = GlobalSource>
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         const float4* grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false) {
+                         const float4* grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false,
+                         float* tau_out = nullptr) {
     Source src{&g, grid};
-    g2p_particle_from<Source, kFp64Clamp>(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp);
+    g2p_particle_from<Source, kFp64Clamp>(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp, tau_out);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

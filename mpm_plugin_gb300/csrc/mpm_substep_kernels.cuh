@@ -5,6 +5,17 @@
 //                 all scenes, and a scene whose advance is done (StepParams::active == 0) is skipped by all.
 // One substep = step_begin -> clear -> P2G -> grid update -> collider contact -> G2P -> particle projection
 // (warp/solver.py:187-212 for the order).
+//
+// Two-grid mode (SubstepArgs::grid2 set; one scene, not in deterministic mode): substep seq uses grid
+// grid_of(seq & 1) and active list seq & 1. Within an advance (or between explicit substeps with the same dt)
+// the G2P of substep seq also scatters every particle it has just updated into the grid of substep seq + 1,
+// and the projection kernel scatters the particles it projected, so the P2G kernel of seq + 1 has nothing
+// left to do (StepParams::p2g_skip). The bookkeeping that makes this hold:
+//   clear(seq)        zeroes the blocks of list (seq - 1) & 1 in grid (seq - 1) & 1 = the grid G2P(seq) fills;
+//   grid update(seq)  empties list (seq + 1) & 1 (cleared above, read by nobody after the clear) and takes the
+//                     block flags of list seq & 1 down, so G2P(seq) can list the blocks it scatters into;
+//   step begin(seq)   empties list seq & 1 only when P2G(seq) will fill it.
+// The host discards a scatter made for a substep that does not follow (zero grids, flags and lists).
 #pragma once
 
 #include <climits>
@@ -104,7 +115,8 @@ __device__ __forceinline__ int scene_of_item(const unsigned int* off, int S, uns
 // the work lists of this substep start empty. A scene that has run all `steps` substeps of its advance
 // goes idle (active = 0) and keeps its counters, so its next advance continues where it stopped.
 // ------------------------------------------------------------------------------------------------------
-__device__ __forceinline__ void step_begin(StepParams* sp, unsigned int* counts, int n_col) {
+// two: two-grid mode (the substep's G2P may scatter for the next substep, see the top of this file).
+__device__ __forceinline__ void step_begin(StepParams* sp, unsigned int* counts, int n_col, bool two) {
     StepParams p = *sp;
     if (p.steps > 0 && p.k + 1 >= p.steps) {
         sp->active = 0;
@@ -119,8 +131,11 @@ __device__ __forceinline__ void step_begin(StepParams* sp, unsigned int* counts,
     } else {
         p.pose_base = 0;
     }
+    // within an advance the next substep has the same dt; an explicit substep scatters on the host's word
+    p.p2g_skip = two && (p.steps > 0 ? p.k > 0 : p.skip_first != 0);
+    p.scatter = two && (p.steps > 0 ? p.k + 1 < p.steps : p.speculate != 0);
     *sp = p;
-    counts[p.seq & 1u] = 0u;
+    if (!p.p2g_skip) counts[p.seq & 1u] = 0u;
     counts[2] = 0u;
     counts[3] = 0u;
 }
@@ -130,7 +145,7 @@ __global__ void k_step_begin(Scenes sc) {
     pdl_begin();
     for (int s = threadIdx.x; s < sc.count(); s += blockDim.x) {
         const SubstepArgs a = sc.get(s);
-        step_begin(a.sp, a.wl.counts, a.cd.n_col);
+        step_begin(a.sp, a.wl.counts, a.cd.n_col, a.grid2 != nullptr);
     }
 }
 
@@ -140,7 +155,7 @@ __device__ __forceinline__ void clear_block(const SubstepArgs& a, unsigned int i
     const unsigned int prev = (a.sp->seq - 1u) & 1u;
     const int64_t b = active_blocks(a.wl, prev)[i];
     const int64_t q = b * 64 + (threadIdx.x & 63);
-    a.grid[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    grid_of(a, prev)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (a.fixed) {
         reinterpret_cast<ulonglong2*>(a.fixed)[2 * q] = make_ulonglong2(0ull, 0ull);
         reinterpret_cast<ulonglong2*>(a.fixed)[2 * q + 1] = make_ulonglong2(0ull, 0ull);
@@ -216,8 +231,8 @@ __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
 // lane holds the sum of the next 2^r lanes of its segment); the segment's first lane adds each node's sums to
 // the grid. kRounds is fixed per warp, so the rounds carry no per-node branches.
 template <int kRounds>
-__device__ __forceinline__ void p2g_segment_sums(const SubstepArgs& a, const P2gTerms& t, bool valid, bool leader,
-                                                 int tail, const StencilIndex& at) {
+__device__ __forceinline__ void p2g_segment_sums(float4* grid, const P2gTerms& t, bool valid, bool leader, int tail,
+                                                 const StencilIndex& at) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -235,7 +250,7 @@ __device__ __forceinline__ void p2g_segment_sums(const SubstepArgs& a, const P2g
                         if (d <= tail) val[c] += o;
                     }
                 }
-                if (leader) grid_add(&a.grid[at(i, j, k)], val[0], val[1], val[2], val[3]);
+                if (leader) grid_add(&grid[at(i, j, k)], val[0], val[1], val[2], val[3]);
             }
 }
 
@@ -246,7 +261,9 @@ __device__ __forceinline__ void p2g_segment_sums(const SubstepArgs& a, const P2g
 // reduction per node instead of eight. Runs are also cut at aligned groups of p2g_group lanes: fewer shuffle
 // rounds for more reductions (the autotuner picks the group). Lanes past the end or with a stencil outside
 // the grid are single-lane segments that add nothing. The segment's first lane lists the blocks it touches.
-__device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, const P2gTerms& t, bool valid) {
+// grid / parity: the grid and the active list scattered into. All 32 lanes of the warp take part.
+__device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* grid, unsigned int parity,
+                                                  const P2gTerms& t, bool valid) {
     const int lane = (int)(threadIdx.x & 31u);
     const GridDesc& g = a.g;
     const int64_t key = valid ? node_index(g, t.base[0], t.base[1], t.base[2]) : -1 - (int64_t)lane;
@@ -259,10 +276,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, const P2
     const int tail = __ffs(ends >> lane) - 1;  // lanes after this one in its segment
     const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned int)tail);
     const bool leader = valid && seg_first;
-    if (leader) {
-        const unsigned int cur = a.sp->seq & 1u;
-        mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, cur), &a.wl.counts[cur]);
-    }
+    if (leader) mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, parity), &a.wl.counts[parity]);
     if (a.fixed) {
         p2g_fixed_warp(a, t, valid, leader, tail, span);
         return;
@@ -271,15 +285,15 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, const P2
     // shuffle rounds needed by the longest segment of the warp: 0, 1, 2, 3 or 5 (4 takes 5)
     const int rounds = span == 0 ? 0 : 32 - __clz(span);
     if (rounds == 0)
-        p2g_segment_sums<0>(a, t, valid, leader, tail, at);
+        p2g_segment_sums<0>(grid, t, valid, leader, tail, at);
     else if (rounds == 1)
-        p2g_segment_sums<1>(a, t, valid, leader, tail, at);
+        p2g_segment_sums<1>(grid, t, valid, leader, tail, at);
     else if (rounds == 2)
-        p2g_segment_sums<2>(a, t, valid, leader, tail, at);
+        p2g_segment_sums<2>(grid, t, valid, leader, tail, at);
     else if (rounds == 3)
-        p2g_segment_sums<3>(a, t, valid, leader, tail, at);
+        p2g_segment_sums<3>(grid, t, valid, leader, tail, at);
     else
-        p2g_segment_sums<5>(a, t, valid, leader, tail, at);
+        p2g_segment_sums<5>(grid, t, valid, leader, tail, at);
 }
 
 // P2G of the 256 particles from `first` (one CTA's share; the warps past the end return).
@@ -289,7 +303,8 @@ __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     const Particles P = particles_of(a);
     P2gTerms t;
     const bool valid = p < a.n && p2g_terms(P, p, a.mats, a.g, a.sp->dt, t);
-    p2g_warp_segments(a, t, valid);
+    const unsigned int cur = a.sp->seq & 1u;
+    p2g_warp_segments(a, grid_of(a, cur), cur, t, valid);
 }
 
 // Five CTAs of 256 per SM (48 registers, a few spilled values): the warps it adds hide more of P2G's memory
@@ -299,7 +314,7 @@ __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
     pdl_begin();
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
-    if (!sc.active(a)) return;
+    if (!sc.active(a) || a.sp->p2g_skip) return;
     p2g_cta(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
 }
 
@@ -324,7 +339,7 @@ __global__ void __launch_bounds__(256) k_p2g_tile(Scenes sc) {
     __shared__ int box[6];             // min x, y, z and max x, y, z of the stencil bases
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
-    if (!sc.active(a)) return;
+    if (!sc.active(a) || a.sp->p2g_skip) return;
     const int64_t first = (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x;
     if (first >= a.n) return;  // CTA-uniform
     const int tid = (int)threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -349,8 +364,10 @@ __global__ void __launch_bounds__(256) k_p2g_tile(Scenes sc) {
     if (lo0 > box[3]) return;  // no particle of the CTA scatters (CTA-uniform)
     const int e1 = box[4] - lo1 + 3, e2 = box[5] - lo2 + 3;
     const int nodes = (box[3] - lo0 + 3) * e1 * e2;
+    const unsigned int cur = a.sp->seq & 1u;
+    float4* grid = grid_of(a, cur);
     if (a.fixed || nodes > kP2gTileNodes) {  // CTA-uniform
-        p2g_warp_segments(a, t, valid);
+        p2g_warp_segments(a, grid, cur, t, valid);
         return;
     }
     for (int q = tid; q < 8 * nodes; q += 256) tiles[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -382,7 +399,6 @@ __global__ void __launch_bounds__(256) k_p2g_tile(Scenes sc) {
                 }
             }
     __syncthreads();
-    const unsigned int cur = a.sp->seq & 1u;
     for (int q = tid; q < nodes; q += 256) {
         float4 v = tiles[q];
 #pragma unroll
@@ -396,7 +412,7 @@ __global__ void __launch_bounds__(256) k_p2g_tile(Scenes sc) {
         if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {  // true for NaN too
             const int qk = q % e2, qij = q / e2;
             const int64_t node = node_index(g, lo0 + qij / e1, lo1 + qij % e1, lo2 + qk);
-            grid_add(&a.grid[node], v.x, v.y, v.z, v.w);
+            grid_add(&grid[node], v.x, v.y, v.z, v.w);
             mark_block(node >> 6, a.wl.block_flag, active_blocks(a.wl, cur), &a.wl.counts[cur]);
         }
     }
@@ -413,6 +429,8 @@ __device__ __forceinline__ void grid_update_block(const SubstepArgs& a, unsigned
     const int bj = (int)((b / g.nb[2]) % g.nb[1]);
     const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
     const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
+    float4* grid = grid_of(a, cur);
+    if (a.grid2 && l == 0) a.wl.block_flag[b] = 0u;  // two-grid mode: this substep's G2P lists blocks anew
     if (a.fixed) {  // deterministic mode: the node's fixed-point sums become its float momentum and mass
         const int64_t q = b * 64 + l;
         const ulonglong2 f01 = reinterpret_cast<const ulonglong2*>(a.fixed)[2 * q];
@@ -422,9 +440,9 @@ __device__ __forceinline__ void grid_update_block(const SubstepArgs& a, unsigned
                                (float)((double)(long long)f23.x * inv), (float)((double)(long long)f23.y * inv));
         if (a.poison[q]) v = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
                                          __int_as_float(0x7fc00000), v.w);
-        a.grid[q] = v;
+        grid[q] = v;
     }
-    bool has_mass = grid_node_walls(g, &a.grid[b * 64 + l], idx, a.sp->dt);
+    bool has_mass = grid_node_walls(g, &grid[b * 64 + l], idx, a.sp->dt);
     if (has_mass && a.cd.n_col > 0) {
         ColliderData cd = a.cd;
         cd.poses += a.sp->pose_base;
@@ -440,9 +458,11 @@ __global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[a.sp->seq & 1u];
+        // two-grid mode: the list G2P fills (its blocks were cleared by this substep's clear kernel)
+        if (a.grid2 && blockIdx.x == 0 && threadIdx.x == 0) a.wl.counts[(a.sp->seq + 1u) & 1u] = 0u;
         for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u)
             grid_update_block(a, i);
-    } else {
+    } else {  // (a batch runs its scenes in one-grid mode)
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total =
             scene_offsets(sc, [](const SubstepArgs& a) { return a.wl.counts[a.sp->seq & 1u]; }, off);
@@ -472,7 +492,7 @@ __device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigne
     const int bj = (int)((b / g.nb[2]) % g.nb[1]);
     const int bi = (int)(b / ((int64_t)g.nb[2] * g.nb[1]));
     const int idx[3] = {bi * 4 + (l >> 4), bj * 4 + ((l >> 2) & 3), bk * 4 + (l & 3)};
-    grid_node_colliders<kWarp>(g, &a.grid[q], idx, cd);
+    grid_node_colliders<kWarp>(g, &grid_of(a, a.sp->seq & 1u)[q], idx, cd);
 }
 
 template <class Scenes>
@@ -513,35 +533,73 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
 // Caps of 128 and 64 registers were slower on the mixed and the 256^3 workloads (measured on a GB300). Both
 // builds are kept; the autotuner picks one per workload. kFp64Clamp: the build with the FP64 redo at the
 // Drucker-Prager and snow clamp (MPM_OPT_FP64_CLAMP), launched only when a scene has the option set.
-template <bool kFp64Clamp = false, class Source = GlobalSource>
+// kScatter: the two-grid build. Where the substep scatters (StepParams::scatter), each warp then adds its
+// particles to the next substep's grid, as k_p2g_scatter would at the start of that substep, from the
+// values just computed (x, v and C read back from L2, the stress from registers): P2G without reading the
+// particle state from memory again. Particles listed for the projection kernel are left to it (it scatters
+// them once projected).
+template <bool kFp64Clamp = false, class Source = GlobalSource, bool kScatter = false>
 __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
     const int64_t p = first + threadIdx.x;
-    if (p >= a.n) return;
-    float nx[3];
-    g2p_particle<kFp64Clamp, Source>(particles_of(a), p, a.mats, a.g, a.sp->dt, a.grid, a.fp64, nx,
-                                     a.fp64_clamp != 0);
-    if (a.cd.n_col > 0) {
-        ColliderData cd = a.cd;
-        cd.poses += a.sp->pose_base;
-        if (near_any_collider(nx, cd)) warp_append(a.wl.part_cand, &a.wl.counts[3], (int32_t)p);
+    const unsigned int cur = a.sp->seq & 1u;
+    if constexpr (!kScatter) {
+        if (p >= a.n) return;
+        float nx[3];
+        g2p_particle<kFp64Clamp, Source>(particles_of(a), p, a.mats, a.g, a.sp->dt, grid_of(a, cur), a.fp64, nx,
+                                         a.fp64_clamp != 0);
+        if (a.cd.n_col > 0) {
+            ColliderData cd = a.cd;
+            cd.poses += a.sp->pose_base;
+            if (near_any_collider(nx, cd)) warp_append(a.wl.part_cand, &a.wl.counts[3], (int32_t)p);
+        }
+    } else {
+        if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end; the others stay whole
+        const Particles P = particles_of(a);
+        const bool live = p < a.n;
+        float nx[3], tau[6];
+        bool listed = false;
+        if (live) {
+            g2p_particle<kFp64Clamp, Source>(P, p, a.mats, a.g, a.sp->dt, grid_of(a, cur), a.fp64, nx,
+                                             a.fp64_clamp != 0, tau);
+            if (a.cd.n_col > 0) {
+                ColliderData cd = a.cd;
+                cd.poses += a.sp->pose_base;
+                listed = near_any_collider(nx, cd);
+                if (listed) warp_append(a.wl.part_cand, &a.wl.counts[3], (int32_t)p);
+            }
+        }
+        if (a.sp->scatter) {  // the same for the whole scene
+            P2gTerms t;
+            const bool valid = live && !listed && p2g_terms_of(ScatterFields{P, p, tau}, a.mats, a.g, a.sp->dt, t);
+            const unsigned int next = cur ^ 1u;
+            p2g_warp_segments(a, grid_of(a, next), next, t, valid);
+        }
     }
 }
 
-template <class Scenes, int kMinCtas, bool kFp64Clamp = false>
+template <class Scenes, int kMinCtas, bool kFp64Clamp = false, bool kScatter = false>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     pdl_begin();
     const int s = sc.scene_of_cta(blockIdx.x);
     const SubstepArgs a = sc.get(s);
     if (!sc.active(a)) return;
-    g2p_cta<kFp64Clamp>(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
+    g2p_cta<kFp64Clamp, GlobalSource, kScatter>(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
 }
 
-// Projection of one listed particle (the same two shapes as for the nodes).
+// Projection of one listed particle (the same two shapes as for the nodes); where the substep scatters for
+// the next one (two-grid mode), the lane that stored the particle then adds it to the next substep's grid.
 template <bool kWarp>
 __device__ __forceinline__ void project_candidate(const SubstepArgs& a, unsigned int i) {
     ColliderData cd = a.cd;
     cd.poses += a.sp->pose_base;
-    project_particle<kWarp>(particles_of(a), a.wl.part_cand[i], a.g, cd);
+    const Particles P = particles_of(a);
+    const int64_t p = a.wl.part_cand[i];
+    project_particle<kWarp>(P, p, a.g, cd);
+    if (a.sp->scatter && stores_result<kWarp>()) {
+        const unsigned int next = (a.sp->seq + 1u) & 1u;
+        p2g_particle(P, p, a.mats, a.g, a.sp->dt, grid_of(a, next), a.wl.block_flag, active_blocks(a.wl, next),
+                     &a.wl.counts[next]);
+    }
 }
 
 template <class Scenes>
@@ -621,7 +679,7 @@ __global__ void __launch_bounds__(256, kMinCtas) k_substeps_coop(OneScene sc, in
     const unsigned int warp = tid >> 5, warps = threads >> 5;
     const int64_t pctas = (a.n + 255) / 256;
     for (int r = 0; r < reps; ++r) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) step_begin(a.sp, a.wl.counts, a.cd.n_col);
+        if (blockIdx.x == 0 && threadIdx.x == 0) step_begin(a.sp, a.wl.counts, a.cd.n_col, false);
         if (!grid_barrier(bar, err)) return;
         {
             const unsigned int n = a.wl.counts[(a.sp->seq - 1u) & 1u];

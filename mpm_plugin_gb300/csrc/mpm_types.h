@@ -113,9 +113,15 @@ struct StepParams {
     float s;             // fraction of the advance at the end of this substep, (k + 1) / steps
     float inv_frame_dt;  // 1 / duration of the current advance call
     int k, steps;        // substep index within the advance; steps == 0 for a single explicit substep
+    // Two-grid mode, single explicit substeps (set by the host with the fields above):
+    int skip_first;      // 1: this substep's grid already holds the scatter of the G2P before it (same dt)
+    int speculate;       // 1: this substep's G2P scatters for a next explicit substep with the same dt
     unsigned int seq;    // substeps run so far on this handle (selects the active-block list in use)
     int pose_base;       // first pose of this substep in the pose array
     int active;          // 1 while this scene has a substep to run (a batch idles scenes whose advance is done)
+    // Two-grid mode, set per substep by the step-begin kernel:
+    int p2g_skip;        // 1: the G2P before this substep scattered into this substep's grid; P2G does nothing
+    int scatter;         // 1: this substep's G2P (and projection) scatter into the next substep's grid
 };
 
 // Work lists the substep builds on the device. Active blocks are the 4x4x4 grid blocks P2G touched;
@@ -157,6 +163,10 @@ struct SubstepArgs {
     GridDesc g;
     StepParams* sp;
     float4* grid;
+    // Two-grid mode (null: one grid). Substeps alternate between grid (even seq) and grid2 (odd seq), so one
+    // substep's G2P can gather from its own grid while it scatters each particle into the next substep's grid
+    // (P2G fused into G2P: the particle state is not read again). Never set together with `fixed`.
+    float4* grid2;
     unsigned int* fp64;
     WorkLists wl;
     ColliderData cd;  // poses: the start of the pose array; kernels add the substep's pose_base
@@ -191,6 +201,11 @@ __host__ __device__ __forceinline__ Particles make_particles(float* arena, int64
 
 __host__ __device__ __forceinline__ Particles particles_of(const SubstepArgs& a) {
     return make_particles(a.arena, a.cap, a.n);
+}
+
+// The grid of the substeps whose seq has this parity (the one grid outside two-grid mode).
+__host__ __device__ __forceinline__ float4* grid_of(const SubstepArgs& a, unsigned int parity) {
+    return (parity && a.grid2) ? a.grid2 : a.grid;
 }
 
 }  // namespace mpm

@@ -6,7 +6,9 @@ Knobs (C options of include/mpm_gb300.h):
   g2p_variant        G2P build: 0 capped at 80 registers (3 CTAs of 256 per SM), 1 uncapped;
   list_ctas_per_sm   CTAs per SM of the kernels that walk the active-block and candidate lists;
   p2g_group          P2G sums same-cell lanes within aligned groups of this many lanes (1 .. 32);
-  pdl                programmatic dependent launch of the substep kernels (1) or plain stream order (0).
+  pdl                programmatic dependent launch of the substep kernels (1) or plain stream order (0);
+  fused_p2g          (a solver, outside deterministic mode) two grids, G2P scattering each particle into the
+                     next substep's grid (1), or P2G on its own at the start of every substep (0).
 
 The shared-memory tile P2G (MPM_OPT_P2G_TILE) is not searched: it was slower than the warp segments on the
 unsorted mixed workload and on the 256^3 pour, and in a short tuning window it could look faster.
@@ -36,6 +38,10 @@ CANDIDATES = {"sort_interval": (0, 2, 4, 8, 16), "g2p_variant": (0, 1), "list_ct
               "p2g_group": (1, 4, 8, 32), "pdl": (0, 1)}
 KNOB_ORDER = ("g2p_variant", "sort_interval", "p2g_group", "list_ctas_per_sm", "pdl")
 MIN_GAIN = 0.02
+# a single solver also chooses between the one- and two-grid substeps, first (the other knobs then suit it)
+SOLVER_DEFAULTS = {**DEFAULTS, "fused_p2g": 0}
+SOLVER_CANDIDATES = {**CANDIDATES, "fused_p2g": (0, 1)}
+SOLVER_ORDER = ("fused_p2g",) + KNOB_ORDER
 
 
 def cache_path() -> Path:
@@ -80,6 +86,8 @@ def apply(target, cfg: dict, sms: int) -> None:
     target.set_option(_abi.OPT_P2G_GROUP, int(cfg.get("p2g_group", 32)))
     target.set_option(_abi.OPT_PDL, int(cfg.get("pdl", 1)))
     target.set_option(_abi.OPT_P2G_TILE, int(cfg.get("p2g_tile", 0)))
+    if "fused_p2g" in cfg:  # solvers only
+        target.set_option(_abi.OPT_FUSED_P2G, int(cfg["fused_p2g"]))
 
 
 def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, min_gain=MIN_GAIN):
@@ -127,7 +135,11 @@ def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20,
         apply(solver, hit, sms)
         return {**hit, "cached": True}
     snapshot = solver.save_state()
-    best, best_t, trials = search(lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps))
+    measure = lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps)  # noqa: E731
+    if deterministic:  # one grid whatever fused_p2g says: that knob is not searched (nor set) there
+        best, best_t, trials = search(measure)
+    else:
+        best, best_t, trials = search(measure, SOLVER_CANDIDATES, SOLVER_DEFAULTS, SOLVER_ORDER)
     solver.load_state(snapshot)
     apply(solver, best, sms)
     cache.setdefault(gkey, {})[wkey] = best
