@@ -150,9 +150,8 @@ __global__ void k_step_begin(Scenes sc) {
 }
 
 // Zeroes the grid blocks the previous substep used (and their flags), so the whole grid is zero again.
-// Four blocks per 256-thread CTA.
-__device__ __forceinline__ void clear_block(const SubstepArgs& a, unsigned int i) {
-    const unsigned int prev = (a.sp->seq - 1u) & 1u;
+// Four blocks per 256-thread CTA. prev: the previous substep's parity.
+__device__ __forceinline__ void clear_block(const SubstepArgs& a, unsigned int prev, unsigned int i) {
     const int64_t b = active_blocks(a.wl, prev)[i];
     const int64_t q = b * 64 + (threadIdx.x & 63);
     grid_of(a, prev)[q] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -208,13 +207,26 @@ __device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTe
     }
 }
 
+// One scene: the clear runs first in the substep and its last CTA to finish begins the substep (step_begin),
+// so there is no step-begin kernel in the launch chain. Every CTA reads seq before any CTA can advance it (a
+// CTA counts itself done only after its reads), so all clear the list of the substep before. The done-counter
+// (counts[4]) is reset by that last CTA; nothing waits on it. A batch runs k_step_begin first, then this.
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
-        const unsigned int n = a.wl.counts[(a.sp->seq - 1u) & 1u];
-        for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) clear_block(a, i);
+        const unsigned int prev = a.sp->seq & 1u;  // not yet advanced: the parity of the substep before
+        const unsigned int n = a.wl.counts[prev];
+        for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) clear_block(a, prev, i);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&a.wl.counts[4], 1u) == gridDim.x - 1u) {
+                a.wl.counts[4] = 0u;
+                step_begin(a.sp, a.wl.counts, a.cd.n_col, a.grid2 != nullptr);
+            }
+        }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
@@ -222,7 +234,8 @@ __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
         }, off);
         for (unsigned int q = blockIdx.x * 4u + (threadIdx.x >> 6); q < total; q += gridDim.x * 4u) {
             const int s = scene_of_item(off, sc.count(), q);
-            clear_block(sc.get(s), q - off[s]);
+            const SubstepArgs a = sc.get(s);
+            clear_block(a, (a.sp->seq - 1u) & 1u, q - off[s]);
         }
     }
 }
@@ -682,8 +695,10 @@ __global__ void __launch_bounds__(256, kMinCtas) k_substeps_coop(OneScene sc, in
         if (blockIdx.x == 0 && threadIdx.x == 0) step_begin(a.sp, a.wl.counts, a.cd.n_col, false);
         if (!grid_barrier(bar, err)) return;
         {
-            const unsigned int n = a.wl.counts[(a.sp->seq - 1u) & 1u];
-            for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += ncta * 4u) clear_block(a, i);
+            const unsigned int prev = (a.sp->seq - 1u) & 1u;
+            const unsigned int n = a.wl.counts[prev];
+            for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += ncta * 4u)
+                clear_block(a, prev, i);
         }
         if (!grid_barrier(bar, err)) return;
         for (int64_t c = blockIdx.x; c < pctas; c += ncta) p2g_cta(a, c * 256);
