@@ -337,7 +337,7 @@ int64_t handle_device_bytes(const Handle* h) {
     const int64_t nblk = (int64_t)h->g.nb[0] * h->g.nb[1] * h->g.nb[2];
     int64_t b = (int64_t)h->P.cap * kFields * 4 * (h->spare_arena ? 2 : 1);
     b += h->grid_nodes * (h->grid2 ? 32 : 16) + (h->vol ? h->grid_nodes * 4 : 0) + (h->d_fixed ? h->grid_nodes * 36 : 0);
-    b += nblk * 12 + h->grid_nodes * 4 + h->part_cand_cap * 4 + 20;                      // work lists
+    b += nblk * 12 + h->grid_nodes * 4 + h->part_cand_cap * 4 + 16;                      // work lists
     b += h->ss_cap * 12 + (h->grid_nodes + 1) * 8 + (h->ss_scan_cap + 2) * 4;           // sort
     b += h->keep_cap * 16 + (h->scan_cap + 2) * 4;                                       // removal
     b += h->pose_cap * (int64_t)sizeof(ColliderPose) + (int64_t)h->collider_bytes + (int64_t)h->sdf_bytes;
@@ -1078,8 +1078,8 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
         CK(cudaMemset(h->wl.block_flag, 0, sizeof(unsigned int) * (size_t)nblk));
         CK(cudaMalloc(&h->wl.blocks[0], sizeof(int32_t) * (size_t)nblk));
         CK(cudaMalloc(&h->wl.blocks[1], sizeof(int32_t) * (size_t)nblk));
-        CK(cudaMalloc(&h->wl.counts, sizeof(unsigned int) * 5));
-        CK(cudaMemset(h->wl.counts, 0, sizeof(unsigned int) * 5));
+        CK(cudaMalloc(&h->wl.counts, sizeof(unsigned int) * 4));
+        CK(cudaMemset(h->wl.counts, 0, sizeof(unsigned int) * 4));
         CK(cudaMalloc(&h->wl.node_cand, sizeof(int32_t) * (size_t)h->grid_nodes));
         // sort by grid node: one count and start per node, plus the key of stencils outside the grid
         CK(cudaMalloc(&h->ss.count, sizeof(unsigned int) * (size_t)(h->grid_nodes + 1)));

@@ -457,7 +457,8 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
     };
     const bool pdl = shape.pdl != 0;
     mark(0);
-    launch_step_kernel(k_clear_blocks<OneScene>, list_ctas, 256, st, pdl, sc);  // ends with the step begin
+    launch_step_kernel(k_step_begin<OneScene>, 1, 1, st, pdl, sc);
+    launch_step_kernel(k_clear_blocks<OneScene>, list_ctas, 256, st, pdl, sc);
     mark(1);
     if (a.n > 0) {
         if (shape.p2g_tile && !a.fixed)
@@ -568,7 +569,7 @@ cudaError_t prepare_substep_kernels() {
 }
 
 int substep_kernel_count(const SubstepArgs& a) {
-    return 2 + (a.n > 0 ? 2 : 0) + (a.cd.n_col > 0 ? 2 : 0);
+    return 3 + (a.n > 0 ? 2 : 0) + (a.cd.n_col > 0 ? 2 : 0);
 }
 
 

@@ -207,26 +207,15 @@ __device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTe
     }
 }
 
-// One scene: the clear runs first in the substep and its last CTA to finish begins the substep (step_begin),
-// so there is no step-begin kernel in the launch chain. Every CTA reads seq before any CTA can advance it (a
-// CTA counts itself done only after its reads), so all clear the list of the substep before. The done-counter
-// (counts[4]) is reset by that last CTA; nothing waits on it. A batch runs k_step_begin first, then this.
+// Runs after k_step_begin: seq has advanced, so the substep before has parity (seq - 1) & 1.
 template <class Scenes>
 __global__ void __launch_bounds__(256) k_clear_blocks(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
-        const unsigned int prev = a.sp->seq & 1u;  // not yet advanced: the parity of the substep before
+        const unsigned int prev = (a.sp->seq - 1u) & 1u;
         const unsigned int n = a.wl.counts[prev];
         for (unsigned int i = blockIdx.x * 4u + (threadIdx.x >> 6); i < n; i += gridDim.x * 4u) clear_block(a, prev, i);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            __threadfence();
-            if (atomicAdd(&a.wl.counts[4], 1u) == gridDim.x - 1u) {
-                a.wl.counts[4] = 0u;
-                step_begin(a.sp, a.wl.counts, a.cd.n_col, a.grid2 != nullptr);
-            }
-        }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {

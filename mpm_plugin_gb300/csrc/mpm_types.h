@@ -130,7 +130,7 @@ struct WorkLists {
     unsigned int* block_flag;   // one per grid block: 1 while the block is in the current list
     int32_t* blocks[2];         // active block ids
     unsigned int* counts;       // [0], [1]: active block counts; [2]: collider node candidates;
-                                // [3]: collider particle candidates; [4]: CTAs of the clear kernel done
+                                // [3]: collider particle candidates
     int32_t* node_cand;         // grid nodes (blocked index) inside some collider's margin box
     int32_t* part_cand;         // particles inside some collider's margin box after G2P
 };
