@@ -16,7 +16,10 @@ unsorted mixed workload and on the 256^3 pour, and in a short tuning window it c
 Search: coordinate descent from the defaults, one knob at a time over its candidates with the others fixed,
 keeping a change only when it is at least 2 % faster. A configuration is timed by CUDA events the solver
 records at the two ends of each substep (MPM_OPT_KERNEL_TIMING 2, so the kernels inside stay chained as
-untimed) over `substeps` substeps after 3 warm-up substeps. The solver's state is saved before and loaded back after, so tuning does not advance the bake
+untimed) over `substeps` substeps after 3 warm-up substeps; or, for a workload that runs as run_substeps
+calls (runs=True), by the host clock around one run_substeps call of `substeps` substeps (eight substeps
+per graph launch, chained across substeps). A small scene's choice differs between the two: with one
+substep per graph the graph launch hides what 1,216 near-idle work-list CTAs cost, with eight it does not. The solver's state is saved before and loaded back after, so tuning does not advance the bake
 (a load recomputes the stored stress from F, a last-bit change).
 
 Cache: JSON at $MPM_GB300_TUNE_CACHE or ~/.cache/mpm_plugin_gb300/autotune.json, keyed by the GPU (name,
@@ -125,19 +128,42 @@ def _time_solver(solver, cfg, sms, dt, frame_dt, substeps):
     return ms / 1e3 / substeps
 
 
+def _time_runs(solver, cfg, sms, dt, substeps, repeats=3):
+    import time
+
+    import torch
+
+    apply(solver, cfg, sms)
+    solver.run_substeps(dt, substeps)  # graphs captured
+    best = float("inf")
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.run_substeps(dt, substeps)  # returns once its substeps are done
+        best = min(best, time.perf_counter() - t0)
+    return best / substeps
+
+
 def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20, path: Path | None = None,
-                force: bool = False, deterministic: bool = False) -> dict:
+                force: bool = False, deterministic: bool = False, runs: bool = False) -> dict:
     """Choose and set the solver's launch choices for its current scene; returns the configuration with
-    ``cached`` (whether it came from the cache) and, when measured, ``seconds_per_substep``."""
+    ``cached`` (whether it came from the cache) and, when measured, ``seconds_per_substep``. runs: time
+    run_substeps calls (the way a fixed-dt workload of many substeps per call runs) instead of single
+    substeps."""
     gkey, sms = gpu_key(solver.device)
     wkey = workload_key(max(solver.domain.grid_shape), solver.particle_count, solver._n_colliders > 0, deterministic)
+    if runs:
+        wkey += "|runs"
     cache = load_cache(path)
     hit = cache.get(gkey, {}).get(wkey)
     if hit and not force:
         apply(solver, hit, sms)
         return {**hit, "cached": True}
     snapshot = solver.save_state()
-    measure = lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps)  # noqa: E731
+    if runs:
+        measure = lambda cfg: _time_runs(solver, cfg, sms, dt, substeps)  # noqa: E731
+    else:
+        measure = lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps)  # noqa: E731
     if deterministic:  # one grid whatever fused_p2g says: that knob is not searched (nor set) there
         best, best_t, trials = search(measure)
     else:

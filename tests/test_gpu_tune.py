@@ -41,6 +41,22 @@ def test_tune_solver_restores_state_and_caches(tmp_path):
     assert rel_err(s.save_state()["x"], ref.save_state()["x"]) <= 1e-4
 
 
+def test_tune_solver_on_run_substeps_restores_state_and_caches_apart(tmp_path):
+    """runs=True times run_substeps calls: the state is restored, the choice is cached under its own key."""
+    from mpm_plugin_gb300 import tune
+
+    path = tmp_path / "autotune.json"
+    s = _solver()
+    before = s.save_state()
+    cfg = tune.tune_solver(s, 2e-4, substeps=16, path=path, runs=True)
+    assert not cfg["cached"] and cfg["seconds_per_substep"] > 0 and "fused_p2g" in cfg
+    after = s.save_state()
+    for k in ("x", "v", "C", "F", "Jp", "mat", "emitter"):
+        np.testing.assert_array_equal(after[k], before[k])
+    assert tune.tune_solver(_solver(), 2e-4, substeps=16, path=path, runs=True)["cached"]
+    assert not tune.tune_solver(_solver(), 2e-4, substeps=8, path=path)["cached"]  # the other key
+
+
 @pytest.mark.parametrize("variant,ctas_per_sm,group,pdl,tile", [(0, 4, 1, 0, 0), (1, 16, 4, 1, 0), (1, 8, 32, 0, 1),
                                                               (0, 16, 8, 1, 1), (0, 8, 32, 1, 0), (1, 4, 8, 0, 1)])
 def test_every_launch_choice_gives_the_same_physics(variant, ctas_per_sm, group, pdl, tile):
