@@ -18,7 +18,7 @@ keeping a change only when it is at least 2 % faster. A configuration is timed b
 records at the two ends of each substep (MPM_OPT_KERNEL_TIMING 2, so the kernels inside stay chained as
 untimed) over `substeps` substeps after 3 warm-up substeps; or, for a workload that runs as run_substeps
 calls (runs=True), by the host clock around one run_substeps call of `substeps` substeps (eight substeps
-per graph launch, chained across substeps). A small scene's choice differs between the two: with one
+per graph launch, chained across substeps), each trial from the saved state. A small scene's choice differs between the two: with one
 substep per graph the graph launch hides what 1,216 near-idle work-list CTAs cost, with eight it does not. The solver's state is saved before and loaded back after, so tuning does not advance the bake
 (a load recomputes the stored stress from F, a last-bit change).
 
@@ -160,8 +160,10 @@ def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20,
         apply(solver, hit, sms)
         return {**hit, "cached": True}
     snapshot = solver.save_state()
-    if runs:
-        measure = lambda cfg: _time_runs(solver, cfg, sms, dt, substeps)  # noqa: E731
+    if runs:  # every trial from the same state: thousands of substeps per trial move the scene on
+        def measure(cfg):
+            solver.load_state(snapshot)
+            return _time_runs(solver, cfg, sms, dt, substeps)
     else:
         measure = lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps)  # noqa: E731
     if deterministic:  # one grid whatever fused_p2g says: that knob is not searched (nor set) there
