@@ -39,3 +39,65 @@ def test_cache_round_trip(tmp_path, monkeypatch):
     assert tune.cache_path() == path
     path.write_text("{not json")
     assert tune.load_cache(path) == {}
+
+
+class _FakeSolver:
+    """The parts of Gb300Solver the tuner uses; a run_substeps call advances a counter standing in for the
+    scene's state, and its cost depends on the options set and on how far the scene has moved on."""
+
+    device = "cuda:0"
+    particle_count = 32_768
+    _n_colliders = 0
+
+    class domain:
+        grid_shape = (64, 64, 64)
+
+    def __init__(self):
+        self.state, self.opts, self.loads = 0, {}, 0
+
+    def save_state(self):
+        return {"step": self.state}
+
+    def load_state(self, st):
+        self.state = st["step"]
+        self.loads += 1
+
+    def set_option(self, option, value):
+        self.opts[option] = value
+
+    def run_substeps(self, dt, count):
+        self.state += count
+
+
+def test_run_substeps_tuning_restores_the_state_per_trial_and_keeps_its_own_key(tmp_path, monkeypatch):
+    import time
+
+    import torch
+
+    from mpm_plugin_gb300 import _abi
+
+    clock = {"t": 0.0}
+    monkeypatch.setattr(tune, "gpu_key", lambda device: ("gpu|152", 152))
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    monkeypatch.setattr(time, "perf_counter", lambda: clock["t"])
+    s = _FakeSolver()
+    real_run = s.run_substeps
+
+    def run(dt, count):  # 1 s per substep, 3 s with the two-grid mode, plus the scene's age if not restored
+        clock["t"] += count * (3.0 if s.opts.get(_abi.OPT_FUSED_P2G) else 1.0) + s.state
+        real_run(dt, count)
+
+    s.run_substeps = run
+    path = tmp_path / "autotune.json"
+    cfg = tune.tune_solver(s, 1e-4, 1e-4, substeps=10, path=path, runs=True)
+    trials = cfg["trials"]
+    assert s.loads == trials + 1  # before every trial, and once at the end
+    assert s.state == 0
+    assert cfg["fused_p2g"] == 0 and s.opts[_abi.OPT_FUSED_P2G] == 0
+    assert list(tune.load_cache(path)["gpu|152"]) == [tune.workload_key(64, 32_768, False) + "|runs"]
+    assert tune.tune_solver(_FakeSolver(), 1e-4, 1e-4, path=path, runs=True)["cached"]
+
+
+def test_the_two_grid_knob_is_searched_last_for_a_solver():
+    assert tune.SOLVER_ORDER[-1] == "fused_p2g" and tune.SOLVER_ORDER[:-1] == tune.KNOB_ORDER
+    assert tune.SOLVER_DEFAULTS["fused_p2g"] == 0 and "fused_p2g" not in tune.DEFAULTS
