@@ -125,8 +125,8 @@ enum {
                                   (exact integer additions, independent of particle order and atomic timing);
                                   results agree with the default mode within float rounding. 0 (default) */
     MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 80 registers, 3 CTAs of 256 per SM; 1 uncapped */
-    MPM_OPT_LIST_CTAS = 6,     /* CTAs of the kernels that walk the active-block and candidate lists (default
-                                  1216 = 8 per SM of a GB300) */
+    MPM_OPT_LIST_CTAS = 6,     /* CTAs of the kernels that walk the active-block and candidate lists (default:
+                                  8 per SM of the device, from cudaDevAttrMultiProcessorCount) */
     MPM_OPT_P2G_GROUP = 7,     /* P2G sums same-cell lanes within aligned groups of this many lanes before one
                                   reduction each: 1, 2, 4, 8, 16 or 32 (default) */
     MPM_OPT_PDL = 8,           /* 1 (default): the substep kernels use programmatic dependent launch, so each

@@ -391,6 +391,10 @@ Status prepare_grids(Handle* h, bool two, bool keep_pending) {
 }
 
 // Drops a scatter made for an explicit substep that may not follow (the particles are about to change).
+// The kept scatter is valid only while the particle state, the materials and dt are what the previous
+// explicit substep left: every entry point that changes particle state or materials (today add_particles and
+// load_state; advance and run_substeps start from fresh grids through prepare_grids) must call this before
+// the change, and so must any such entry point added later.
 Status drop_pending(Handle* h) {
     return h->pending ? prepare_grids(h, h->two_live, false) : Status{};
 }
@@ -1033,6 +1037,7 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     if (!dom || !gravity || !out || (n_mat > 0 && !mats)) return {MPM_ERR_ARGUMENT, "null argument"};
     if (n_mat > kMaxMaterials) return {MPM_ERR_VALUE, "too many materials"};
     if (ppc <= 0) return {MPM_ERR_VALUE, "particles_per_cell must be positive"};
+    if (const char* why = domain_problem(*dom)) return {MPM_ERR_VALUE, why};
     for (int m = 0; m < n_mat; ++m)
         if (mats[m].model < 0 || mats[m].model > 3)
             return {MPM_ERR_NOT_IMPLEMENTED, "material model is not supported by the gb300 backend"};

@@ -9,7 +9,7 @@ namespace mpm {
 
 void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
     const SceneTable sc{b.scenes, b.cta_scene, b.cta_first, b.n_scenes};
-    const unsigned int list_ctas = b.shape.list_ctas;
+    const unsigned int list_ctas = b.shape.list_ctas ? b.shape.list_ctas : sm_count() * kCtasPerSm;
     const bool pdl = b.shape.pdl != 0;
     launch_step_kernel(k_step_begin<SceneTable>, 1, 128, st, pdl, sc);
     launch_step_kernel(k_clear_blocks<SceneTable>, list_ctas, 256, st, pdl, sc);

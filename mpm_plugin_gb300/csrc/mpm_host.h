@@ -20,6 +20,19 @@ struct HostDomain {
     int dims[3];
 };
 
+// A domain make_grid can build: a positive resolution and finite bounds with max > min on every axis
+// (Domain.__post_init__, mpm_core/scene.py:44-51, refuses max <= min and resolutions below 4 on the Python
+// side; a raw descriptor reaches this layer unchecked). Returns a message for the first violation, or nullptr.
+inline const char* domain_problem(const MpmDomainDesc& dom) {
+    if (dom.resolution <= 0) return "domain resolution must be positive";
+    for (int a = 0; a < 3; ++a) {
+        if (!std::isfinite(dom.min[a]) || !std::isfinite(dom.max[a])) return "domain bounds must be finite";
+        if (!(dom.max[a] > dom.min[a])) return "domain max must exceed min on every axis";
+    }
+    if (!std::isfinite(dom.wall_friction)) return "wall friction must be finite";
+    return nullptr;
+}
+
 // mpm_core/scene.py:60-67 (dx, grid shape) and warp/solver.py:37-53 (padding, origin, walls, clamps)
 inline GridDesc make_grid(const MpmDomainDesc& dom, const double gravity[3], int ppc, HostDomain* hd) {
     GridDesc g{};

@@ -18,7 +18,10 @@ struct EscapeBounds {  // particles past these planes on open sides are removed 
 // Records the message mpm_last_error(NULL) returns on this thread.
 void set_last_error(const std::string& msg);
 
-constexpr unsigned int kListCtas = 152 * 8;  // CTAs of the kernels that walk device-sized work lists
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount, cached per device; 1 if
+// the query fails). Grids that stride over device-sized work are sized as a multiple of it.
+unsigned int sm_count();
+constexpr unsigned int kCtasPerSm = 8;  // default CTAs per SM of the kernels that stride over work lists
 
 
 void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, ColliderPose* poses, int steps,
@@ -29,7 +32,7 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 // Launch choices the autotuner sets: CTAs of the kernels that walk work lists, the G2P build (0: capped
 // at 80 registers, 3 CTAs of 256 per SM; 1: uncapped) and P2G's reduction group.
 struct LaunchShape {
-    unsigned int list_ctas = kListCtas;
+    unsigned int list_ctas = 0;  // 0: kCtasPerSm per SM of the device (resolved at launch)
     int g2p_variant = 0;
     int p2g_group = 32;  // lanes of the aligned groups P2G sums within (a power of two, 1 .. 32)
     int pdl = 1;         // 1: the substep kernels launch with programmatic dependent launch

@@ -11,6 +11,23 @@
 
 namespace mpm {
 
+unsigned int sm_count() {
+    static unsigned int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev < 64 && cached[dev]) return cached[dev];
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        return 1;
+    }
+    if (dev < 64) cached[dev] = (unsigned int)sms;
+    return (unsigned int)sms;
+}
+
 // ------------------------------------------------------------------------------------------------------
 // Collider poses of every substep of an advance, one thread per (substep, collider): substep k ends at
 // s = (k + 1) / steps (warp/solver.py:218-219). steps == 0: one pose at the given s.
@@ -448,7 +465,7 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
 }
 
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing) {
-    const unsigned int list_ctas = shape.list_ctas;
+    const unsigned int list_ctas = shape.list_ctas ? shape.list_ctas : sm_count() * kCtasPerSm;
     const OneScene sc{a};
     // while a graph is being captured the records become event nodes that fire on every replay; with them
     // in place the kernels around them launch in plain stream order
@@ -576,7 +593,7 @@ int substep_kernel_count(const SubstepArgs& a) {
 void launch_max_speed(cudaStream_t st, const Particles& P, unsigned int* out) {
     if (P.n == 0) return;
     unsigned int b = blocks_for(P.n, 256);
-    if (b > 152 * 8) b = 152 * 8;
+    b = std::min(b, sm_count() * kCtasPerSm);
     k_max_speed<<<b, 256, 0, st>>>(P, out);
 }
 
@@ -635,7 +652,7 @@ void launch_query_fill_fixed(cudaStream_t st, const GridDesc& g, const unsigned 
 void launch_conservation(cudaStream_t st, const Particles& P, const Material* mats, double* out) {
     cudaMemsetAsync(out, 0, sizeof(double) * 9, st);
     if (P.n == 0) return;
-    k_conservation<<<std::min<unsigned int>(blocks_for(P.n, 256), 152 * 8), 256, 0, st>>>(P, mats, out);
+    k_conservation<<<std::min<unsigned int>(blocks_for(P.n, 256), sm_count() * kCtasPerSm), 256, 0, st>>>(P, mats, out);
 }
 
 void launch_grid_unblock(cudaStream_t st, const GridDesc& g, const float4* grid, float4* out) {

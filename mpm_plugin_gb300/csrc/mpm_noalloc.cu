@@ -88,7 +88,14 @@ extern "C" int mpm_is_occupied_noalloc(const MpmDomainDesc* domain, int32_t part
                                        int32_t device, void* stream) {
     if (!domain || particles_per_cell <= 0 || n < 0 || m < 0 || (n > 0 && !d_x) || (m > 0 && (!d_points || !d_out)))
         return fail(MPM_ERR_ARGUMENT, "bad arguments");
-    if (device < 0 || device >= kMaxDevices) return fail(MPM_ERR_ARGUMENT, "device index out of range");
+    if (const char* why = mpm::domain_problem(*domain)) return fail(MPM_ERR_VALUE, why);
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MPM_ERR_CUDA, "no CUDA device");
+    }
+    if (device < 0 || device >= count || device >= kMaxDevices)
+        return fail(MPM_ERR_ARGUMENT, "device index out of range");
     const double gravity[3] = {0.0, 0.0, 0.0};
     mpm::HostDomain hd{};
     mpm::GridDesc g = mpm::make_grid(*domain, gravity, particles_per_cell, &hd);
@@ -98,22 +105,32 @@ extern "C" int mpm_is_occupied_noalloc(const MpmDomainDesc* domain, int32_t part
                                        std::to_string(kNoAllocNodes) + " (16 MiB): use mpm_is_occupied");
     if (m == 0) return MPM_OK;
     int prev = -1;
-    cudaGetDevice(&prev);
-    if (prev != device) cudaSetDevice(device);
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MPM_ERR_CUDA, "cudaGetDevice failed");
+    }
+    if (prev != device && cudaSetDevice(device) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(MPM_ERR_CUDA, "cudaSetDevice failed");  // before any address is looked up or cached
+    }
     float* vol = nullptr;
     cudaError_t e = scratch_address(device, &vol);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(vol, 0, (size_t)nodes * sizeof(float), st);  // starts from zero
+    // launched through cudaLaunchKernel, whose return value is this launch's own status (an error pending
+    // from the caller's earlier calls is neither reported here nor cleared)
     if (e == cudaSuccess && n > 0) {
-        k_noalloc_scatter<<<(unsigned int)((n + 255) / 256), 256, 0, st>>>(d_x, n, g, vol);
-        e = cudaGetLastError();
+        void* args[] = {&d_x, &n, &g, &vol};
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(k_noalloc_scatter), dim3((unsigned int)((n + 255) / 256)),
+                             dim3(256), args, 0, st);
     }
     if (e == cudaSuccess) {
-        k_noalloc_query<<<(unsigned int)((m + 255) / 256), 256, 0, st>>>(g, vol, (float)std::pow(hd.dx, 3.0), m,
-                                                                        d_points, d_out);
-        e = cudaGetLastError();
+        float cell_vol = (float)std::pow(hd.dx, 3.0);
+        void* args[] = {&g, &vol, &cell_vol, &m, &d_points, &d_out};
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(k_noalloc_query), dim3((unsigned int)((m + 255) / 256)),
+                             dim3(256), args, 0, st);
     }
-    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+    if (prev != device) cudaSetDevice(prev);
     if (e != cudaSuccess) return fail(MPM_ERR_CUDA, cudaGetErrorString(e));
     return MPM_OK;
 }

@@ -382,7 +382,7 @@ int mpm_surface_upload(void* surfacer, int64_t n, const float* x, const float* v
         e = cudaMemcpyAsync(s->small.p, init, sizeof(init), cudaMemcpyHostToDevice, st);
     }
     if (e == cudaSuccess) {
-        const unsigned int blocks = (unsigned int)std::min<int64_t>(blocks_of(n), 152 * 8);
+        const unsigned int blocks = (unsigned int)std::min<int64_t>(blocks_of(n), (int64_t)mpm::sm_count() * mpm::kCtasPerSm);
         k_surf_bounds<<<blocks, 256, 0, st>>>(n, s->x.as<float>(), s->small.as<int>());
         e = cudaGetLastError();
     }

@@ -83,16 +83,18 @@ def store_cache(cache: dict, path: Path | None = None) -> None:
     tmp.replace(path)
 
 
-def apply(target, cfg: dict, sms: int) -> None:
-    """Set a configuration on a Gb300Solver or Gb300Batch."""
+def apply(target, cfg: dict, sms: int, solver: bool = False) -> None:
+    """Set a configuration on a Gb300Solver (solver=True) or Gb300Batch. A solver always gets a grid mode: a
+    configuration without the fused_p2g knob (one cached before the knob existed, or a deterministic one)
+    means one grid, the mode it was measured in."""
     target.set_option(_abi.OPT_SORT_INTERVAL, int(cfg["sort_interval"]))
     target.set_option(_abi.OPT_G2P_VARIANT, int(cfg["g2p_variant"]))
     target.set_option(_abi.OPT_LIST_CTAS, int(cfg["list_ctas_per_sm"]) * sms)
     target.set_option(_abi.OPT_P2G_GROUP, int(cfg.get("p2g_group", 32)))
     target.set_option(_abi.OPT_PDL, int(cfg.get("pdl", 1)))
     target.set_option(_abi.OPT_P2G_TILE, int(cfg.get("p2g_tile", 0)))
-    if "fused_p2g" in cfg:  # solvers only
-        target.set_option(_abi.OPT_FUSED_P2G, int(cfg["fused_p2g"]))
+    if solver:
+        target.set_option(_abi.OPT_FUSED_P2G, int(cfg.get("fused_p2g", 0)))
 
 
 def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, min_gain=MIN_GAIN):
@@ -116,7 +118,7 @@ def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, 
 
 
 def _time_solver(solver, cfg, sms, dt, frame_dt, substeps):
-    apply(solver, cfg, sms)
+    apply(solver, cfg, sms, solver=True)
     for _ in range(3):
         solver.substep(dt, 1.0, frame_dt)
     solver.set_option(_abi.OPT_KERNEL_TIMING, 2)  # events at the two ends of each substep
@@ -133,7 +135,7 @@ def _time_runs(solver, cfg, sms, dt, substeps, repeats=3):
 
     import torch
 
-    apply(solver, cfg, sms)
+    apply(solver, cfg, sms, solver=True)
     solver.run_substeps(dt, substeps)  # graphs captured
     best = float("inf")
     for _ in range(repeats):
@@ -157,7 +159,7 @@ def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20,
     cache = load_cache(path)
     hit = cache.get(gkey, {}).get(wkey)
     if hit and not force:
-        apply(solver, hit, sms)
+        apply(solver, hit, sms, solver=True)
         return {**hit, "cached": True}
     snapshot = solver.save_state()
     if runs:  # every trial from the same state: thousands of substeps per trial move the scene on
@@ -171,7 +173,7 @@ def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20,
     else:
         best, best_t, trials = search(measure, SOLVER_CANDIDATES, SOLVER_DEFAULTS, SOLVER_ORDER)
     solver.load_state(snapshot)
-    apply(solver, best, sms)
+    apply(solver, best, sms, solver=True)
     cache.setdefault(gkey, {})[wkey] = best
     store_cache(cache, path)
     return {**best, "cached": False, "seconds_per_substep": best_t, "trials": len(trials)}

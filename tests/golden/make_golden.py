@@ -1,6 +1,8 @@
 """Generate the golden fixtures in this folder by running the reference's own MLS-MPM code.
 
-    python tests/golden/make_golden.py [--reference /root/reference] [--only NAME ...]
+    python tests/golden/make_golden.py --reference PATH_TO_MPM_PLUGIN_CHECKOUT [--only NAME ...]
+
+(or MPM_PLUGIN_REFERENCE=PATH in the environment instead of --reference)
 
 The reference backend (``mpm_core/backends/warp/{solver,kernels,colliders}.py``) is imported from the
 reference checkout and run unchanged on the CPU through ``warp_emu`` (a CPU emulator of the Warp API subset
@@ -15,6 +17,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import os
 import sys
 import time
 from fractions import Fraction
@@ -323,7 +326,9 @@ def geometry_cases(only):
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", type=Path, default=Path("/root/reference"))
+    env = os.environ.get("MPM_PLUGIN_REFERENCE")
+    ap.add_argument("--reference", type=Path, default=Path(env) if env else None,
+                    required=env is None, help="checkout of jonatanhedborg/mpm_plugin (or $MPM_PLUGIN_REFERENCE)")
     ap.add_argument("--only", nargs="*", default=[])
     args = ap.parse_args()
     _install(args.reference)

@@ -72,6 +72,33 @@ def test_create_without_gpu_reports_cuda_error():
     assert b"not supported" in L.mpm_last_error(None)
 
 
+@pytest.mark.parametrize("field,value,message", [
+    ("resolution", 0, b"resolution"), ("resolution", -3, b"resolution"), ("max", 0.0, b"max must exceed min"),
+    ("max", float("nan"), b"finite"), ("min", float("-inf"), b"finite")])
+def test_bad_domain_descriptors_are_refused_before_the_device(field, value, message):
+    """mpm_create and mpm_is_occupied_noalloc take a raw domain descriptor: a non-positive resolution,
+    non-finite bounds or max <= min are value errors, found before any grid is derived or device touched."""
+    from mpm_plugin_gb300 import _abi
+
+    L = _abi.lib()
+    d = _abi.MpmDomainDesc()
+    for a in range(3):
+        d.max[a] = 1.0
+        d.wall_lo[a] = d.wall_hi[a] = 1
+    d.resolution = 8
+    if field == "resolution":
+        d.resolution = value
+    else:
+        getattr(d, field)[2] = value
+    m = (_abi.MpmMaterialDesc * 1)()
+    h = ctypes.c_void_p()
+    g = (ctypes.c_double * 3)(0, 0, -9.81)
+    assert L.mpm_create(ctypes.byref(d), m, 1, g, 8, 0, ctypes.byref(h)) == _abi.MPM_ERR_VALUE
+    assert message in L.mpm_last_error(None) and not h.value
+    assert L.mpm_is_occupied_noalloc(ctypes.byref(d), 8, 0, None, 0, None, None, 0, None) == _abi.MPM_ERR_VALUE
+    assert message in L.mpm_last_error(None)
+
+
 def test_surfacer_entry_points_validate_before_the_device():
     """Surfacer calls with a null surfacer or null outputs fail with an argument error; without a GPU the
     creation fails with a CUDA error rather than crashing."""

@@ -108,8 +108,8 @@ def test_run_substeps_and_advance_match_one_grid_mode():
 
 
 def test_a_scatter_for_a_substep_that_does_not_follow_is_dropped():
-    """After an explicit substep (which scattered for a next one with its dt): another dt, new particles, a
-    loaded state, an advance, a batch, deterministic mode and the option switched off and on, each against the
+    """After an explicit substep (which scattered for a next one with its dt): another dt, an occupancy query
+    (kept), new particles, a loaded state, an advance, a batch, deterministic mode and the option switched off and on, each against the
     same calls in one-grid mode."""
     from mpm_plugin_gb300.batch import Gb300Batch
 
@@ -119,7 +119,12 @@ def test_a_scatter_for_a_substep_that_does_not_follow_is_dropped():
         s.substep(2e-4, 1.0, 1 / 24)
         s.substep(1e-4, 1.0, 1 / 24)  # another dt
         s.substep(1e-4, 1.0, 1 / 24)
-        add(s, box_particles((0.1, 0.1, 0.6), (0.2, 0.2, 0.7), d.dx, seed=5), 0, 0)  # new particles
+        # the emission path between explicit substeps: an occupancy query (no particle changes, the scatter
+        # is kept) and then the free points added (the scatter is dropped)
+        probe = box_particles((0.1, 0.1, 0.6), (0.2, 0.2, 0.7), d.dx, seed=5)
+        assert not s.is_occupied(probe).any()
+        s.substep(1e-4, 1.0, 1 / 24)
+        add(s, probe, 0, 0)  # new particles
         s.substep(1e-4, 1.0, 1 / 24)
         state = s.save_state()
         s.substep(1e-4, 1.0, 1 / 24)
