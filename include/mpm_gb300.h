@@ -168,6 +168,10 @@ int mpm_kernel_times(void *handle, int32_t n_slots, float *ms, int64_t *launches
  * mpm_read_collider_pose: collider c's pose of the last substep as 3x4 row-major matrices: the world
  * transform M, its inverse, and dM, the time derivative the collider velocity is taken from. */
 int mpm_grid_dims(void *handle, int32_t dims[3]);
+/* The padded node counts a solver created with this domain would have (grid_shape + 6 per axis,
+ * mpm_core/scene.py:60-67 and warp/solver.py:37-40), without creating one or touching a device: for footprint
+ * estimates before admission. MPM_ERR_VALUE for a domain mpm_create would refuse. */
+int mpm_domain_grid_dims(const MpmDomainDesc *domain, int32_t dims[3]);
 int mpm_read_grid(void *handle, float *out);
 int mpm_read_collider_pose(void *handle, int32_t c, float *M12, float *Minv12, float *dM12);
 

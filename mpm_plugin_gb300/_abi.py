@@ -29,7 +29,7 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
            "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count", "mpm_surface_create",
            "mpm_surface_destroy", "mpm_surface_upload", "mpm_surface_last_error", "mpm_surface_build", "mpm_surface_read", "mpm_surface_read_field",
-           "mpm_mc_table")
+           "mpm_mc_table", "mpm_domain_grid_dims")
 
 
 class MpmDomainDesc(C.Structure):
@@ -85,6 +85,7 @@ def lib() -> C.CDLL:
         "mpm_synchronize": [P],
         "mpm_kernel_times": [P, I32, P, P, I32],
         "mpm_grid_dims": [P, P],
+        "mpm_domain_grid_dims": [C.POINTER(MpmDomainDesc), P],
         "mpm_read_grid": [P, P],
         "mpm_read_collider_pose": [P, I32, P, P, P],
         "mpm_launch_count": [P, C.POINTER(I64)],

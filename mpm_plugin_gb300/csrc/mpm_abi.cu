@@ -1038,9 +1038,16 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
     if (n_mat > kMaxMaterials) return {MPM_ERR_VALUE, "too many materials"};
     if (ppc <= 0) return {MPM_ERR_VALUE, "particles_per_cell must be positive"};
     if (const char* why = domain_problem(*dom)) return {MPM_ERR_VALUE, why};
-    for (int m = 0; m < n_mat; ++m)
-        if (mats[m].model < 0 || mats[m].model > 3)
+    for (int m = 0; m < n_mat; ++m) {
+        const MpmMaterialDesc& md = mats[m];
+        if (md.model < 0 || md.model > 3)
             return {MPM_ERR_NOT_IMPLEMENTED, "material model is not supported by the gb300 backend"};
+        // the ranges MaterialParams enforces (mpm_core/materials.py:38-46), checked again here because a raw
+        // descriptor can reach this boundary without passing through that record
+        if (!(md.youngs_modulus > 0)) return {MPM_ERR_VALUE, "youngs_modulus must be > 0"};
+        if (!(md.poisson_ratio >= 0 && md.poisson_ratio < 0.5)) return {MPM_ERR_VALUE, "poisson_ratio must be in [0, 0.5)"};
+        if (!(md.density > 0)) return {MPM_ERR_VALUE, "density must be > 0"};
+    }
     Handle* h = new Handle();
     *out = h;
     h->device = device;
@@ -1748,6 +1755,16 @@ int mpm_grid_dims(void* handle, int32_t dims[3]) {
     HANDLE_OR_FAIL(handle);
     if (!dims) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
     for (int a = 0; a < 3; ++a) dims[a] = h->dims[a];
+    return MPM_OK;
+}
+
+int mpm_domain_grid_dims(const MpmDomainDesc* domain, int32_t dims[3]) {
+    if (!domain || !dims) return finish(nullptr, {MPM_ERR_ARGUMENT, "null argument"});
+    if (const char* why = domain_problem(*domain)) return finish(nullptr, {MPM_ERR_VALUE, why});
+    const double gravity[3] = {0.0, 0.0, 0.0};
+    HostDomain hd{};
+    make_grid(*domain, gravity, 1, &hd);
+    for (int a = 0; a < 3; ++a) dims[a] = hd.dims[a];
     return MPM_OK;
 }
 

@@ -18,9 +18,10 @@ namespace mpm {
 using std::isfinite;
 #endif
 
-// Arithmetic with every operation rounded on its own (no fused multiply-add), for the few values whose
-// last bits decide a discrete choice (the collider pose, a grid node's position, the local query point,
-// FP64 distances that break near-ties between mesh faces): these follow the reference's operation order.
+// Arithmetic with every operation rounded on its own (no fused multiply-add), for the values whose last bits
+// decide a discrete choice or are magnified downstream (the collider pose, a grid node's position, the local
+// query point, FP64 distances that break near-ties between mesh faces, the closest point, normal and contact
+// response of a collider query): these follow the reference's operation order.
 #ifdef __CUDA_ARCH__
 MPM_HD float fadd(float a, float b) { return __fadd_rn(a, b); }
 MPM_HD float fsub(float a, float b) { return __fsub_rn(a, b); }
@@ -30,6 +31,7 @@ MPM_HD double dadd(double a, double b) { return __dadd_rn(a, b); }
 MPM_HD double dsub(double a, double b) { return __dsub_rn(a, b); }
 MPM_HD double dmul(double a, double b) { return __dmul_rn(a, b); }
 MPM_HD double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+MPM_HD float fsqrt(float a) { return __fsqrt_rn(a); }
 #else  // host: a volatile store keeps the compiler from fusing the operation into a multiply-add
 MPM_HD float fadd(float a, float b) { volatile float r = a + b; return r; }
 MPM_HD float fsub(float a, float b) { volatile float r = a - b; return r; }
@@ -39,7 +41,12 @@ MPM_HD double dadd(double a, double b) { volatile double r = a + b; return r; }
 MPM_HD double dsub(double a, double b) { volatile double r = a - b; return r; }
 MPM_HD double dmul(double a, double b) { volatile double r = a * b; return r; }
 MPM_HD double ddiv(double a, double b) { volatile double r = a / b; return r; }
+MPM_HD float fsqrt(float a) { volatile float r = sqrtf(a); return r; }
 #endif
+// a0 b0 + a1 b1 + a2 b2, left to right, each operation rounded on its own
+MPM_HD float fdot3(const float a[3], const float b[3]) {
+    return fadd(fadd(fmul(a[0], b[0]), fmul(a[1], b[1])), fmul(a[2], b[2]));
+}
 
 // ---------------------------------------------------------------------------------------------------------
 // 3x3 SVD with the convention of Warp's svd3 (called at kernels.py:35,57,252): U and V proper rotations,
@@ -575,24 +582,33 @@ struct ClosestState {
         }
     }
 
+    // The FP32 pass above only chooses the face. The winner's closest point is evaluated again in FP64 (its
+    // barycentrics and region by the exact-order routine, the point rounded to FP32 once from FP32-rounded
+    // barycentrics u, v and 1 - u - v): near the surface the normal is (p - cp) / |p - cp|, and a closest
+    // point carrying FP32 rounding would put an error of about ulp(p) / |p - cp| into it (4e-3 for a node
+    // 2e-4 cells off the surface). The sign is the side of the feature's pseudonormal, in FP64.
     MPM_HD MeshHit finish(const MeshTri* __restrict__ tris, const float p[3], const double pd[3]) {
         MeshHit hit;
         hit.tri = tri;
         hit.sign = 1.f;
         if (tri < 0) return hit;
         const MeshTri& t = tris[tri];
-        float bb[3] = {bary[0], bary[1], bary[2]};
-        int rg = region;
-        if (best_d >= 0.0) {  // the winner was settled in FP64: take its region from the FP64 evaluation too
-            double bd[3];
-            tri_dist2_exact(t, pd, bd, &rg);
-            bb[0] = (float)bd[0]; bb[1] = (float)bd[1]; bb[2] = (float)bd[2];
-        }
+        double bd[3];
+        int rg;
+        tri_dist2_exact(t, pd, bd, &rg);
+        const double u = (float)bd[0], v = (float)bd[1], w = dsub(dsub(1.0, u), v);
+        double cpd[3];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) hit.cp[k] = bb[0] * t.a[k] + bb[1] * t.b[k] + bb[2] * t.c[k];
+        for (int k = 0; k < 3; ++k) {
+            const double a = t.a[k], b = t.b[k], c = t.c[k];
+            cpd[k] = dadd(dadd(dmul(bd[0], a), dmul(bd[1], b)), dmul(bd[2], c));
+            hit.cp[k] = (float)dadd(dadd(dmul(u, a), dmul(v, b)), dmul(w, c));
+        }
         const float* pn = rg == 0 ? t.fn : (rg <= 3 ? t.vn[rg - 1] : t.en[rg - 4]);
-        float s = (p[0] - hit.cp[0]) * pn[0] + (p[1] - hit.cp[1]) * pn[1] + (p[2] - hit.cp[2]) * pn[2];
-        hit.sign = s >= 0.f ? 1.f : -1.f;
+        const double s = dadd(dadd(dmul(dsub(pd[0], cpd[0]), (double)pn[0]), dmul(dsub(pd[1], cpd[1]), (double)pn[1])),
+                              dmul(dsub(pd[2], cpd[2]), (double)pn[2]));
+        hit.sign = s >= 0.0 ? 1.f : -1.f;
+        (void)p;
         return hit;
     }
 };
@@ -862,25 +878,28 @@ MPM_HD void collider_sdf(const ColliderDev& c, const ColliderPose& pose, const B
 #endif
         h = mesh_closest_sdf(c, nodes + c.node_offset, tris + c.tri_offset, cells, cand, pl, query_tol(c, pl));
     if (h.tri < 0) return;  // empty mesh, or a far voxel
-    float off[3] = {pl[0] - h.cp[0], pl[1] - h.cp[1], pl[2] - h.cp[2]};
+    // the offset to the surface in world space, its length and direction, in the reference's order
+    const float off[3] = {fsub(pl[0], h.cp[0]), fsub(pl[1], h.cp[1]), fsub(pl[2], h.cp[2])};
     float d[3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) d[r] = pose.M[r][0] * off[0] + pose.M[r][1] * off[1] + pose.M[r][2] * off[2];
-    float dist = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for (int r = 0; r < 3; ++r) d[r] = fdot3(pose.M[r], off);
+    const float dist = fsqrt(fdot3(d, d));
     if (dist > 1.0e-9f) {
-        float k = h.sign / dist;
-        n[0] = d[0] * k; n[1] = d[1] * k; n[2] = d[2] * k;
+        const float k = fdiv(h.sign, dist);
+        n[0] = fmul(d[0], k); n[1] = fmul(d[1], k); n[2] = fmul(d[2], k);
     } else {  // on the surface: the face normal mapped by the inverse transpose
         const float* fn = tris[c.tri_offset + h.tri].fn;
         float tn[3];
 #pragma unroll
-        for (int r = 0; r < 3; ++r) tn[r] = pose.Minv[0][r] * fn[0] + pose.Minv[1][r] * fn[1] + pose.Minv[2][r] * fn[2];
-        float l = sqrtf(tn[0] * tn[0] + tn[1] * tn[1] + tn[2] * tn[2]);
-        float k = l > 0.f ? 1.f / l : 0.f;
-        n[0] = tn[0] * k; n[1] = tn[1] * k; n[2] = tn[2] * k;
+        for (int r = 0; r < 3; ++r)
+            tn[r] = fadd(fadd(fmul(pose.Minv[0][r], fn[0]), fmul(pose.Minv[1][r], fn[1])), fmul(pose.Minv[2][r], fn[2]));
+        const float l = fsqrt(fdot3(tn, tn));
+        n[0] = l > 0.f ? fdiv(tn[0], l) : 0.f;
+        n[1] = l > 0.f ? fdiv(tn[1], l) : 0.f;
+        n[2] = l > 0.f ? fdiv(tn[2], l) : 0.f;
     }
     if (!c.closed && h.sign < 0.f && dist > thickness) return;
-    *phi = h.sign * dist;
+    *phi = fmul(h.sign, dist);
 }
 
 // colliders.py:68-74: velocity of the collider material point at p (central difference of the pose in s)
@@ -888,7 +907,7 @@ MPM_HD void collider_velocity(const ColliderPose& c, const float p[3], float out
     float pl[3];
     to_local(c, p, pl);
 #pragma unroll
-    for (int r = 0; r < 3; ++r) out[r] = c.dM[r][0] * pl[0] + c.dM[r][1] * pl[1] + c.dM[r][2] * pl[2] + c.dM[r][3];
+    for (int r = 0; r < 3; ++r) out[r] = fadd(fdot3(c.dM[r], pl), c.dM[r][3]);
 }
 
 }  // namespace mpm

@@ -429,24 +429,24 @@ MPM_HD void grid_node_colliders(const GridDesc& g, float4* node, const int idx[3
         const ColliderDev& col = cd.cols[c];
         float n[3], phi;
         collider_sdf<kWarp>(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, pos, g.thickness, n, &phi);
-        if (phi < g.band) {
+        if (phi < g.band) {  // the response in the reference's operation order, each operation rounded
             float vcol[3];
             collider_velocity(cd.poses[c], pos, vcol);
-            float rel[3] = {vel[0] - vcol[0], vel[1] - vcol[1], vel[2] - vcol[2]};
-            float vn = rel[0] * n[0] + rel[1] * n[1] + rel[2] * n[2];
+            const float rel[3] = {fsub(vel[0], vcol[0]), fsub(vel[1], vcol[1]), fsub(vel[2], vcol[2])};
+            const float vn = fdot3(rel, n);
             if (vn < 0.0f) {
-                float rt[3] = {rel[0] - vn * n[0], rel[1] - vn * n[1], rel[2] - vn * n[2]};
-                float rt_len = sqrtf(rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2]);
+                float rt[3] = {fsub(rel[0], fmul(vn, n[0])), fsub(rel[1], fmul(vn, n[1])), fsub(rel[2], fmul(vn, n[2]))};
+                const float rt_len = fsqrt(fdot3(rt, rt));
                 if (rt_len > 0.0f) {
-                    float f = fmaxf(0.0f, 1.0f - col.friction * (-vn) / rt_len);
-                    rt[0] *= f; rt[1] *= f; rt[2] *= f;
+                    const float f = fmaxf(0.0f, fsub(1.0f, fdiv(fmul(col.friction, -vn), rt_len)));
+                    rt[0] = fmul(rt[0], f); rt[1] = fmul(rt[1], f); rt[2] = fmul(rt[2], f);
                 }
                 if (phi < 0.0f) {  // behind the surface: no penetration
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) vel[a] = vcol[a] + rt[a];
+                    for (int a = 0; a < 3; ++a) vel[a] = fadd(vcol[a], rt[a]);
                 } else {  // in the band: friction only
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) vel[a] = vcol[a] + rt[a] + vn * n[a];
+                    for (int a = 0; a < 3; ++a) vel[a] = fadd(fadd(vcol[a], rt[a]), fmul(vn, n[a]));
                 }
             }
         }
@@ -716,15 +716,16 @@ MPM_HD void project_particle(const Particles& P, int64_t p, const GridDesc& g, c
         const ColliderDev& col = cd.cols[c];
         float n[3], phi;
         collider_sdf<kWarp>(col, cd.poses[c], cd.nodes, cd.tris, cd.cells, cd.cand, nx, g.thickness, n, &phi);
-        if (phi < 0.0f) {
+        if (phi < 0.0f) {  // in the reference's operation order, each operation rounded
 #pragma unroll
-            for (int a = 0; a < 3; ++a) nx[a] = nx[a] - phi * n[a];
+            for (int a = 0; a < 3; ++a) nx[a] = fsub(nx[a], fmul(phi, n[a]));
             float vcol[3];
             collider_velocity(cd.poses[c], nx, vcol);
-            float vn = (nv[0] - vcol[0]) * n[0] + (nv[1] - vcol[1]) * n[1] + (nv[2] - vcol[2]) * n[2];
+            const float rel[3] = {fsub(nv[0], vcol[0]), fsub(nv[1], vcol[1]), fsub(nv[2], vcol[2])};
+            const float vn = fdot3(rel, n);
             if (vn < 0.0f) {
 #pragma unroll
-                for (int a = 0; a < 3; ++a) nv[a] = nv[a] - vn * n[a];
+                for (int a = 0; a < 3; ++a) nv[a] = fsub(nv[a], fmul(vn, n[a]));
             }
         }
     }

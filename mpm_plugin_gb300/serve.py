@@ -27,7 +27,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from mpm_plugin_gb300.interface import ParticleData
+from mpm_plugin_gb300.interface import ParticleData, domain_grid_dims
 
 PARTICLE_BYTES = 136  # arena words per particle x 4 B (x v C F Jp stress mat emitter id)
 
@@ -59,7 +59,7 @@ def estimate_device_bytes(domain, max_particles: int, collider_triangles: int = 
     """Upper estimate of a job's device memory: two particle arenas plus per-particle sort, removal and
     candidate scratch, the padded blocked grid with its work lists and occupancy scratch, and the colliders'
     BVHs and narrow-band voxel grids. Capacity doubles on growth, so particles count twice."""
-    dims = [s + 6 for s in domain.grid_shape]
+    dims = domain_grid_dims(domain)
     nodes = math.prod(-(-d // 4) * 4 for d in dims)
     cap = 2 * max(int(max_particles), 4096)
     per_particle = 2 * PARTICLE_BYTES + 12 + 16 + 4 + 72

@@ -13,7 +13,7 @@ from collections.abc import Sequence
 import numpy as np
 
 from mpm_plugin_gb300 import _abi
-from mpm_plugin_gb300.interface import AdvanceStats, ColliderGeometry, ParticleData, Solver
+from mpm_plugin_gb300.interface import AdvanceStats, ColliderGeometry, ParticleData, Solver, domain_desc
 
 STATE_KEYS = ("x", "v", "C", "F", "Jp", "mat", "emitter")
 _SHAPES = {"x": ((3,), np.float32), "v": ((3,), np.float32), "C": ((3, 3), np.float32), "F": ((3, 3), np.float32),
@@ -112,14 +112,7 @@ class Gb300Solver(Solver):
         for m in self.materials:
             if m.model not in _abi.MODEL_IDS:
                 raise NotImplementedError(f"material model {m.model!r} is not supported by the gb300 backend")
-        d = _abi.MpmDomainDesc()
-        for a, ax in enumerate("xyz"):
-            d.min[a] = domain.min[a]
-            d.max[a] = domain.max[a]
-            d.wall_lo[a] = int(bool(domain.walls[f"{ax}-"]))
-            d.wall_hi[a] = int(bool(domain.walls[f"{ax}+"]))
-        d.resolution = int(domain.resolution)
-        d.wall_friction = float(domain.wall_friction)
+        d = domain_desc(domain)
         mats = (_abi.MpmMaterialDesc * max(1, len(self.materials)))()
         for i, m in enumerate(self.materials):
             mats[i] = _abi.MpmMaterialDesc(_abi.MODEL_IDS[m.model], m.youngs_modulus, m.poisson_ratio, m.density,
@@ -299,10 +292,15 @@ class Gb300Solver(Solver):
         self._check(self._lib.mpm_kernel_times(self._h, 5, ms, n, int(reset)))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_abi.KERNEL_SLOTS + ("substep",))}
 
-    def read_grid(self) -> np.ndarray:
-        """(dims..., 4) float32: node velocity (momentum where the mass is 0) and mass after the last substep."""
+    def grid_dims(self) -> tuple[int, int, int]:
+        """Nodes per axis of the padded grid (grid shape + 6)."""
         dims = (C.c_int32 * 3)()
         self._check(self._lib.mpm_grid_dims(self._h, dims))
+        return int(dims[0]), int(dims[1]), int(dims[2])
+
+    def read_grid(self) -> np.ndarray:
+        """(dims..., 4) float32: node velocity (momentum where the mass is 0) and mass after the last substep."""
+        dims = self.grid_dims()
         out = np.zeros((dims[0], dims[1], dims[2], 4), np.float32)
         self._check(self._lib.mpm_read_grid(self._h, _ptr(out)))
         return out

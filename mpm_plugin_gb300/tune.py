@@ -153,7 +153,7 @@ def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20,
     run_substeps calls (the way a fixed-dt workload of many substeps per call runs) instead of single
     substeps."""
     gkey, sms = gpu_key(solver.device)
-    wkey = workload_key(max(solver.domain.grid_shape), solver.particle_count, solver._n_colliders > 0, deterministic)
+    wkey = workload_key(max(solver.grid_dims()) - 6, solver.particle_count, solver._n_colliders > 0, deterministic)
     if runs:
         wkey += "|runs"
     cache = load_cache(path)
@@ -188,7 +188,7 @@ def tune_batch(batch, frame_dt: float, frames: int = 2, path: Path | None = None
     scenes = batch.scenes
     gkey, sms = gpu_key(scenes[0].device)
     n = sum(s.particle_count for s in scenes)
-    res = max(max(s.domain.grid_shape) for s in scenes)
+    res = max(max(s.grid_dims()) - 6 for s in scenes)
     wkey = "batch|" + workload_key(res, n, any(s._n_colliders > 0 for s in scenes)) + f"|scenes{len(scenes)}"
     cache = load_cache(path)
     hit = cache.get(gkey, {}).get(wkey)

@@ -201,14 +201,16 @@ class OracleSolver:
 
     # -- state (warp/solver.py:82-138)
     def _set(self, s):
+        """Copies of the given arrays (the kernels update the state in place; the caller's arrays stay as
+        they were, as the reference's state upload leaves them)."""
         r = self.real
-        self.x = np.ascontiguousarray(np.asarray(s["x"], r).reshape(-1, 3))
-        self.v = np.ascontiguousarray(np.asarray(s["v"], r).reshape(-1, 3))
-        self.C = np.ascontiguousarray(np.asarray(s["C"], r).reshape(-1, 3, 3))
-        self.F = np.ascontiguousarray(np.asarray(s["F"], r).reshape(-1, 3, 3))
-        self.Jp = np.ascontiguousarray(np.asarray(s["Jp"], r).reshape(-1))
-        self.mat = np.ascontiguousarray(np.asarray(s["mat"], np.int32).reshape(-1))
-        self.emitter = np.ascontiguousarray(np.asarray(s["emitter"], np.int32).reshape(-1))
+        self.x = np.array(s["x"], r, order="C").reshape(-1, 3)
+        self.v = np.array(s["v"], r, order="C").reshape(-1, 3)
+        self.C = np.array(s["C"], r, order="C").reshape(-1, 3, 3)
+        self.F = np.array(s["F"], r, order="C").reshape(-1, 3, 3)
+        self.Jp = np.array(s["Jp"], r, order="C").reshape(-1)
+        self.mat = np.array(s["mat"], np.int32, order="C").reshape(-1)
+        self.emitter = np.array(s["emitter"], np.int32, order="C").reshape(-1)
         self.present = np.unique(self.mat)
 
     def load_state(self, s):

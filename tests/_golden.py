@@ -7,7 +7,36 @@ from pathlib import Path
 
 import numpy as np
 
-from mpm_plugin_gb300.interface import Domain, MaterialParams
+from dataclasses import fields
+
+from mpm_plugin_gb300.interface import Domain as _Domain
+from mpm_plugin_gb300.interface import MaterialParams
+from oracle.oracle import domain_dx, domain_grid_shape
+
+WALL_SIDES = ("x-", "x+", "y-", "y+", "z-", "z+")
+
+
+class Domain(_Domain):
+    """The interface's Domain (mpm_core's, or the data-only stand-in) with dx and grid_shape from the oracle's
+    restatement of mpm_core/scene.py:60-67, so tests read the same either way; every wall side is listed."""
+
+    def __init__(self, min, max, resolution, walls=None, wall_friction=0.5):  # noqa: A002
+        super().__init__(tuple(min), tuple(max), resolution, {**{s: True for s in WALL_SIDES}, **(walls or {})},
+                         wall_friction)
+
+    @property
+    def dx(self) -> float:
+        return domain_dx(self)
+
+    @property
+    def grid_shape(self) -> tuple[int, int, int]:
+        return domain_grid_shape(self)
+
+
+def material_from_dict(d: dict) -> MaterialParams:
+    """A MaterialParams from a preset's material table (keys that are not fields are ignored)."""
+    known = {f.name for f in fields(MaterialParams)}
+    return MaterialParams(**{k: v for k, v in d.items() if k in known})
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 STATE_KEYS = ("x", "v", "C", "F", "Jp", "mat", "emitter")
@@ -23,7 +52,7 @@ class Case:
         self.meta = json.loads(str(self.z["meta"]))
         d = self.meta["domain"]
         self.domain = Domain(tuple(d["min"]), tuple(d["max"]), d["resolution"], d["walls"], d["wall_friction"])
-        self.materials = [MaterialParams.from_dict(m) for m in self.meta["materials"]]
+        self.materials = [material_from_dict(m) for m in self.meta["materials"]]
         self.gravity = tuple(self.meta["gravity"])
         self.ppc = self.meta["ppc"]
         self.action = self.meta["action"]

@@ -140,12 +140,13 @@ class SubstepEmulator:
 
     def load_state(self, s):
         n = len(s["x"])
-        self.state = {"x": np.ascontiguousarray(np.asarray(s["x"], np.float32).reshape(n, 3).T),
-                      "v": np.ascontiguousarray(np.asarray(s["v"], np.float32).reshape(n, 3).T),
-                      "C": np.ascontiguousarray(np.asarray(s["C"], np.float32).reshape(n, 9).T),
-                      "F": np.ascontiguousarray(np.asarray(s["F"], np.float32).reshape(n, 9).T),
-                      "Jp": np.ascontiguousarray(np.asarray(s["Jp"], np.float32).reshape(n)),
-                      "mat": np.ascontiguousarray(np.asarray(s["mat"], np.int32).reshape(n)),
+        # copies: the substep updates these in place, and the caller's arrays must stay as they were
+        self.state = {"x": np.array(np.asarray(s["x"], np.float32).reshape(n, 3).T, order="C"),
+                      "v": np.array(np.asarray(s["v"], np.float32).reshape(n, 3).T, order="C"),
+                      "C": np.array(np.asarray(s["C"], np.float32).reshape(n, 9).T, order="C"),
+                      "F": np.array(np.asarray(s["F"], np.float32).reshape(n, 9).T, order="C"),
+                      "Jp": np.array(s["Jp"], np.float32, order="C").reshape(n),
+                      "mat": np.array(s["mat"], np.int32, order="C").reshape(n),
                       "emitter": np.asarray(s["emitter"], np.int32).copy(),
                       "tau": np.zeros((6, n), np.float32)}
         self.stress_valid = False

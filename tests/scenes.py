@@ -9,9 +9,9 @@ from __future__ import annotations
 import json
 
 import numpy as np
-from _golden import GOLDEN
+from _golden import GOLDEN, Domain, material_from_dict
 
-from mpm_plugin_gb300.interface import Domain, MaterialParams
+from mpm_plugin_gb300.interface import MaterialParams
 from oracle import geometry
 
 WALL_SIDES = ("x-", "x+", "y-", "y+", "z-", "z+")
@@ -22,7 +22,7 @@ _PRESETS = json.loads(str(np.load(GOLDEN / "geometry.npz")["meta"]))["presets"]
 
 def preset(name: str) -> MaterialParams:
     """Material parameters of the reference's built-in preset ``name`` (mpm_core/presets/*.toml)."""
-    return MaterialParams.from_dict(_PRESETS[name]["material"])
+    return material_from_dict(_PRESETS[name]["material"])
 
 
 def preset_names() -> list[str]:

@@ -15,11 +15,10 @@ from scenes import add, box_particles, domain, mix_scene, perturbed_state, prese
 
 pytestmark = pytest.mark.gpu
 
-# Tolerances against the reference fixtures: float atomics make the P2G sum order differ, and FMA
-# contraction changes last-bit rounding, both at the 1e-7 level. Cases with mesh colliders see a few more
-# because a contact branch (phi < band, vn < 0) can flip on a last-bit difference.
+# Tolerance against the reference fixtures, the same for every fixture, colliders and multi-substep runs
+# included: float atomics make the P2G sum order differ, and FMA contraction changes last-bit rounding, both
+# at the 1e-7 level. C is measured against the velocity-gradient scale |v| / dx.
 TOL = {"x": 1e-5, "v": 1e-5, "C": 1e-5, "F": 1e-5, "Jp": 1e-5}
-TOL_COLLIDER = {"x": 1e-5, "v": 1e-3, "C": 1e-3, "F": 1e-5, "Jp": 1e-5}
 
 
 def gpu_solver(domain_, materials, gravity=(0.0, 0.0, -9.81), ppc=8):
@@ -57,12 +56,10 @@ def test_matches_reference_fixture(name):
     np.testing.assert_array_equal(out["emitter"], ref["emitter"])
     for k in ("x", "v"):
         np.testing.assert_array_equal(np.isfinite(out[k]), np.isfinite(ref[k]))
-    tol = TOL_COLLIDER if case.meta["colliders"] else TOL
-    if case.action["kind"] == "advance" or case.action.get("count", 1) > 1:
-        tol = {k: 10 * v for k, v in tol.items()}  # several substeps amplify rounding differences
-    errs = {k: rel_err(out[k], ref[k]) for k in tol}
-    print(name, {k: f"{e:.2e}" for k, e in errs.items()})
-    for k, t in tol.items():
+    gnorm = float(np.linalg.norm(ref["v"][np.isfinite(ref["v"]).all(1)]) / case.domain.dx)
+    errs = {k: rel_err(out[k], ref[k], floor=gnorm if k == "C" else 0.0) for k in TOL}
+    print(name, len(ref["x"]), {k: f"{e:.2e}" for k, e in errs.items()})
+    for k, t in TOL.items():
         assert errs[k] <= t, (k, errs[k])
     if "stats" in extra:
         np.testing.assert_allclose(extra["stats"], case.z["stats"], rtol=1e-12)

@@ -106,19 +106,24 @@ def test_emission_times():
 
 
 def test_material_constants():
-    from mpm_plugin_gb300.interface import MaterialParams
+    from _golden import material_from_dict
 
     meta = json.loads(str(np.load(GOLDEN / "geometry.npz")["meta"]))
     for pid, p in meta["presets"].items():
-        m = MaterialParams.from_dict(p["material"])
+        m = material_from_dict(p["material"])
         assert lame(m) == (p["mu"], p["lam"])
         assert dp_alpha(m.friction_angle_deg) == p["alpha"]
 
 
 def test_domain_constants():
-    from mpm_plugin_gb300.interface import Domain
+    """dx and the grid shape the reference derives from a domain, against the oracle's restatement and the
+    library's own (mpm_domain_grid_dims: grid shape + 6 padding nodes), which needs no GPU."""
+    from _golden import Domain
+
+    from mpm_plugin_gb300.interface import domain_grid_dims
 
     meta = json.loads(str(np.load(GOLDEN / "geometry.npz")["meta"]))
     for d in meta["domains"]:
         dom = Domain(tuple(d["min"]), tuple(d["max"]), d["resolution"])
         assert dom.dx == d["dx"] and list(dom.grid_shape) == d["grid_shape"]
+        assert list(domain_grid_dims(dom)) == [s + 6 for s in d["grid_shape"]]

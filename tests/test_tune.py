@@ -49,8 +49,8 @@ class _FakeSolver:
     particle_count = 32_768
     _n_colliders = 0
 
-    class domain:
-        grid_shape = (64, 64, 64)
+    def grid_dims(self):
+        return (70, 70, 70)
 
     def __init__(self):
         self.state, self.opts, self.loads = 0, {}, 0
