@@ -241,6 +241,22 @@ void emu_collider_sdf(void* ev, int c, float s, int use_sdf, int n, const float*
     }
 }
 
+// The C++ host decomposition of a world matrix (mpm_host.h decompose): t (3), q (4, x y z w), S (9)
+void host_decompose(const float* m16, double* t, double* q, double* S) {
+    double min_sv;
+    decompose(m16, t, q, S, &min_sv);
+}
+
+// The collider pose the kernels use at substep fraction s for the pose pair (start, end): M (12, 3x4)
+void host_collider_matrix(const float* start16, const float* end16, double dx, float s, float* M12) {
+    ColliderDev col{};
+    collider_set_pose(col, start16, end16, dx);
+    ColliderPose pose;
+    collider_pose_at(col, s, 1.0f, pose);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) M12[r * 4 + c] = pose.M[r][c];
+}
+
 void emu_read_grid(void* ev, float* out) {
     Emu* e = static_cast<Emu*>(ev);
     const GridDesc& g = e->g;

@@ -53,6 +53,8 @@ def lib():
     L.emu_use_sdf.argtypes = [P, C.c_int]
     L.emu_particle_stress.argtypes = [P, C.c_int64, P, P, P, P]
     L.emu_collider_sdf.argtypes = [P, C.c_int, C.c_float, C.c_int, C.c_int, P, P]
+    L.host_decompose.argtypes = [P, P, P, P]
+    L.host_collider_matrix.argtypes = [P, P, C.c_double, C.c_float, P]
     _lib = L
     return L
 
@@ -75,6 +77,23 @@ def stress(F, model, mu, lam):
     tau = np.zeros_like(F)
     lib().stress_batch(len(F), model, _p(F), mu, lam, _p(tau))
     return tau
+
+
+def decompose(m):
+    """(t, q, S) of a world matrix by the library's C++ decomposition (float32 matrix in, float64 out)."""
+    m = np.ascontiguousarray(np.asarray(m, np.float32).reshape(4, 4))
+    t, q, S = np.zeros(3), np.zeros(4), np.zeros(9)
+    lib().host_decompose(_p(m), _p(t), _p(q), _p(S))
+    return t, q, S.reshape(3, 3)
+
+
+def collider_matrix(start, end, s, dx=1.0):
+    """The 3x4 pose the kernels evaluate at substep fraction s between world matrices start and end."""
+    a = np.ascontiguousarray(np.asarray(start, np.float32).reshape(4, 4))
+    b = np.ascontiguousarray(np.asarray(end, np.float32).reshape(4, 4))
+    out = np.zeros(12, np.float32)
+    lib().host_collider_matrix(_p(a), _p(b), dx, s, _p(out))
+    return out.reshape(3, 4)
 
 
 class HostMesh:

@@ -1,9 +1,13 @@
-"""The backend's device math built for the host (CPU only): SVD accuracy, stress accuracy, mesh queries."""
+"""The backend's device math built for the host (CPU only): SVD accuracy, stress accuracy, mesh queries, and
+the collider pose decomposition and interpolation against the reference's recorded outputs."""
 
 from __future__ import annotations
 
+import json
+
 import numpy as np
 import pytest
+from _golden import GOLDEN
 from device_math import HostMesh, stress, svd
 from scenes import icosphere, plane_mesh, unit_cube_mesh
 
@@ -168,3 +172,37 @@ def test_closest_point_against_independent_method(mesh):
         assert abs(np.linalg.norm(cp[i] - p) - exact) < 2e-6 * (1 + exact), i
         _, _, _, _, d2 = om.query(p)
         assert abs(np.sqrt(d2) - exact) < 1e-9 * (1 + exact), i
+
+
+def test_pose_decomposition_matches_reference():
+    """The library's C++ decomposition of a collider's world matrix (mpm_host.h decompose, the host side of
+    warp/solver.py:154-172) against the reference's geometry.decompose_transform (geometry.py:30-39) on its
+    recorded outputs: 24 seeded matrices with non-uniform, uniform and mirrored scales. The quaternion is
+    compared up to sign (q and -q are one rotation; the solver flips the end pose to the short way round)."""
+    from device_math import decompose
+
+    z = np.load(GOLDEN / "geometry.npz")
+    for m, t_ref, q_ref, S_ref in zip(z["mats"], z["t"], z["q"], z["S"]):
+        t, q, S = decompose(m)
+        np.testing.assert_allclose(t, t_ref, rtol=0, atol=1e-12)
+        sign = 1.0 if np.dot(q, q_ref) >= 0 else -1.0
+        np.testing.assert_allclose(sign * q, q_ref, rtol=0, atol=1e-12)
+        np.testing.assert_allclose(S, S_ref, rtol=0, atol=1e-12 * np.abs(S_ref).max())
+
+
+def test_collider_pose_matches_reference_interpolation():
+    """The pose the kernels evaluate at a substep fraction s (decomposed poses, slerped rotation, lerped
+    stretch and translation; colliders.py:30-37) against the reference's geometry.interpolate_transform
+    (geometry.py:69-86) on its recorded outputs for 12 matrix pairs at s = 0, 0.25, 0.5, 0.8, 1: the same
+    motion up to FP32 rounding."""
+    from device_math import collider_matrix
+
+    z = np.load(GOLDEN / "geometry.npz")
+    svals = json.loads(str(z["meta"]))["svals"]
+    mats = z["mats"]
+    for i, row in enumerate(z["interp"]):
+        a, b = mats[2 * i], mats[2 * i + 1]
+        for s, ref in zip(svals, row):
+            M = collider_matrix(a, b, s)
+            scale = np.abs(ref[:3]).max()
+            np.testing.assert_allclose(M, ref[:3], rtol=0, atol=1e-6 * scale, err_msg=f"pair {i} s {s}")
