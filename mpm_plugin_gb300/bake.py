@@ -1,7 +1,7 @@
 """Bake runner entry point with the gb300 backend registered.
 
     python -m mpm_plugin_gb300.bake CACHE_DIR [--device cuda:0] [--resume] [--watch-stdin] [--host-sampling]
-                                    [--sync-io]
+                                    [--sync-io] [--deterministic]
 
 Runs the reference's own, unchanged runner (``mpm_core.bake.main``) with ``--backend gb300`` unless another
 backend is named; needs the reference package on the path. Around it:
@@ -11,6 +11,8 @@ backend is named; needs the reference package on the path. Around it:
   bit for bit;
 * the gb300 solvers the runner creates read each frame's whole state in one copy, shared by the frame's
   get_particles and save_state (bake.py:195-201);
+* with --deterministic the gb300 solvers run in deterministic mode (fixed-point P2G: the same cache, bit for
+  bit, on every run of the same scene);
 * unless --sync-io is given, the frame files and checkpoints (``CacheWriter.write_frame``,
   ``write_checkpoint``, cache.py:131-160) are written by the same functions on one writer thread, in the
   order the runner asks for them, while the next frame simulates. Every file is still written atomically
@@ -118,10 +120,21 @@ def main(argv: list[str] | None = None) -> int:
     import mpm_core.bake as runner
     from mpm_core.backends import register_backend
 
+    from mpm_plugin_gb300 import _abi
     from mpm_plugin_gb300.solver import Gb300Solver
 
-    register_backend(mpm_plugin_gb300.BACKEND_NAME, lambda **kw: Gb300Solver(**kw, frame_reads=True))
     argv = list(sys.argv[1:] if argv is None else argv)
+    deterministic = "--deterministic" in argv
+    if deterministic:
+        argv.remove("--deterministic")
+
+    def factory(**kw):
+        solver = Gb300Solver(**kw, frame_reads=True)
+        if deterministic:
+            solver.set_option(_abi.OPT_DETERMINISTIC, 1)
+        return solver
+
+    register_backend(mpm_plugin_gb300.BACKEND_NAME, factory)
     if "--host-sampling" in argv:
         argv.remove("--host-sampling")
     else:

@@ -283,3 +283,50 @@ def cylinder(radius: float, height: float, segments: int = 32):
         k1 = (k + 1) % segments
         tris += [[k, k1, segments + k1], [k, segments + k1, segments + k], [bc, k1, k], [tc, segments + k, segments + k1]]
     return verts.astype(np.float32), np.array(tris, np.int32)
+
+
+def bake_scene(resolution: int = 16, frame_end: int = 4, emit_frames=(1, 3), substeps: int = 2,
+               preset_name: str = "jelly", velocity=(0.0, 0.0, -1.0)):
+    """A scene for the reference's bake runner (needs mpm_core): unit-cube domain, one closed cube inflow
+    emitter "pour" above the floor (active over emit_frames, `substeps` emissions per frame), one open plane
+    collider drifting along x by a cell per frame, jelly or another preset. Returns a SceneDescription."""
+    from mpm_core.materials import load_preset
+    from mpm_core.scene import Collider, Emitter, SceneDescription
+    from mpm_core.scene import Domain as CoreDomain
+    from mpm_core.scene import MeshData as CoreMesh
+
+    n = frame_end
+    dx = 1.0 / resolution
+    cube_v, cube_t = unit_cube_mesh()
+    emitter = Emitter(name="pour", kind="inflow", material=0, mesh=CoreMesh(cube_v, cube_t),
+                      transforms=np.repeat((translate(0.35, 0.35, 0.55) @ scale(0.3, 0.3, 0.25))[None], n, 0),
+                      velocity=tuple(velocity), frame_start=emit_frames[0], frame_end=emit_frames[1],
+                      substeps=substeps)
+    pv, pt = plane_mesh(0.8)
+    floor = Collider(name="floor", mesh=CoreMesh(pv, pt),
+                     transforms=np.stack([translate(0.5 + k * dx, 0.5, 0.1) for k in range(n)]), friction=0.5,
+                     closed=False)
+    return SceneDescription(domain=CoreDomain((0.0, 0.0, 0.0), (1.0, 1.0, 1.0), resolution),
+                            materials=[load_preset(preset_name).material], emitters=[emitter], colliders=[floor],
+                            frame_start=1, frame_end=frame_end)
+
+
+def cache_contents(cache_dir) -> dict:
+    """{relative path: content} of a bake cache for comparisons: every frame and checkpoint archive as its
+    members' raw bytes (the .npy payloads; zip member timestamps left out), cache.json as text. The progress
+    file (timings) is left out."""
+    import zipfile
+    from pathlib import Path
+
+    root = Path(cache_dir)
+    out = {}
+    for p in sorted(root.rglob("*")):
+        rel = str(p.relative_to(root))
+        if p.is_dir() or rel.startswith("scene") or rel in ("progress.json", "bake.lock"):
+            continue
+        if p.suffix == ".npz":
+            with zipfile.ZipFile(p) as z:
+                out[rel] = {name: z.read(name) for name in sorted(z.namelist())}
+        else:
+            out[rel] = p.read_bytes()
+    return out
