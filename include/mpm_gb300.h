@@ -142,13 +142,19 @@ enum {
                                   (default) never, 1 always (without kernel timing, the FP64 clamp or the tile
                                   P2G), 2 for scenes of up to 131,072 particles. Slower than the graphs of
                                   separate kernels on a GB300 at the sizes measured */
-    MPM_OPT_FUSED_P2G = 12     /* 1: two grids that alternate between substeps; G2P adds each particle it has
+    MPM_OPT_FUSED_P2G = 12,    /* 1: two grids that alternate between substeps; G2P adds each particle it has
                                   updated to the next substep's grid right away (and the collider projection
                                   the particles it moved), so the next substep's P2G reads no particle state.
                                   Within mpm_advance / mpm_run_substeps, and between mpm_substep calls with the
                                   same dt (a scatter for a call that does not follow is dropped). Not in
                                   deterministic mode, with the FP64 clamp or in a batch (those run one grid).
                                   Costs a second grid of device memory. 0 (default) */
+    MPM_OPT_BLOCK_SWEEP = 13   /* 1: P2G marks the grid blocks it touches with plain stores, and a short kernel
+                                  after it lists the marked blocks (a sweep over the block flags) for the grid
+                                  update; 0 (default): P2G lists a block itself the first time it touches it
+                                  (an atomic exchange on the flag and an atomic add on the list's length).
+                                  One grid only (two-grid mode, cooperative launches and batches list
+                                  blocks in P2G) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

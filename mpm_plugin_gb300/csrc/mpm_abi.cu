@@ -423,6 +423,8 @@ SubstepArgs substep_args(Handle* h) {
     a.fixed_exp = h->fixed_exp;
     a.p2g_group = h->shape.p2g_group;
     a.fp64_clamp = h->fp64_clamp ? 1 : 0;
+    a.err = h->d_coop + 3;
+    a.block_sweep = h->shape.block_sweep && !two_grids(h) && !h->shape.p2g_tile ? 1 : 0;
     return a;
 }
 
@@ -529,9 +531,9 @@ Status run_substep(Handle* h, int reps = 1) {
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
                                      (int64_t)h->shape.list_ctas,
-                                     ((((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
+                                     (((((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
                                                 2 + (h->fp64_clamp ? 1 : 0)) * 2 + h->shape.p2g_tile) * 2 +
-                                              (a.grid2 ? 1 : 0)) * 64 + reps};
+                                              (a.grid2 ? 1 : 0)) * 2 + a.block_sweep) * 64 + reps};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -626,6 +628,7 @@ Status run_coop(Handle* h, int reps) {
     TRY(ensure_part_cand(h));
     SubstepArgs a = substep_args(h);
     a.grid2 = nullptr;  // one grid (coop_eligible excludes two-grid mode)
+    a.block_sweep = 0;  // the cooperative kernel's P2G lists the blocks itself
     CK(launch_substeps_coop(h->stream, a, reps, h->d_coop));
     h->launches += 1;
     h->coop_used = true;
@@ -634,11 +637,18 @@ Status run_coop(Handle* h, int reps) {
 
 // After a synchronisation: fails if a grid barrier of a cooperative launch gave up waiting.
 Status check_coop(Handle* h) {
-    if (!h->coop_used) return {};
+    unsigned int err[2] = {0u, 0u};
+    if (!h->coop_used && h->shape.g2p_variant != 2) return {};
+    CK(cudaMemcpy(err, h->d_coop + 2, sizeof(err), cudaMemcpyDeviceToHost));
+    if (err[0] && h->coop_used) {
+        h->coop_used = false;
+        return {MPM_ERR_CUDA, "cooperative substeps: a grid barrier timed out"};
+    }
     h->coop_used = false;
-    unsigned int err = 0;
-    CK(cudaMemcpy(&err, h->d_coop + 2, sizeof(err), cudaMemcpyDeviceToHost));
-    if (err) return {MPM_ERR_CUDA, "cooperative substeps: a grid barrier timed out"};
+    if (err[1]) {
+        CK(cudaMemset(h->d_coop + 3, 0, sizeof(unsigned int)));
+        return {MPM_ERR_CUDA, "tile G2P: a wait for its TMA copies timed out"};
+    }
     return {};
 }
 
@@ -964,6 +974,7 @@ Status download_particles(Handle* h, float* x, float* v, float* C, float* F, flo
     CK(get(mat, dm, (size_t)n * 4));
     CK(get(emitter, de, (size_t)n * 4));
     CK(cudaStreamSynchronize(h->stream));
+    TRY(check_coop(h));  // a kernel that gave up a bounded wait since the last check
     return {};
 }
 
@@ -1285,6 +1296,7 @@ Status batch_upload(Batch* b) {
         TRY(prepare_grids(h, false, false));  // a batch runs its scenes in one-grid mode
         table[s] = substep_args(h);
         table[s].grid2 = nullptr;
+        table[s].block_sweep = 0;  // a batch's P2G lists the blocks itself
         table[s].p2g_group = b->shape.p2g_group;
         layout.push_back(h->P.cap);
         ctas += (h->P.cap + 255) / 256;
@@ -1681,7 +1693,7 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
         case MPM_OPT_DETERMINISTIC:
             return finish(h, set_deterministic(h, value != 0));
         case MPM_OPT_G2P_VARIANT:
-            if (value != 0 && value != 1) return finish(h, {MPM_ERR_VALUE, "G2P variant must be 0 or 1"});
+            if (value < 0 || value > 2) return finish(h, {MPM_ERR_VALUE, "G2P variant must be 0, 1 or 2"});
             h->shape.g2p_variant = (int)value;
             return MPM_OK;
         case MPM_OPT_LIST_CTAS:
@@ -1693,6 +1705,9 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             return MPM_OK;
         case MPM_OPT_P2G_TILE:
             h->shape.p2g_tile = value != 0;
+            return MPM_OK;
+        case MPM_OPT_BLOCK_SWEEP:
+            h->shape.block_sweep = value != 0;
             return MPM_OK;
         case MPM_OPT_COOP:
             if (value < 0 || value > 2) return finish(h, {MPM_ERR_VALUE, "cooperative mode must be 0, 1 or 2"});
@@ -1730,7 +1745,7 @@ int mpm_synchronize(void* handle) {
     HANDLE_OR_FAIL(handle);
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
-    return MPM_OK;
+    return finish(h, check_coop(h));
 }
 
 int mpm_kernel_times(void* handle, int32_t n_slots, float* ms, int64_t* launches, int32_t reset) {

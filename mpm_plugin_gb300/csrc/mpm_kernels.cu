@@ -8,6 +8,7 @@
 
 #include "mpm_internal.h"
 #include "mpm_substep_kernels.cuh"
+#include "mpm_tile.cuh"
 
 namespace mpm {
 
@@ -464,6 +465,61 @@ void launch_collider_poses(cudaStream_t st, const ColliderDev* cols, int n_col, 
     k_collider_poses<<<blocks_for(total, 128), 128, 0, st>>>(cols, n_col, poses, steps, s_given, inv_frame_dt);
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against the driver library).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            cudaGetLastError();
+    }
+    return fn;
+}
+
+// The tile G2P's tensor maps for one scene: the arena as a 2-D tensor of floats (particle, plane: cap x 34,
+// rows cap * 4 bytes apart), boxes of 256 x 1; the grid as a 4-D tensor (256 floats of a block, then the
+// blocks along k, j, i), boxes of 2 x 2 x 2 blocks. Out-of-range box parts read as zero.
+static bool encode_tile_maps(const SubstepArgs& a, TileMaps* m) {
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return false;
+    const cuuint64_t pdim[2] = {(cuuint64_t)a.cap, (cuuint64_t)kParticleFields};
+    const cuuint64_t pstride[1] = {(cuuint64_t)a.cap * sizeof(float)};
+    const cuuint32_t pbox[2] = {(cuuint32_t)kTileChunk, 1u};
+    const cuuint32_t ones[4] = {1u, 1u, 1u, 1u};
+    if (fn(&m->planes, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, a.arena, pdim, pstride, pbox, ones,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const GridDesc& g = a.g;
+    const cuuint64_t gdim[4] = {256u, (cuuint64_t)g.nb[2], (cuuint64_t)g.nb[1], (cuuint64_t)g.nb[0]};
+    const cuuint64_t gstride[3] = {1024u, (cuuint64_t)g.nb[2] * 1024u, (cuuint64_t)g.nb[2] * g.nb[1] * 1024u};
+    const cuuint32_t gbox[4] = {256u, 2u, 2u, 2u};
+    return fn(&m->grid, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, a.grid, gdim, gstride, gbox, ones,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The tile G2P (one grid, FP32 return mapping): persistent, at most three CTAs per SM. False when its tensor
+// maps could not be encoded (the caller launches the plain G2P, which gives the same results).
+static bool g2p_tile_launch(cudaStream_t st, const SubstepArgs& a, bool pdl, const OneScene& sc) {
+    TileMaps maps;
+    if (!encode_tile_maps(a, &maps)) return false;
+    const int64_t chunks = (a.n + kTileChunk - 1) / kTileChunk;
+    const unsigned int ctas = (unsigned int)std::min<int64_t>(chunks, (int64_t)sm_count() * 3);
+    launch_step_kernel_smem(k_g2p_tile<3>, ctas, 256, kTileSmemBytes + 128, st, pdl, maps, sc);
+    return true;
+}
+
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing) {
     const unsigned int list_ctas = shape.list_ctas ? shape.list_ctas : sm_count() * kCtasPerSm;
     const OneScene sc{a};
@@ -482,6 +538,12 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
             launch_step_kernel_smem(k_p2g_tile<OneScene>, blocks_for(a.n, 256), 256, kP2gTileBytes, st, pdl, sc);
         else
             launch_step_kernel(k_p2g_scatter<OneScene>, blocks_for(a.n, 256), 256, st, pdl, sc);
+        if (a.block_sweep) {
+            const int64_t nblk = (int64_t)a.g.nb[0] * a.g.nb[1] * a.g.nb[2];
+            launch_step_kernel(k_list_blocks<OneScene>,
+                               (unsigned int)std::min<int64_t>(blocks_for(nblk, 256), (int64_t)sm_count() * kCtasPerSm),
+                               256, st, pdl, sc);
+        }
     }
     mark(2);
     launch_step_kernel(k_grid_update<OneScene>, list_ctas, 256, st, pdl, sc);
@@ -496,6 +558,8 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
             launch_step_kernel(k_g2p<OneScene, 1, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
         else if (shape.g2p_variant == 1)
             launch_step_kernel(k_g2p<OneScene, 1>, blocks_for(a.n, 256), 256, st, pdl, sc);
+        else if (shape.g2p_variant == 2 && g2p_tile_launch(st, a, pdl, sc))
+            ;  // the tile G2P (its maps could not be made otherwise: then the plain build below)
         else
             launch_step_kernel(k_g2p<OneScene, 3>, blocks_for(a.n, 256), 256, st, pdl, sc);
     }
@@ -582,11 +646,16 @@ cudaError_t barrier_selftest(cudaStream_t st, bool stall, unsigned int* bar, uns
 }
 
 cudaError_t prepare_substep_kernels() {
-    return cudaFuncSetAttribute(k_p2g_tile<OneScene>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2gTileBytes);
+    cudaError_t e =
+        cudaFuncSetAttribute(k_p2g_tile<OneScene>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kP2gTileBytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_g2p_tile<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kTileSmemBytes + 128));
+    return e;
 }
 
+
 int substep_kernel_count(const SubstepArgs& a) {
-    return 3 + (a.n > 0 ? 2 : 0) + (a.cd.n_col > 0 ? 2 : 0);
+    return 3 + (a.n > 0 ? 2 + (a.block_sweep ? 1 : 0) : 0) + (a.cd.n_col > 0 ? 2 : 0);
 }
 
 

@@ -322,6 +322,23 @@ MPM_HD void mark_stencil_blocks(const GridDesc& g, const int base[3], unsigned i
                 mark_block(((int64_t)bi * g.nb[1] + bj) * g.nb[2] + bk, flags, list, count);
 }
 
+// Flags the grid blocks a stencil at `base` touches with plain stores (no list; k_list_blocks lists the
+// flagged blocks after P2G). Lanes of the warp that would write the same flags leave it to the lowest of them.
+MPM_HD void flag_stencil_blocks(const GridDesc& g, const int base[3], unsigned int* flags) {
+    const int b0[3] = {base[0] >> 2, base[1] >> 2, base[2] >> 2};
+    const int b1[3] = {(base[0] + 2) >> 2, (base[1] + 2) >> 2, (base[2] + 2) >> 2};
+    const int64_t first = ((int64_t)b0[0] * g.nb[1] + b0[1]) * g.nb[2] + b0[2];
+#ifdef __CUDA_ARCH__
+    const unsigned long long key = (unsigned long long)first * 8u + (b1[0] - b0[0]) * 4u + (b1[1] - b0[1]) * 2u +
+                                   (b1[2] - b0[2]);
+    const unsigned int same = __match_any_sync(__activemask(), key);
+    if ((threadIdx.x & 31u) != (unsigned int)(__ffs(same) - 1)) return;
+#endif
+    for (int bi = b0[0]; bi <= b1[0]; ++bi)
+        for (int bj = b0[1]; bj <= b1[1]; ++bj)
+            for (int bk = b0[2]; bk <= b1[2]; ++bk) flags[((int64_t)bi * g.nb[1] + bj) * g.nb[2] + bk] = 1u;
+}
+
 // P2G of one particle into `sink` (sink.begin(base) once, then sink.add(i, j, k, mv x, y, z, m) per node);
 // false for a particle whose stencil leaves the padded grid (it scatters nothing).
 template <class Sink>
@@ -528,26 +545,41 @@ MPM_HD void plastic_redo_fp64(const Particles& P, int64_t p, const Material& m, 
     t_out[5] = (float)tau[1][2];
 }
 
-// G2P of one particle gathering node velocities from `src` (src(node index) -> float4); the new position goes
-// to nx_out and, when tau_out is given, the stress stored for the next P2G to tau_out as well. kFp64Clamp
-// builds in the FP64 redo at an active Drucker-Prager or snow clamp, taken where fp64_clamp is set.
-template <class Source, bool kFp64Clamp = false>
-MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g,
-                              float dt, const Source& src, unsigned int* fp64, float nx_out[3],
+// The inputs G2P reads (x, F, Jp, mat): from the particle arrays (ParticleIn), or from a copy a kernel has
+// staged in shared memory (the tile G2P's planes). kPrefetch: request F's, Jp's and mat's lines ahead.
+struct ParticleIn {
+    static constexpr bool kPrefetch = true;
+    const Particles& P;
+    int64_t p;
+    MPM_HD float x(int a) const { return P.x[a][p]; }
+    MPM_HD float F(int e) const { return P.F[e][p]; }
+    MPM_HD float Jp() const { return P.Jp[p]; }
+    MPM_HD int mat() const { return P.mat[p]; }
+};
+
+// G2P of one particle gathering node velocities from `src` (src.stencil(base)(i, j, k) -> float4 of stencil
+// node base + (i, j, k)); the new position goes to nx_out and, when tau_out is given, the stress stored for
+// the next P2G to tau_out as well. kFp64Clamp builds in the FP64 redo at an active Drucker-Prager or snow
+// clamp, taken where fp64_clamp is set. Inputs come from `in`, results are stored to particle p of P.
+template <class Source, bool kFp64Clamp = false, class In = ParticleIn>
+MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const In& in, const Material* __restrict__ mats,
+                              const GridDesc& g, float dt, const Source& src, unsigned int* fp64, float nx_out[3],
                               bool fp64_clamp = false, float* tau_out = nullptr) {
     // F, Jp and mat are read after the gather and the C store; their lines are requested now so that the
     // memory latency overlaps the gather
+    if constexpr (In::kPrefetch) {
 #pragma unroll
-    for (int e = 0; e < 9; ++e) prefetch_l1(&P.F[e][p]);
-    prefetch_l1(&P.Jp[p]);
-    prefetch_l1(&P.mat[p]);
+        for (int e = 0; e < 9; ++e) prefetch_l1(&P.F[e][p]);
+        prefetch_l1(&P.Jp[p]);
+        prefetch_l1(&P.mat[p]);
+    }
     float xo[3];
     int base[3];
     float fx[3], w[3][3];
     bool inside = true;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        xo[a] = P.x[a][p];
+        xo[a] = in.x(a);
         float xp = (xo[a] - g.origin[a]) * g.inv_dx;
         inside &= stencil_axis(xp, g.dims[a], &base[a], &fx[a]);
         bspline_weights(fx[a], w[a]);
@@ -557,7 +589,7 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     // i, so each node costs six multiply-adds (w gv and idx_k w gv) instead of twenty-one.
     float nv[3] = {0.f, 0.f, 0.f}, S[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     if (inside) {
-        const StencilIndex at = stencil_index(g, base);
+        const auto at = src.stencil(base);
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
             float Q[3] = {0.f, 0.f, 0.f}, Qj[3] = {0.f, 0.f, 0.f}, Qk[3] = {0.f, 0.f, 0.f};
@@ -566,7 +598,7 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
                 float R[3] = {0.f, 0.f, 0.f}, Rk[3] = {0.f, 0.f, 0.f};
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    const float4 gv = src(at(i, j, k));
+                    const float4 gv = at(i, j, k);
                     const float gva[3] = {gv.x, gv.y, gv.z};
 #pragma unroll
                     for (int a = 0; a < 3; ++a) {
@@ -618,7 +650,8 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     }
 
     float F[3][3], Fn[3][3];
-    load_mat3(P.F, p, F);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) F[e / 3][e % 3] = in.F(e);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -628,10 +661,10 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
     // SVD of the trial F: the plastic models project its singular values (kernels.py:241-262); all models then
     // take the next substep's stress from the same decomposition (F = U diag(sig + delta) V^T), which is what
     // P2G would get from decomposing the stored F again.
-    const Material m = mats[P.mat[p]];
+    const Material m = mats[in.mat()];
     float U[3][3], sig[3], d[3], V[3][3];
     svd3(Fn, U, sig, d, V, fp64);
-    const float jp_old = P.Jp[p];
+    const float jp_old = in.Jp();
     float jp = jp_old;
     bool redo = false;  // FP64 redo at an active Drucker-Prager or snow clamp
     if (m.model != 0) {
@@ -682,7 +715,12 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const Material* __r
 struct GlobalSource {
     const GridDesc* g;
     const float4* grid;
-    MPM_HD float4 operator()(int64_t node) const { return load_node(&grid[node]); }
+    struct Stencil {
+        StencilIndex at;
+        const float4* grid;
+        MPM_HD float4 operator()(int i, int j, int k) const { return load_node(&grid[at(i, j, k)]); }
+    };
+    MPM_HD Stencil stencil(const int base[3]) const { return Stencil{stencil_index(*g, base), grid}; }
 };
 
 // Grid nodes from L2 (inside a kernel that also writes the grid in an earlier phase, where the read-only
@@ -690,13 +728,18 @@ struct GlobalSource {
 struct CoherentSource {
     const GridDesc* g;
     const float4* grid;
-    MPM_HD float4 operator()(int64_t node) const {
+    struct Stencil {
+        StencilIndex at;
+        const float4* grid;
+        MPM_HD float4 operator()(int i, int j, int k) const {
 #ifdef __CUDA_ARCH__
-        return __ldcg(&grid[node]);
+            return __ldcg(&grid[at(i, j, k)]);
 #else
-        return grid[node];
+            return grid[at(i, j, k)];
 #endif
-    }
+        }
+    };
+    MPM_HD Stencil stencil(const int base[3]) const { return Stencil{stencil_index(*g, base), grid}; }
 };
 
 template <bool kFp64Clamp = false, class Source = GlobalSource>
@@ -704,7 +747,7 @@ MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restri
                          const float4* grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false,
                          float* tau_out = nullptr) {
     Source src{&g, grid};
-    g2p_particle_from<Source, kFp64Clamp>(P, p, mats, g, dt, src, fp64, nx_out, fp64_clamp, tau_out);
+    g2p_particle_from<Source, kFp64Clamp>(P, p, ParticleIn{P, p}, mats, g, dt, src, fp64, nx_out, fp64_clamp, tau_out);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

@@ -278,7 +278,12 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
     const int tail = __ffs(ends >> lane) - 1;  // lanes after this one in its segment
     const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned int)tail);
     const bool leader = valid && seg_first;
-    if (leader) mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, parity), &a.wl.counts[parity]);
+    if (leader) {
+        if (a.block_sweep)
+            flag_stencil_blocks(g, t.base, a.wl.block_flag);
+        else
+            mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, parity), &a.wl.counts[parity]);
+    }
     if (a.fixed) {
         p2g_fixed_warp(a, t, valid, leader, tail, span);
         return;
@@ -418,6 +423,18 @@ __global__ void __launch_bounds__(256) k_p2g_tile(Scenes sc) {
             mark_block(node >> 6, a.wl.block_flag, active_blocks(a.wl, cur), &a.wl.counts[cur]);
         }
     }
+}
+
+// The active-block list of this substep from the block flags P2G set with plain stores (one scene, one grid,
+// SubstepArgs::block_sweep): a sweep over every block's flag, one warp-aggregated append per warp.
+template <class Scenes>
+__global__ void __launch_bounds__(256) k_list_blocks(Scenes sc) {
+    pdl_begin();
+    const SubstepArgs a = sc.get(0);
+    const unsigned int cur = a.sp->seq & 1u;
+    const int64_t nblk = (int64_t)a.g.nb[0] * a.g.nb[1] * a.g.nb[2];
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblk; b += (int64_t)gridDim.x * blockDim.x)
+        if (a.wl.block_flag[b]) warp_append(active_blocks(a.wl, cur), &a.wl.counts[cur], (int32_t)b);
 }
 
 // Grid update (normalise, gravity, walls) over the active blocks, four 4x4x4 blocks per 256-thread CTA;

@@ -178,6 +178,8 @@ struct SubstepArgs {
     int fixed_exp;
     int p2g_group;  // P2G sums runs of same-base lanes within aligned groups of this many lanes (1 .. 32)
     int fp64_clamp;  // 1: Drucker-Prager and snow particles at an active clamp are redone in FP64 in G2P
+    unsigned int* err;  // set to nonzero by a kernel whose bounded wait gave up (the host reports it)
+    int block_sweep;    // 1: P2G only flags the blocks it touches; k_list_blocks lists them afterwards
 };
 
 // The field pointers of a particle arena: plane f starts at arena + f * cap (x3 v3 C9 F9 Jp tau6 mat

@@ -3,10 +3,13 @@ the choice per GPU and workload class.
 
 Knobs (C options of include/mpm_gb300.h):
   sort_interval      reorder of the particles by grid node after every N substeps (0: never);
-  g2p_variant        G2P build: 0 capped at 80 registers (3 CTAs of 256 per SM), 1 uncapped;
+  g2p_variant        G2P build: 0 capped at 80 registers (3 CTAs of 256 per SM), 1 uncapped, 2 (a solver) the
+                     persistent tile G2P, its inputs and grid boxes brought into shared memory by TMA;
   list_ctas_per_sm   CTAs per SM of the kernels that walk the active-block and candidate lists;
   p2g_group          P2G sums same-cell lanes within aligned groups of this many lanes (1 .. 32);
   pdl                programmatic dependent launch of the substep kernels (1) or plain stream order (0);
+  block_sweep        (a solver) P2G flags the blocks it touches and a sweep lists them (1), or P2G lists them
+                     with atomics (0);
   fused_p2g          (a solver, outside deterministic mode) two grids, G2P scattering each particle into the
                      next substep's grid (1), or P2G on its own at the start of every substep (0).
 
@@ -44,9 +47,13 @@ MIN_GAIN = 0.02
 # A single solver also chooses between the one- and two-grid substeps, last: the two-grid mode has to beat
 # the tuned one-grid choice. (Searched first, on the 256^3 pour it beat the untuned defaults, the descent
 # then never reached the reorder that makes one grid faster, and a frame took 1.3x as long: measured.)
-SOLVER_DEFAULTS = {**DEFAULTS, "fused_p2g": 0}
-SOLVER_CANDIDATES = {**CANDIDATES, "fused_p2g": (0, 1)}
-SOLVER_ORDER = KNOB_ORDER + ("fused_p2g",)
+SOLVER_DEFAULTS = {**DEFAULTS, "block_sweep": 0, "fused_p2g": 0}
+SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2), "block_sweep": (0, 1), "fused_p2g": (0, 1)}
+SOLVER_ORDER = KNOB_ORDER + ("block_sweep", "fused_p2g")
+# The tile G2P (g2p_variant 2) stages a chunk's grid boxes in shared memory, which pays when the particles are
+# in grid-block order, i.e. with a periodic reorder: the two knobs are also tried together, from the best
+# configuration of the descent (one knob at a time would try the tile G2P only at the sort interval then set).
+SOLVER_JOINT = tuple({"g2p_variant": 2, "sort_interval": k, "fused_p2g": 0} for k in (1, 2, 4, 8, 16))
 
 
 def cache_path() -> Path:
@@ -94,11 +101,13 @@ def apply(target, cfg: dict, sms: int, solver: bool = False) -> None:
     target.set_option(_abi.OPT_PDL, int(cfg.get("pdl", 1)))
     target.set_option(_abi.OPT_P2G_TILE, int(cfg.get("p2g_tile", 0)))
     if solver:
+        target.set_option(_abi.OPT_BLOCK_SWEEP, int(cfg.get("block_sweep", 0)))
         target.set_option(_abi.OPT_FUSED_P2G, int(cfg.get("fused_p2g", 0)))
 
 
-def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, min_gain=MIN_GAIN):
-    """Coordinate descent: measure(cfg) -> seconds (lower is better). Returns (best cfg, its time, trials)."""
+def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, min_gain=MIN_GAIN, joint=()):
+    """Coordinate descent: measure(cfg) -> seconds (lower is better), then each of the `joint` overrides (several
+    knobs at once) applied to the best so far. Returns (best cfg, its time, trials)."""
     best = dict(defaults)
     best_t = measure(best)
     trials = [(dict(best), best_t)]
@@ -114,6 +123,17 @@ def search(measure, candidates=CANDIDATES, defaults=DEFAULTS, order=KNOB_ORDER, 
             trials.append((cfg, t))
             if t < best_t * (1.0 - min_gain):
                 best, best_t = cfg, t
+    base = dict(best)
+    for over in joint:
+        cfg = {**base, **over}
+        key = tuple(sorted(cfg.items()))
+        if key in seen:
+            continue
+        seen.add(key)
+        t = measure(cfg)
+        trials.append((cfg, t))
+        if t < best_t * (1.0 - min_gain):
+            best, best_t = cfg, t
     return best, best_t, trials
 
 
@@ -169,9 +189,12 @@ def tune_solver(solver, dt: float, frame_dt: float = 1 / 24, substeps: int = 20,
     else:
         measure = lambda cfg: _time_solver(solver, cfg, sms, dt, frame_dt, substeps)  # noqa: E731
     if deterministic:  # one grid whatever fused_p2g says: that knob is not searched (nor set) there
-        best, best_t, trials = search(measure)
+        best, best_t, trials = search(measure, {k: v for k, v in SOLVER_CANDIDATES.items() if k != "fused_p2g"},
+                                      {k: v for k, v in SOLVER_DEFAULTS.items() if k != "fused_p2g"},
+                                      tuple(k for k in SOLVER_ORDER if k != "fused_p2g"),
+                                      joint=tuple({k: v for k, v in o.items() if k != "fused_p2g"} for o in SOLVER_JOINT))
     else:
-        best, best_t, trials = search(measure, SOLVER_CANDIDATES, SOLVER_DEFAULTS, SOLVER_ORDER)
+        best, best_t, trials = search(measure, SOLVER_CANDIDATES, SOLVER_DEFAULTS, SOLVER_ORDER, joint=SOLVER_JOINT)
     solver.load_state(snapshot)
     apply(solver, best, sms, solver=True)
     cache.setdefault(gkey, {})[wkey] = best

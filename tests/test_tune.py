@@ -99,5 +99,21 @@ def test_run_substeps_tuning_restores_the_state_per_trial_and_keeps_its_own_key(
 
 
 def test_the_two_grid_knob_is_searched_last_for_a_solver():
-    assert tune.SOLVER_ORDER[-1] == "fused_p2g" and tune.SOLVER_ORDER[:-1] == tune.KNOB_ORDER
+    """fused_p2g is the last knob of the descent (it must beat the tuned one-grid choice); the solver-only
+    knobs come after the batch knobs; the joint tile-G2P-with-reorder trials keep one grid."""
+    assert tune.SOLVER_ORDER[-1] == "fused_p2g" and tune.SOLVER_ORDER[:len(tune.KNOB_ORDER)] == tune.KNOB_ORDER
     assert tune.SOLVER_DEFAULTS["fused_p2g"] == 0 and "fused_p2g" not in tune.DEFAULTS
+    assert tune.SOLVER_DEFAULTS["block_sweep"] == 0 and "block_sweep" not in tune.DEFAULTS
+    assert all(o["g2p_variant"] == 2 and o["sort_interval"] > 0 and o["fused_p2g"] == 0 for o in tune.SOLVER_JOINT)
+
+
+def test_joint_overrides_are_tried_from_the_best_of_the_descent():
+    times = {(0, 0): 1.0, (1, 0): 0.9, (2, 0): 1.2, (0, 4): 1.1, (1, 4): 0.95, (2, 4): 0.5}
+
+    def measure(cfg):
+        return times.get((cfg["a"], cfg["b"]), 2.0)
+
+    best, t, trials = tune.search(measure, {"a": (0, 1, 2), "b": (0, 4)}, {"a": 0, "b": 0}, ("a", "b"),
+                                  joint=({"a": 2, "b": 4},))
+    assert best == {"a": 2, "b": 4} and t == 0.5  # one knob at a time stops at (1, 0)
+    assert len(trials) == 5
