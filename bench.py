@@ -36,7 +36,6 @@ import numpy as np
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
-sys.path.insert(0, str(ROOT / "tests"))
 
 METRIC = "particle-substeps/s on 1 GB300, batched vs plain; p50/p99 frame latency"
 UNIT = "particle-substeps/s"
@@ -128,21 +127,33 @@ class Clocks:
                 "samples": len(sm)}
 
 
-def build_scene(seed: int = 0):
-    from scenes import mix_scene
+def _index(device: str) -> int:
+    return int(device.split(":")[1]) if ":" in device else 0
 
-    return mix_scene(res=128, seed=seed)
+
+def build_scene(device: str = "cuda:0", sample=None):
+    """The headline workload (mpm_plugin_gb300.workloads.mixed_scene), its mesh volumes sampled on `device`, or
+    by `sample` (the CPU arms pass the oracle's sampler: the same points, no GPU kernel)."""
+    from mpm_plugin_gb300.workloads import mixed_scene
+
+    return mixed_scene(res=128, seed=0, device=_index(device), sample=sample)
+
+
+def _cpu_sampler():
+    from oracle import geometry
+
+    return geometry.sample_mesh_volume
 
 
 def make_gpu_solver(device: str):
     from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
-    from scenes import add
+    from mpm_plugin_gb300.workloads import add_group
 
-    d, mats, groups, (cv, ct, xf) = build_scene()
+    d, mats, groups, (cv, ct, xf) = build_scene(device)
     s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
     for pos, m, vel in groups:
-        add(s, pos, m, m, vel)
+        add_group(s, pos, m, m, vel)
     s.set_colliders([ColliderGeometry(MeshData(cv, ct), True, 0.5)])
     s.set_collider_transforms(xf[None], xf[None])
     return s, xf
@@ -162,13 +173,13 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
     from mpm_plugin_gb300.batch import Gb300Batch
     from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
-    from scenes import add, batched_scenes
+    from mpm_plugin_gb300.workloads import add_group, batched_scenes
 
     specs = batched_scenes(seed=0, n_hi=n_hi)
     solvers = []
     for d, mats, pos, vel, cols in specs:
         s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
-        add(s, pos, 0, 0, vel)
+        add_group(s, pos, 0, 0, vel)
         if cols:
             s.set_colliders([ColliderGeometry(MeshData(cv, ct), True, fr) for cv, ct, _, fr in cols])
             xf = np.stack([c[2] for c in cols])
@@ -233,7 +244,7 @@ class _FrameSink:
 def serve_trace(seconds: float, rate: float, seed: int = 0):
     """Poisson arrivals (mean `rate` per second) over `seconds`; each request one seeded pour job."""
     from mpm_plugin_gb300.serve import BakeJob
-    from scenes import pour_job_spec
+    from mpm_plugin_gb300.workloads import pour_job as pour_job_spec
 
     rng = np.random.default_rng(seed)
     t, trace, i = 0.0, [], 0
@@ -300,62 +311,35 @@ def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float
 
 
 def large_scene(res: int, pile_top: float, seed: int = 3):
-    """The large inflow workload at resolution `res`: a Drucker-Prager pile (E 3.5e5, nu 0.3, 30 deg,
-    rho 1600) filling (0.2-0.8)^2 x (0-pile_top) at 8 per cell, a seeded perturbed torus of 20,480 triangles
-    (R 0.2, r 0.05, friction 0.4) turning at 1 rev/s about z, and a disc inflow r = 0.05 m at 2 m/s downward
-    (a closed 48-sided cylinder emitter, one emission substep's slab high).
-    Returns (domain, materials, pile, torus mesh, pose(t), emit(solver, piece))."""
-    from mpm_plugin_gb300.interface import MaterialParams
-    from scenes import cylinder, domain, lattice_box, rot_x, rot_z, torus, translate
+    from mpm_plugin_gb300.workloads import large_scene as make
 
-    d = domain(res=res)
-    mats = [MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)]
-    pile = lattice_box((0.2, 0.2, 0.0), (0.8, 0.8, pile_top), d.dx / 2, np.random.default_rng(seed))
-    tv, tt = torus(0.2, 0.05, 256, 40, seed=seed, jitter=0.05)
-
-    def pose(t):
-        return translate(0.5, 0.5, pile_top + 0.12) @ rot_z(360.0 * t) @ rot_x(90.0)
-
-    ev, et = cylinder(0.05, 2.0 / 96, 48)  # one emission substep's slab of the disc inflow
-    ev = ev + np.float32([0.5, 0.5, 0.9])
-
-    def emit(s, piece):
-        """One emission substep as the bake runner's _emit does it for an inflow (bake.py:56-86): the
-        emitter volume sampled at spacing dx / 2 with the runner's seed list (here: seed, frame, emitter 0,
-        the substep fraction), points outside the domain dropped, points on occupied nodes dropped, the rest
-        added at 2 m/s downward. The sampling runs on the GPU (mpm_plugin_gb300.emit)."""
-        from mpm_plugin_gb300.emit import sample_mesh_volume
-
-        frame, quarter = divmod(piece, 4)
-        pts = sample_mesh_volume(ev, et, d.dx / 2, [seed, frame + 1, 0, quarter + 1, 4])
-        pts = pts[((pts >= np.asarray(d.min)) & (pts <= np.asarray(d.max))).all(1)]
-        if len(pts) and s.particle_count:
-            pts = pts[~s.is_occupied(pts)]
-        if len(pts):
-            s.add_particles(pts, np.tile(np.float32([0.0, 0.0, -2.0]), (len(pts), 1)), np.zeros(len(pts), np.int32),
-                            np.zeros(len(pts), np.int32))
-        return len(pts)
-
-    return d, mats, pile, (tv, tt), pose, emit
+    return make(res, pile_top, seed)
 
 
-def run_large(device: str, frames: int) -> dict:
+def run_large(device: str, frames: int, fp64_mode: int = 0, tuned_cfg: dict | None = None) -> dict:
     """The 256^3 inflow workload (about 7.5M particles at the start), driven as the bake runner drives it:
     per 24 fps frame, four pieces of 1/96 s, each with the collider's start and end pose, an advance at the
     CFL step and an emission (occupancy query + add_particles); then the frame's particles are read back.
-    One untimed frame first. FP64 conservation totals are read at the start and the end."""
+    One untimed frame first. FP64 conservation totals are read at the start and the end. fp64_mode: the
+    Drucker-Prager return mapping redone in FP64 for marginal decisions (1) or not (0)."""
     import torch
 
-    from mpm_plugin_gb300 import tune
+    from mpm_plugin_gb300 import _abi, tune
     from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
 
+    dev = _index(device)
     d, mats, pile, (tv, tt), pose, emit = large_scene(256, 0.155)
     s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
     s.add_particles(pile, np.zeros_like(pile), np.zeros(len(pile), np.int32), np.zeros(len(pile), np.int32))
     s.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
     s.set_collider_transforms(pose(0.0)[None], pose(0.0)[None])
-    tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=12)
+    if tuned_cfg is None:
+        tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=12)
+    else:  # the FP64 run keeps the FP32 run's launch choices
+        tune.apply(s, tuned_cfg, tune.gpu_key(device)[1], solver=True)
+        tuned = {**tuned_cfg, "cached": True}
+    s.set_option(_abi.OPT_FP64_CLAMP, fp64_mode)
     n0 = s.particle_count
     c0 = s.conservation()
     t_adv = t_emit = t_read = 0.0
@@ -371,7 +355,7 @@ def run_large(device: str, frames: int) -> dict:
             t0 = time.perf_counter()
             st = s.advance(1 / 96)
             t1 = time.perf_counter()
-            added = emit(s, k)
+            added = emit(s, k, dev)
             t2 = time.perf_counter()
             if f > 0:
                 ps += n * st.substeps
@@ -389,77 +373,93 @@ def run_large(device: str, frames: int) -> dict:
             frame_ms.append(1e3 * (t4 - f0))
     c1 = s.conservation()
     n1 = s.particle_count
+    redo = s.fp64_redo_lanes()
     # kernel-group times of a few substeps at the end state (event nodes in the substep graph)
-    from mpm_plugin_gb300 import _abi
-
     s.set_option(_abi.OPT_KERNEL_TIMING, 1)
     s.kernel_times(reset=True)
     for _ in range(4):
         s.substep(8e-5, 1.0, 1 / 96)
     kt = s.kernel_times(reset=True)
     s.set_option(_abi.OPT_KERNEL_TIMING, 0)
+    final = s.save_state() if fp64_mode == 0 else None
+    pose_end = pose((4 * frames + 4) / 96)
     s.close()
     total = t_adv + t_emit + t_read
-    return {"value": ps / total, "advance_only": ps / t_adv, "unit": UNIT, "frames": frames,
-            "particles_start": n0, "particles_end": n1, "emitted": emitted, "substeps": substeps,
-            "seconds": {"advance": t_adv, "emission": t_emit, "read_back": t_read},
-            "frame_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
-            "tuned": tuned,
-            "kernels_ms_per_substep": {k: t / max(c, 1) for k, (t, c) in kt.items()},
-            "conservation_fp64": {"mass": [c0["mass"], c1["mass"]], "ke": [c0["ke"], c1["ke"]],
-                                  "momentum_z": [float(c0["momentum"][2]), float(c1["momentum"][2])]},
-            "fp64_oracle_error": fp64_error_sample(device)}
+    out = {"value": ps / total, "advance_only": ps / t_adv, "unit": UNIT, "frames": frames,
+           "fp64_return_mapping": {0: "off (FP32; FP64 only for SVDs that did not converge)",
+                                   1: "marginal decisions redone in FP64"}[fp64_mode],
+           "fp64_redo_lanes": redo, "fp64_redo_share": redo / max(ps, 1.0),
+           "particles_start": n0, "particles_end": n1, "emitted": emitted, "substeps": substeps,
+           "seconds": {"advance": t_adv, "emission": t_emit, "read_back": t_read},
+           "frame_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
+           "tuned": tuned,
+           "kernels_ms_per_substep": {k: t / max(c, 1) for k, (t, c) in kt.items()},
+           "conservation_fp64": {"mass": [c0["mass"], c1["mass"]], "ke": [c0["ke"], c1["ke"]],
+                                 "momentum_z": [float(c0["momentum"][2]), float(c1["momentum"][2])]}}
+    return out, final, (tv, tt), pose_end
 
 
-def fp64_error_sample(device: str, substeps: int = 100) -> dict:
-    """The large workload's physics at 48^3 (pile, turning torus; about 22k particles), 100 substeps at
-    dt = 2e-4 on the GPU (FP32) and on the FP64 oracle: relative error of x, v and of the invariants, for the
-    default build and with the Drucker-Prager clamp redone in FP64 (MPM_OPT_FP64_CLAMP)."""
+def fp64_subbox_error(device: str, state: dict, torus_mesh, pose, seed: int = 7, checks=(100, 200, 300),
+                      dt: float = 5e-5) -> dict:
+    """Error against the FP64 oracle on a seeded sub-box of the pour: the particles of the large workload's
+    final state inside an 8 cm cube at a seeded place on the pile floor, in a 25 cm domain around it at the
+    same dx (walls at its sides and floor), with the torus at its final pose. The same substeps on the GPU
+    (FP32 bulk, marginal return-mapping decisions in FP64) and on the FP64 oracle (the checker); relative
+    errors of x, v, F and of the invariants after every 100 substeps, and with the FP64 redo off at the end."""
     from mpm_plugin_gb300 import _abi
-    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+    from mpm_plugin_gb300.interface import ColliderGeometry, MaterialParams, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
+    from mpm_plugin_gb300.workloads import make_domain
     from oracle.oracle import OracleSolver
 
-    d, mats, pile, (tv, tt), pose, _ = large_scene(48, 0.1)
+    rng = np.random.default_rng(seed)
+    cx, cy = (float(c) for c in rng.uniform(0.3, 0.7, 2))
+    x = state["x"]
+    sel = (np.abs(x[:, 0] - cx) <= 0.04) & (np.abs(x[:, 1] - cy) <= 0.04) & (x[:, 2] <= 0.08)
+    sub = {k: np.ascontiguousarray(v[sel]) for k, v in state.items()}
+    d = make_domain(64, (cx - 0.125, cy - 0.125, 0.0), (cx + 0.125, cy + 0.125, 0.25))
+    mats = [MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)]
+    tv, tt = torus_mesh
+    xf = pose.astype(np.float32)[None]
     gs = [Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device) for _ in range(2)]
-    gs[1].set_option(_abi.OPT_FP64_CLAMP, 1)
+    gs[0].set_option(_abi.OPT_FP64_CLAMP, 1)
     o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f64", threads=os.cpu_count() or 1)
-    z = np.zeros(len(pile), np.int32)
-    xf0, xf1 = pose(0.0), pose(1 / 24)
     for g in gs:
-        g.add_particles(pile, np.zeros_like(pile), z, z)
+        g.load_state(sub)
         g.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
-        g.set_collider_transforms(xf0[None], xf1[None])
-    o.add_particles(pile, np.zeros_like(pile), z, z)
+        g.set_collider_transforms(xf, xf)
+    o.load_state(sub)
     o.set_colliders([(tv, tt, True, 0.4)])
-    o.set_collider_transforms(xf0[None], xf1[None])
-    o.frame_dt = 1 / 24
+    o.set_collider_transforms(xf, xf)
+    steps = max(checks)
+    o.frame_dt = steps * dt
+    pm = float(np.float32(1600.0) * np.float32((0.25 / 64) ** 3 / 8))
+    rel = lambda u, w: float(np.linalg.norm(u - w) / max(np.linalg.norm(w), 1e-30))  # noqa: E731
+
+    def errors(a, b):
+        va, vb = a["v"].astype(np.float64), b["v"].astype(np.float64)
+        return {"x": rel(a["x"], b["x"]), "v": rel(a["v"], b["v"]), "F": rel(a["F"], b["F"]),
+                "momentum": rel((pm * va).sum(0), (pm * vb).sum(0)),
+                "com": rel(a["x"].astype(np.float64).mean(0), b["x"].astype(np.float64).mean(0)),
+                "ke": abs((va * va).sum() - (vb * vb).sum()) / max((vb * vb).sum(), 1e-30)}
+
     t0 = time.perf_counter()
-    for k in range(substeps):
-        sk = (k + 1) / substeps
+    per = {}
+    for k in range(steps):
+        sk = (k + 1) / steps
         for g in gs:
-            g.substep(2e-4, sk, 1 / 24)
-        o.substep(2e-4, sk)
-    b = o.save_state()
-    states = [g.save_state() for g in gs]
+            g.substep(dt, sk, steps * dt)
+        o.substep(dt, sk)
+        if k + 1 in checks:
+            per[k + 1] = errors(gs[0].save_state(), o.save_state())
+    off = errors(gs[1].save_state(), o.save_state())
+    redo = gs[0].fp64_redo_lanes()
     for g in gs:
         g.close()
-    pm = float(np.float32(1600.0) * np.float32(d.dx ** 3 / 8))
-
-    def inv(st):
-        x, v = st["x"].astype(np.float64), st["v"].astype(np.float64)
-        return (pm * v).sum(0), (x.mean(0)), 0.5 * pm * (v * v).sum()
-
-    rel = lambda u, w: float(np.linalg.norm(u - w) / max(np.linalg.norm(w), 1e-30))
-    pb, cb, kb = inv(b)
-
-    def errors(a):
-        pa, ca, ka = inv(a)
-        return {"x": rel(a["x"], b["x"]), "v": rel(a["v"], b["v"]), "F": rel(a["F"], b["F"]),
-                "momentum": rel(pa, pb), "com": rel(ca, cb), "ke": abs(ka - kb) / kb}
-
-    return {"particles": len(pile), "substeps": substeps, "dt": 2e-4, **errors(states[0]),
-            "fp64_clamp": errors(states[1]), "oracle_seconds": time.perf_counter() - t0}
+    return {"particles": int(sel.sum()), "sub_box": [[cx - 0.04, cy - 0.04, 0.0], [cx + 0.04, cy + 0.04, 0.08]],
+            "dt": dt, "errors_every_100_substeps": per, f"errors_at_{steps}_fp64_off": off,
+            "fp64_redo_lanes": redo, "oracle_seconds": time.perf_counter() - t0,
+            "reference": "FP64 oracle (C restatement of the reference kernels, REAL = double)"}
 
 
 def run_surface(device: str, repeats: int = 3) -> dict:
@@ -474,9 +474,12 @@ def run_surface(device: str, repeats: int = 3) -> dict:
     from mpm_plugin_gb300.surface import SurfaceSettings, surface_particles
     from oracle import surface as S
 
+    from mpm_plugin_gb300.workloads import cell_size
+
     d, _, pile, _, _, _ = large_scene(256, 0.155)
     rng = np.random.default_rng(5)
-    sets = {"pour_pile_256": (pile.astype(np.float32), rng.normal(0, 0.1, pile.shape).astype(np.float32), d.dx / 2),
+    sets = {"pour_pile_256": (pile.astype(np.float32), rng.normal(0, 0.1, pile.shape).astype(np.float32),
+                              cell_size(d) / 2),
             "blob_1m": ((rng.normal(0, 0.05, (1_000_000, 3)) + 0.5).astype(np.float32),
                         rng.normal(0, 1.0, (1_000_000, 3)).astype(np.float32), 0.004)}
     out = {}
@@ -515,14 +518,11 @@ def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict
     `cpu_substeps` substeps of the same scene on all host cores."""
     import torch
 
-    from mpm_plugin_gb300.interface import MaterialParams
     from mpm_plugin_gb300.solver import Gb300Solver
+    from mpm_plugin_gb300.workloads import jelly_cube
     from oracle.oracle import OracleSolver
-    from scenes import domain, lattice_box
 
-    d = domain(res=64)
-    mats = [MaterialParams("jelly_cube", "elastic", 1e5, 0.3, 1000.0)]
-    pos = lattice_box((0.375, 0.475, 0.375), (0.625, 0.725, 0.625), d.dx / 2, np.random.default_rng(0))
+    d, mats, pos = jelly_cube(64)
     z = np.zeros(len(pos), np.int32)
     from mpm_plugin_gb300 import tune
 
@@ -558,13 +558,13 @@ def run_small(device: str, substeps: int = 1000, cpu_substeps: int = 50) -> dict
 
 def cpu_oracle_time(threads: int, budget_s: float):
     """FP32 oracle (C restatement of the reference kernels, OpenMP) on the same scene; returns rate, sample."""
+    from mpm_plugin_gb300.workloads import add_group
     from oracle.oracle import OracleSolver
-    from scenes import add
 
-    d, mats, groups, (cv, ct, xf) = build_scene()
+    d, mats, groups, (cv, ct, xf) = build_scene(sample=_cpu_sampler())
     o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f32", threads=threads)
     for pos, m, vel in groups:
-        add(o, pos, m, m, vel)
+        add_group(o, pos, m, m, vel)
     o.set_colliders([(cv, ct, True, 0.5)])
     o.set_collider_transforms(xf[None], xf[None])
     n = o.particle_count
@@ -584,13 +584,13 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    from mpm_plugin_gb300.workloads import add_group
     from oracle.oracle import OracleSolver
-    from scenes import add
 
-    d, mats, groups, (cv, ct, xf) = build_scene()
+    d, mats, groups, (cv, ct, xf) = build_scene(sample=_cpu_sampler())
     o = OracleSolver(d, mats, (0.0, 0.0, -9.81), 8, precision="f32", threads=threads)
     for pos, m, vel in groups:
-        add(o, pos, m, m, vel)
+        add_group(o, pos, m, m, vel)
     o.set_colliders([(cv, ct, True, 0.5)])
     o.set_collider_transforms(xf[None], xf[None])
     n = o.particle_count
@@ -728,13 +728,19 @@ def run_gpu(args, world, rank, local):
     peak, peak_kind = peaks()
     bytes_per_launch = names.get(dom, 16) * n
     achieved = bytes_per_launch / (avg_ms[dom] / 1e3) / 1e9
-    traffic = None
+    traffic, warp_inst = None, None
     tfile = ROOT / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get(dom)
+            tdoc = json.loads(tfile.read_text())
+            traffic, warp_inst = tdoc.get(dom), tdoc.get(f"{dom}_warp_instructions")
         except Exception:
-            traffic = None
+            traffic = warp_inst = None
+    clocks = clk.summary()
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    # issue use: the kernel's warp instructions (ncu, committed) over what 4 schedulers per SM issue in its time
+    issue_frac = warp_inst / (sms * 4 * mhz * 1e6 * avg_ms[dom] / 1e3) if warp_inst else None
     cpu_rate, cpu_n, cpu_k, cpu_el = cpu_oracle_time(os.cpu_count() or 1, args.cpu_budget)
     batched = None
     if args.batched_frames > 0:
@@ -742,7 +748,13 @@ def run_gpu(args, world, rank, local):
         batched = run_batched(device, args.batched_frames)
         batched["small_scenes"] = run_batched(device, args.batched_frames, n_hi=1e5)
     serving = run_serving(device, args.serve_seconds) if args.serve_seconds > 0 else None
-    large = run_large(device, args.large_frames) if args.large_frames > 0 else None
+    large = None
+    if args.large_frames > 0:
+        large, final, tmesh, pose_end = run_large(device, args.large_frames)
+        on = run_large(device, args.large_frames, fp64_mode=1, tuned_cfg=large["tuned"])[0]
+        large["fp64_on"] = {k: on[k] for k in ("value", "advance_only", "fp64_return_mapping", "fp64_redo_lanes",
+                                                "fp64_redo_share", "substeps", "kernels_ms_per_substep")}
+        large["fp64_oracle_error"] = fp64_subbox_error(device, final, tmesh, pose_end)
     small = run_small(device) if args.small else None
     surface = run_surface(device) if args.surface and rank == 0 else None
     line = {
@@ -755,7 +767,10 @@ def run_gpu(args, world, rank, local):
                              "over the timed substeps; the L2 writes between them are outside"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": bytes_per_launch},
+                     "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "issue_frac": issue_frac, "warp_instructions_per_launch": warp_inst,
+                     "note": "HBM fraction of the algorithmic bytes; the kernel is bound by instruction issue and "
+                             "latency (issue_frac: warp instructions / (SMs x 4 x SM clock x kernel time))"},
         "kernels_ms_per_launch": avg_ms,
         "substep_bytes": {"algorithmic_per_particle": SUBSTEP_BYTES,
                           "achieved_gbs": SUBSTEP_BYTES * n * args.steps / (total_ms / 1e3) / 1e9},
@@ -768,7 +783,7 @@ def run_gpu(args, world, rank, local):
                 "substeps_per_frame": substeps / e2e_frames},
         "frame_latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99))},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "fp64_svd_lanes": fp64_lanes,
         "tuned": tuned,
         "deterministic": {"value": n * args.steps / (det_ms / 1e3), "unit": UNIT,
@@ -783,6 +798,39 @@ def run_gpu(args, world, rank, local):
     print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_profile_case(args) -> None:
+    """A fixed case for profilers (no timing, no output but one line): `--profile-case mix128` (the headline
+    scene) or `pour256` (the large workload's 7.45M-particle pile and torus, no inflow), with the given launch
+    choices, `--profile-substeps` explicit substeps without graphs, so each kernel is its own launch and a
+    profiler can select launches by kernel name and count."""
+    from mpm_plugin_gb300 import _abi
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+    from mpm_plugin_gb300.solver import Gb300Solver
+
+    device = "cuda:0"
+    if args.profile_case == "mix128":
+        s, _ = make_gpu_solver(device)
+        dt = DT
+    else:
+        d, mats, pile, (tv, tt), pose, _ = large_scene(256, 0.155)
+        s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
+        z = np.zeros(len(pile), np.int32)
+        s.add_particles(pile, np.zeros_like(pile), z, z)
+        s.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
+        s.set_collider_transforms(pose(0.0)[None], pose(1 / 96)[None])
+        dt = 8e-5
+    s.set_option(_abi.OPT_USE_GRAPH, 0)
+    s.set_option(_abi.OPT_G2P_VARIANT, args.g2p_variant)
+    s.set_option(_abi.OPT_SORT_INTERVAL, args.sort_interval)
+    s.set_option(_abi.OPT_BLOCK_SWEEP, args.block_sweep)
+    s.set_option(_abi.OPT_FP64_CLAMP, args.fp64_clamp)
+    for k in range(args.profile_substeps):
+        s.substep(dt, (k + 1) / args.profile_substeps, 1 / 96)
+    s.synchronize()
+    print(f"profile case {args.profile_case}: {s.particle_count} particles, {args.profile_substeps} substeps")
+    s.close()
 
 
 def main():
@@ -801,7 +849,17 @@ def main():
     ap.add_argument("--batched-frames", type=int, default=3,
                     help="frames of the 64-scene batched workload, plain and batched (0: skip)")
     ap.add_argument("--surface", type=int, default=1, help="measure the surfacer (0: skip)")
+    ap.add_argument("--profile-case", choices=["mix128", "pour256"], default=None,
+                    help="run a fixed case for a profiler instead of the benchmark (see run_profile_case)")
+    ap.add_argument("--profile-substeps", type=int, default=30)
+    ap.add_argument("--g2p-variant", type=int, default=0)
+    ap.add_argument("--sort-interval", type=int, default=0)
+    ap.add_argument("--block-sweep", type=int, default=0)
+    ap.add_argument("--fp64-clamp", type=int, default=0)
     args = ap.parse_args()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     args.warmup = max(args.warmup, 3)
     world, rank, local = dist_env()
     if args.impl == "reference":

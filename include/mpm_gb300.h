@@ -131,9 +131,11 @@ enum {
                                   reduction each: 1, 2, 4, 8, 16 or 32 (default) */
     MPM_OPT_PDL = 8,           /* 1 (default): the substep kernels use programmatic dependent launch, so each
                                   kernel's launch overlaps the tail of the one before; 0: plain stream order */
-    MPM_OPT_FP64_CLAMP = 9,    /* 1: a Drucker-Prager or snow particle whose return mapping clamps is redone in
-                                  FP64 (SVD, projection, hardening, stress); 0 (default): FP32, with the FP64
-                                  redo only for SVDs that did not converge */
+    MPM_OPT_FP64_CLAMP = 9,    /* FP64 in the Drucker-Prager and snow return mapping: 1 a particle whose FP32
+                                  decision is marginal (the cone or separation test, a snow bound within a
+                                  relative 2e-5, or nearly equal log singular values) is redone in FP64 (SVD,
+                                  projection, hardening, stress); 2 every particle whose clamp is active is;
+                                  0 (default): FP32, with the FP64 redo only for SVDs that did not converge */
     MPM_OPT_P2G_TILE = 10,     /* 1: P2G sums each CTA's contributions in shared-memory tiles of the nodes its
                                   particles touch, then adds them to the grid; 0 (default): warp segments
                                   (shuffle sums of same-cell lanes) only. Deterministic mode uses segments */
@@ -206,6 +208,9 @@ int mpm_device_bytes(void *handle, int64_t *bytes);
 
 /* Number of SVD lanes that took the FP64 path since the handle was created. */
 int mpm_fp64_lanes(void *handle, int64_t *lanes);
+/* Number of Drucker-Prager / snow lanes whose return mapping G2P redid in FP64 under MPM_OPT_FP64_CLAMP since the
+ * handle was created (no counterpart in the reference; it reports how far FP64 is confined). */
+int mpm_fp64_redo_lanes(void *handle, int64_t *lanes);
 
 /* Occupancy query that allocates no device memory. It has no counterpart in the reference: it is for callers
  * that cannot allocate device memory when they ask, such as a serving process whose device memory budget

@@ -24,7 +24,7 @@ EXPORTS = ("mpm_create", "mpm_destroy", "mpm_last_error", "mpm_add_particles", "
            "mpm_set_collider_transforms", "mpm_advance", "mpm_substep", "mpm_run_substeps", "mpm_particle_count", "mpm_get_particles",
            "mpm_is_occupied", "mpm_save_state", "mpm_load_state", "mpm_set_option", "mpm_get_stream",
            "mpm_synchronize", "mpm_kernel_times", "mpm_grid_dims", "mpm_read_grid", "mpm_read_collider_pose",
-           "mpm_launch_count", "mpm_fp64_lanes", "mpm_is_occupied_noalloc", "mpm_volume_lattice", "mpm_read_begin", "mpm_read_wait", "mpm_host_alloc", "mpm_coop_barrier_selftest",
+           "mpm_launch_count", "mpm_fp64_lanes", "mpm_fp64_redo_lanes", "mpm_is_occupied_noalloc", "mpm_volume_lattice", "mpm_read_begin", "mpm_read_wait", "mpm_host_alloc", "mpm_coop_barrier_selftest",
            "mpm_host_free", "mpm_conservation", "mpm_device_bytes", "mpm_batch_create", "mpm_batch_destroy",
            "mpm_batch_last_error", "mpm_batch_add", "mpm_batch_remove", "mpm_batch_size", "mpm_batch_advance",
            "mpm_batch_set_option", "mpm_batch_get_stream", "mpm_batch_launch_count", "mpm_surface_create",
@@ -90,6 +90,7 @@ def lib() -> C.CDLL:
         "mpm_read_collider_pose": [P, I32, P, P, P],
         "mpm_launch_count": [P, C.POINTER(I64)],
         "mpm_fp64_lanes": [P, C.POINTER(I64)],
+        "mpm_fp64_redo_lanes": [P, C.POINTER(I64)],
         "mpm_is_occupied_noalloc": [C.POINTER(MpmDomainDesc), I32, I64, P, I64, P, P, I32, P],
         "mpm_volume_lattice": [P, I64, P, I32, P, I32, P, I32, D, P, I64, I64, I32, P, I64, C.POINTER(I64)],
         "mpm_read_begin": [P, P, P, P, P, P, P, P],

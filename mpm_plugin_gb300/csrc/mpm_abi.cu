@@ -151,7 +151,7 @@ struct Handle {
     int64_t since_sort = 0;
 
     LaunchShape shape;                      // autotuned launch choices
-    bool fp64_clamp = false;                // Drucker-Prager / snow return mapping in FP64 at an active clamp
+    int fp64_clamp = 0;                     // Drucker-Prager / snow return mapping redone in FP64 (0, 1, 2)
     bool deterministic = false;
     unsigned long long* d_fixed = nullptr;  // deterministic mode: fixed-point node sums (4 per node)
     unsigned int* d_poison = nullptr;       // deterministic mode: non-finite marks (1 per node)
@@ -422,7 +422,8 @@ SubstepArgs substep_args(Handle* h) {
     a.poison = h->deterministic ? h->d_poison : nullptr;
     a.fixed_exp = h->fixed_exp;
     a.p2g_group = h->shape.p2g_group;
-    a.fp64_clamp = h->fp64_clamp ? 1 : 0;
+    a.fp64_clamp = h->fp64_clamp;
+    a.fp64_redo = h->d_counters + 2 + kMaxMaterials;
     a.err = h->d_coop + 3;
     a.block_sweep = h->shape.block_sweep && !two_grids(h) && !h->shape.p2g_tile ? 1 : 0;
     return a;
@@ -1110,8 +1111,8 @@ Status create(const MpmDomainDesc* dom, const MpmMaterialDesc* mats, int32_t n_m
         h->ss_scan_cap = scan_tile_count(h->grid_nodes + 1) + 1;
         CK(cudaMalloc(&h->ss_scan, sizeof(int32_t) * (size_t)(h->ss_scan_cap + 2)));
     }
-    CK(cudaMalloc(&h->d_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
-    CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * (2 + kMaxMaterials)));
+    CK(cudaMalloc(&h->d_counters, sizeof(unsigned int) * (3 + kMaxMaterials)));
+    CK(cudaMemset(h->d_counters, 0, sizeof(unsigned int) * (3 + kMaxMaterials)));
     CK(cudaMalloc(&h->d_coop, sizeof(unsigned int) * 4));
     CK(cudaMemset(h->d_coop, 0, sizeof(unsigned int) * 4));
     CK(cudaMallocHost(&h->h_counters, sizeof(unsigned int) * (2 + kMaxMaterials)));
@@ -1714,7 +1715,8 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             h->coop = (int)value;
             return MPM_OK;
         case MPM_OPT_FP64_CLAMP:
-            h->fp64_clamp = value != 0;
+            if (value < 0 || value > 2) return finish(h, {MPM_ERR_VALUE, "FP64 clamp mode must be 0, 1 or 2"});
+            h->fp64_clamp = (int)value;
             invalidate_graph(h);  // the flag is a kernel argument of the captured graphs
             return MPM_OK;
         case MPM_OPT_P2G_GROUP:
@@ -1828,6 +1830,17 @@ int mpm_launch_count(void* handle, int64_t* launches) {
     HANDLE_OR_FAIL(handle);
     if (!launches) return finish(h, {MPM_ERR_ARGUMENT, "null output"});
     *launches = h->launches;
+    return MPM_OK;
+}
+
+int mpm_fp64_redo_lanes(void* handle, int64_t* lanes) {
+    HANDLE_OR_FAIL(handle);
+    unsigned int v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, h->d_counters + 2 + kMaxMaterials, sizeof(unsigned int),
+                                    cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return finish(h, {MPM_ERR_CUDA, cudaGetErrorString(e)});
+    if (lanes) *lanes = v;
     return MPM_OK;
 }
 

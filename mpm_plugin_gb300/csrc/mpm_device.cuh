@@ -345,7 +345,7 @@ MPM_HD void hencky_tau(const float F[3][3], float mu, float lam, float tau[3][3]
 // change of the singular values, delta = new - old, computed without cancellation; the caller applies
 // F <- F + U diag(delta) V^T, which equals U diag(new) V^T exactly when the SVD is exact and leaves F
 // untouched (no reconstruction round-off) when nothing is projected. Returns false when delta == 0.
-// Written for either precision: FP32 for the bulk, FP64 for the optional redo at an active clamp.
+// Written for either precision: FP32 for the bulk, FP64 for the optional redo of marginal decisions.
 // ---------------------------------------------------------------------------------------------------------
 template <typename T>
 MPM_HD bool project_von_mises(const T sig[3], const T d[3], T mu, T yield_stress, T delta[3]) {
@@ -361,10 +361,21 @@ MPM_HD bool project_von_mises(const T sig[3], const T d[3], T mu, T yield_stress
     return true;
 }
 
+// Relative width of the band around a return-mapping decision inside which an FP32 evaluation may decide
+// differently from an exact one (a few hundred FP32 ulps of the terms compared): the FP32 call reports such
+// a marginal decision, and the G2P build with the FP64 option redoes those lanes in FP64.
+constexpr float kMarginalRel = 2.0e-5f;
+
+// marginal (optional): set when the decision is within kMarginalRel of flipping (the sign of tr eps at the
+// separation test, the sign of dgamma at the cone) or the deviatoric direction is ill-conditioned (the three
+// log singular values nearly equal, n below kMarginalRel of their size).
 template <typename T>
-MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T alpha, T delta[3]) {
+MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T alpha, T delta[3],
+                                   bool* marginal = nullptr) {
     T e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
     T tr = e[0] + e[1] + e[2];
+    const T size = fabs(e[0]) + fabs(e[1]) + fabs(e[2]);
+    if (marginal) *marginal = fabs(tr) <= T(kMarginalRel) * size;
     if (tr >= T(0)) {  // separation: stress-free, singular values back to 1
 #pragma unroll
         for (int i = 0; i < 3; ++i) delta[i] = -d[i];
@@ -373,8 +384,10 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     T third = tr / T(3);
     T dev[3] = {e[0] - third, e[1] - third, e[2] - third};
     T n = sqrt_t(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
+    const T cone = (T(3) * lam + T(2) * mu) / (T(2) * mu) * tr * alpha;
+    if (marginal) *marginal = *marginal || n <= T(kMarginalRel) * size || fabs(n + cone) <= T(kMarginalRel) * (n - cone);
     if (n < T(1.0e-10f)) return false;
-    T dgamma = n + (T(3) * lam + T(2) * mu) / (T(2) * mu) * tr * alpha;
+    T dgamma = n + cone;
     if (dgamma <= T(0)) return false;
     T f = dgamma / n;
 #pragma unroll
@@ -382,19 +395,24 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     return true;
 }
 
+// marginal (optional): set when a singular value lies within kMarginalRel of a clamp bound (whether it is
+// clamped could change with its last bits).
 template <typename T>
-MPM_HD bool project_snow(const T sig[3], const T d[3], T clamp_lo, T clamp_hi, T delta[3], T* jp_ratio) {
-    bool any = false;
+MPM_HD bool project_snow(const T sig[3], const T d[3], T clamp_lo, T clamp_hi, T delta[3], T* jp_ratio,
+                         bool* marginal = nullptr) {
+    bool any = false, near = false;
     T num = T(1), den = T(1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         T ns = min_t(max_t(sig[i], clamp_lo), clamp_hi);
         delta[i] = ns == sig[i] ? T(0) : (ns - T(1)) - d[i];
         any |= delta[i] != T(0);
+        near |= fabs(sig[i] - clamp_lo) <= T(kMarginalRel) * clamp_lo || fabs(sig[i] - clamp_hi) <= T(kMarginalRel) * clamp_hi;
         num *= sig[i];
         den *= ns;
     }
     *jp_ratio = num / den;
+    if (marginal) *marginal = near;
     return any;
 }
 

@@ -564,7 +564,7 @@ struct ParticleIn {
 template <class Source, bool kFp64Clamp = false, class In = ParticleIn>
 MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const In& in, const Material* __restrict__ mats,
                               const GridDesc& g, float dt, const Source& src, unsigned int* fp64, float nx_out[3],
-                              bool fp64_clamp = false, float* tau_out = nullptr) {
+                              int fp64_clamp = 0, float* tau_out = nullptr, unsigned int* fp64_redo = nullptr) {
     // F, Jp and mat are read after the gather and the C store; their lines are requested now so that the
     // memory latency overlaps the gather
     if constexpr (In::kPrefetch) {
@@ -666,20 +666,26 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const In& in, const
     svd3(Fn, U, sig, d, V, fp64);
     const float jp_old = in.Jp();
     float jp = jp_old;
-    bool redo = false;  // FP64 redo at an active Drucker-Prager or snow clamp
+    bool redo = false;  // FP64 redo of a marginal Drucker-Prager or snow decision (or of every active clamp)
     if (m.model != 0) {
         float delta[3];
-        bool moved;
+        bool moved, marginal = false;
         if (m.model == 1) {
             moved = project_von_mises(sig, d, m.mu, m.yield_stress, delta);
         } else if (m.model == 2) {
-            moved = project_drucker_prager(sig, d, m.mu, m.lam, m.alpha, delta);
+            moved = project_drucker_prager(sig, d, m.mu, m.lam, m.alpha, delta, kFp64Clamp ? &marginal : nullptr);
         } else {
             float ratio;
-            moved = project_snow(sig, d, m.clamp_lo, m.clamp_hi, delta, &ratio);
+            moved = project_snow(sig, d, m.clamp_lo, m.clamp_hi, delta, &ratio, kFp64Clamp ? &marginal : nullptr);
             jp = jp * ratio;
         }
-        redo = kFp64Clamp && fp64_clamp && moved && m.model >= 2;
+        // fp64_clamp 1: the lanes whose FP32 decision was marginal; 2: every lane whose clamp was active
+        redo = kFp64Clamp && m.model >= 2 && (fp64_clamp == 2 ? moved : (fp64_clamp == 1 && marginal));
+#ifdef __CUDA_ARCH__
+        if (redo && fp64_redo) atomicAdd(fp64_redo, 1u);
+#else
+        if (redo && fp64_redo) *fp64_redo += 1u;
+#endif
         if (moved) {  // F = U diag(new) V^T, applied as F + U diag(new - old) V^T
 #pragma unroll
             for (int i = 0; i < 3; ++i)
@@ -744,10 +750,11 @@ struct CoherentSource {
 
 template <bool kFp64Clamp = false, class Source = GlobalSource>
 MPM_HD void g2p_particle(const Particles& P, int64_t p, const Material* __restrict__ mats, const GridDesc& g, float dt,
-                         const float4* grid, unsigned int* fp64, float nx_out[3], bool fp64_clamp = false,
-                         float* tau_out = nullptr) {
+                         const float4* grid, unsigned int* fp64, float nx_out[3], int fp64_clamp = 0,
+                         float* tau_out = nullptr, unsigned int* fp64_redo = nullptr) {
     Source src{&g, grid};
-    g2p_particle_from<Source, kFp64Clamp>(P, p, ParticleIn{P, p}, mats, g, dt, src, fp64, nx_out, fp64_clamp, tau_out);
+    g2p_particle_from<Source, kFp64Clamp>(P, p, ParticleIn{P, p}, mats, g, dt, src, fp64, nx_out, fp64_clamp, tau_out,
+                                          fp64_redo);
 }
 
 // Pushes a particle that ended up inside a collider onto its surface and removes its inward velocity

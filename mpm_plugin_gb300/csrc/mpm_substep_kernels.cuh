@@ -565,7 +565,7 @@ __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
         if (p >= a.n) return;
         float nx[3];
         g2p_particle<kFp64Clamp, Source>(particles_of(a), p, a.mats, a.g, a.sp->dt, grid_of(a, cur), a.fp64, nx,
-                                         a.fp64_clamp != 0);
+                                         a.fp64_clamp, nullptr, a.fp64_redo);
         if (a.cd.n_col > 0) {
             ColliderData cd = a.cd;
             cd.poses += a.sp->pose_base;
@@ -579,7 +579,7 @@ __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
         bool listed = false;
         if (live) {
             g2p_particle<kFp64Clamp, Source>(P, p, a.mats, a.g, a.sp->dt, grid_of(a, cur), a.fp64, nx,
-                                             a.fp64_clamp != 0, tau);
+                                             a.fp64_clamp, tau, a.fp64_redo);
             if (a.cd.n_col > 0) {
                 ColliderData cd = a.cd;
                 cd.poses += a.sp->pose_base;

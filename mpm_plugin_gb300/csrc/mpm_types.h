@@ -177,7 +177,9 @@ struct SubstepArgs {
     unsigned int* poison;
     int fixed_exp;
     int p2g_group;  // P2G sums runs of same-base lanes within aligned groups of this many lanes (1 .. 32)
-    int fp64_clamp;  // 1: Drucker-Prager and snow particles at an active clamp are redone in FP64 in G2P
+    int fp64_clamp;  // Drucker-Prager / snow return mapping redone in FP64 in G2P: 1 the lanes whose FP32
+                     // decision was marginal, 2 every lane whose clamp was active, 0 none
+    unsigned int* fp64_redo;  // count of the lanes redone in FP64
     unsigned int* err;  // set to nonzero by a kernel whose bounded wait gave up (the host reports it)
     int block_sweep;    // 1: P2G only flags the blocks it touches; k_list_blocks lists them afterwards
 };

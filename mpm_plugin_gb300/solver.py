@@ -334,3 +334,9 @@ class Gb300Solver(Solver):
         v = C.c_int64()
         self._check(self._lib.mpm_fp64_lanes(self._h, C.byref(v)))
         return v.value
+
+    def fp64_redo_lanes(self) -> int:
+        """Drucker-Prager / snow lanes G2P redid in FP64 (MPM_OPT_FP64_CLAMP) since the solver was created."""
+        v = C.c_int64()
+        self._check(self._lib.mpm_fp64_redo_lanes(self._h, C.byref(v)))
+        return v.value

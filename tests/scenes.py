@@ -12,6 +12,9 @@ import numpy as np
 from _golden import GOLDEN, Domain, material_from_dict
 
 from mpm_plugin_gb300.interface import MaterialParams
+from mpm_plugin_gb300.workloads import (cylinder, lattice_box, plane_mesh, rot_x, rot_y, rot_z, scale,  # noqa: F401
+                                        torus, translate)
+from mpm_plugin_gb300.workloads import pour_job as pour_job_spec  # noqa: F401
 from oracle import geometry
 
 WALL_SIDES = ("x-", "x+", "y-", "y+", "z-", "z+")
@@ -29,30 +32,6 @@ def preset_names() -> list[str]:
     return sorted(_PRESETS)
 
 
-def translate(x, y, z) -> np.ndarray:
-    m = np.eye(4, dtype=np.float32)
-    m[:3, 3] = (x, y, z)
-    return m
-
-
-def scale(x, y=None, z=None) -> np.ndarray:
-    return np.diag([x, x if y is None else y, x if z is None else z, 1.0]).astype(np.float32)
-
-
-def rot_x(deg: float) -> np.ndarray:
-    a = np.radians(deg)
-    m = np.eye(4, dtype=np.float32)
-    m[1, 1], m[1, 2], m[2, 1], m[2, 2] = np.cos(a), -np.sin(a), np.sin(a), np.cos(a)
-    return m
-
-
-def rot_y(deg: float) -> np.ndarray:
-    a = np.radians(deg)
-    m = np.eye(4, dtype=np.float32)
-    m[0, 0], m[0, 2], m[2, 0], m[2, 2] = np.cos(a), np.sin(a), -np.sin(a), np.cos(a)
-    return m
-
-
 def unit_cube_mesh(centered: bool = False):
     """Closed cube with outward winding: [0,1]^3, or [-0.5,0.5]^3 when centered."""
     v = np.array([[x, y, z] for z in (0, 1) for y in (0, 1) for x in (0, 1)], np.float32)
@@ -61,13 +40,6 @@ def unit_cube_mesh(centered: bool = False):
     t = np.array([[0, 2, 1], [1, 2, 3], [4, 5, 6], [5, 7, 6], [0, 1, 4], [1, 5, 4],
                   [2, 6, 3], [3, 6, 7], [0, 4, 2], [2, 4, 6], [1, 3, 5], [3, 7, 5]], np.int32)
     return v, t
-
-
-def plane_mesh(size: float):
-    """Open square in the xy plane centred at the origin, normal +z."""
-    h = size / 2
-    return (np.array([[-h, -h, 0], [h, -h, 0], [h, h, 0], [-h, h, 0]], np.float32),
-            np.array([[0, 1, 2], [0, 2, 3]], np.int32))
 
 
 def icosphere(radius: float, subdivisions: int, seed: int | None = None, jitter: float = 0.0):
@@ -158,131 +130,6 @@ def mix_scene(res: int = 128, seed: int = 0):
     cv, ct = icosphere(1.0, 4, seed=seed + 3, jitter=0.03)
     xf = translate(0.75, 0.7, 0.1) @ scale(0.12)
     return d, mats, groups, (cv, ct, xf)
-
-
-def lattice_box(lo, hi, spacing: float, rng) -> np.ndarray:
-    """Particles on a lattice of the given spacing filling [lo, hi], each jittered by U(+-spacing / 4)."""
-    axes = [np.arange(lo[a] + spacing / 2, hi[a], spacing, dtype=np.float64) for a in range(3)]
-    g = np.stack(np.meshgrid(*axes, indexing="ij"), -1).reshape(-1, 3)
-    g += rng.uniform(-0.25 * spacing, 0.25 * spacing, g.shape)
-    return g.astype(np.float32)
-
-
-BATCH_MODELS = ("elastic", "von_mises", "drucker_prager", "snow")
-
-
-def batched_scenes(seed: int = 0, count: int = 64, n_lo: float = 1e4, n_hi: float = 2e6):
-    """Independent scenes of the batched workload: particle counts log-uniform in [n_lo, n_hi], grids from 32^3
-    to 192^3 matched to the count (a cube of material filling the same fraction of every grid, 8 per cell),
-    one material per scene with the model uniform over the four and parameters uniform within the ranges of the
-    jelly and mixed-materials workloads, a random initial velocity, and 0-2 static seeded perturbed icosphere
-    colliders of 1,280, 5,120 or 20,480 triangles below the material.
-
-    Returns [(domain, [material], positions, velocity, [(verts, tris, world matrix, friction)])].
-    """
-    rng = np.random.default_rng(seed)
-    out = []
-    for i in range(count):
-        n_target = float(np.exp(rng.uniform(np.log(n_lo), np.log(n_hi))))
-        res = int(np.clip(round(32 * (n_target / 1e4) ** (1 / 3)), 32, 192))
-        d = domain(res=res)
-        side = min((n_target / 8) ** (1 / 3) / res, 0.6)
-        lo = (0.5 - side / 2, 0.5 - side / 2, 0.25)
-        hi = (0.5 + side / 2, 0.5 + side / 2, 0.25 + side)
-        pos = lattice_box(lo, hi, d.dx / 2, rng)
-        model = BATCH_MODELS[int(rng.integers(4))]
-        mat = MaterialParams(f"batch{i}", model, float(rng.uniform(2e4, 3.5e5)), float(rng.uniform(0.2, 0.45)),
-                             float(rng.uniform(400.0, 1600.0)), yield_stress=float(rng.uniform(300.0, 3000.0)),
-                             friction_angle_deg=float(rng.uniform(30.0, 35.0)), hardening=10.0,
-                             critical_compression=2.5e-2, critical_stretch=7.5e-3,
-                             max_hardening=float(rng.uniform(5.0, 20.0)))
-        vel = tuple(float(c) for c in rng.uniform(-1.0, 1.0, 3))
-        cols = []
-        for c in range(int(rng.integers(0, 3))):
-            cv, ct = icosphere(1.0, int(rng.choice([3, 4, 5])), seed=seed * 1000 + i * 10 + c, jitter=0.03)
-            r = float(rng.uniform(0.06, 0.12))
-            xf = translate(float(rng.uniform(0.25, 0.75)), float(rng.uniform(0.25, 0.75)), r) @ scale(r)
-            cols.append((cv, ct, xf, float(rng.uniform(0.0, 0.5))))
-        out.append((d, [mat], pos, vel, cols))
-    return out
-
-
-def torus(major: float, minor: float, n_major: int, n_minor: int, seed: int | None = None, jitter: float = 0.0):
-    """Closed torus around the z axis (2 * n_major * n_minor triangles, outward winding); with a seed every
-    vertex's tube radius is scaled by 1 + U(-jitter, jitter)."""
-    u = 2 * np.pi * np.arange(n_major) / n_major
-    v = 2 * np.pi * np.arange(n_minor) / n_minor
-    r = np.full((n_major, n_minor), minor)
-    if seed is not None:
-        r = r * (1 + np.random.default_rng(seed).uniform(-jitter, jitter, r.shape))
-    cu, su, cv, sv = np.cos(u)[:, None], np.sin(u)[:, None], np.cos(v)[None, :], np.sin(v)[None, :]
-    verts = np.stack([(major + r * cv) * cu, (major + r * cv) * su, r * sv], -1).reshape(-1, 3)
-    i, j = np.meshgrid(np.arange(n_major), np.arange(n_minor), indexing="ij")
-    a = i * n_minor + j
-    b = ((i + 1) % n_major) * n_minor + j
-    c = ((i + 1) % n_major) * n_minor + (j + 1) % n_minor
-    d = i * n_minor + (j + 1) % n_minor
-    tris = np.concatenate([np.stack([a, b, c], -1).reshape(-1, 3), np.stack([a, c, d], -1).reshape(-1, 3)])
-    return verts.astype(np.float32), tris.astype(np.int32)
-
-
-def rot_z(deg: float) -> np.ndarray:
-    c, s = np.cos(np.radians(deg)), np.sin(np.radians(deg))
-    m = np.eye(4)
-    m[:2, :2] = [[c, -s], [s, c]]
-    return m
-
-
-def pour_job_spec(seed: int, res: int = 96, frames: int = 12, fps: float = 24.0, side_range=(0.2, 0.4)):
-    """A granular pour (the large inflow workload's distribution at a serving size): a Drucker-Prager pile
-    (E 3.5e5, nu 0.3, 30 deg, rho 1600) of seeded size, a disc inflow r = 0.05 m at 2 m/s downward whose slab
-    of one frame is added where no material is, and a seeded torus collider (2,048 triangles, friction 0.4)
-    turning at 1 rev/s. Returns (domain, materials, setup(solver), before_frame(solver, k), frames, fps,
-    max_particles, collider_triangles)."""
-    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
-
-    rng = np.random.default_rng(seed)
-    d = domain(res=res)
-    mat = MaterialParams("pour", "drucker_prager", 3.5e5, 0.3, 1600.0, friction_angle_deg=30.0)
-    side = float(rng.uniform(*side_range))
-    pile = lattice_box((0.5 - side / 2, 0.5 - side / 2, 0.0), (0.5 + side / 2, 0.5 + side / 2, side / 2), d.dx / 2,
-                       rng)
-    tv, tt = torus(0.18, 0.04, 64, 16, seed=seed, jitter=0.05)
-
-    def pose(t):
-        return translate(0.5, 0.5, 0.35) @ rot_z(360.0 * t) @ rot_x(90.0)
-
-    def setup(s):
-        s.add_particles(pile, np.zeros_like(pile), np.zeros(len(pile), np.int32), np.zeros(len(pile), np.int32))
-        s.set_colliders([ColliderGeometry(MeshData(tv, tt), closed=True, friction=0.4)])
-
-    def before_frame(s, k):
-        s.set_collider_transforms(pose((k - 1) / fps)[None], pose(k / fps)[None])
-        r = np.random.default_rng(seed * 1000 + k)
-        slab = lattice_box((0.45, 0.45, 0.85), (0.55, 0.55, 0.85 + 2.0 / fps), d.dx / 2, r)
-        slab = slab[np.hypot(slab[:, 0] - 0.5, slab[:, 1] - 0.5) <= 0.05]
-        free = ~s.is_occupied(slab)
-        if free.any():
-            p = slab[free]
-            s.add_particles(p, np.tile(np.float32([0.0, 0.0, -2.0]), (len(p), 1)), np.zeros(len(p), np.int32),
-                            np.zeros(len(p), np.int32))
-
-    slab_n = int(np.pi * 0.05 ** 2 * 2.0 / fps * 8 * res ** 3) + 1
-    return d, [mat], setup, before_frame, frames, fps, len(pile) + frames * slab_n, len(tt)
-
-
-def cylinder(radius: float, height: float, segments: int = 32):
-    """Closed cylinder around the z axis from z = 0 to height (4 * segments triangles, outward winding)."""
-    a = 2 * np.pi * np.arange(segments) / segments
-    ring = np.stack([radius * np.cos(a), radius * np.sin(a)], -1)
-    verts = np.concatenate([np.c_[ring, np.zeros(segments)], np.c_[ring, np.full(segments, height)],
-                            [[0.0, 0.0, 0.0], [0.0, 0.0, height]]])
-    bc, tc = 2 * segments, 2 * segments + 1
-    tris = []
-    for k in range(segments):
-        k1 = (k + 1) % segments
-        tris += [[k, k1, segments + k1], [k, segments + k1, segments + k], [bc, k1, k], [tc, segments + k, segments + k1]]
-    return verts.astype(np.float32), np.array(tris, np.int32)
 
 
 def bake_scene(resolution: int = 16, frame_end: int = 4, emit_frames=(1, 3), substeps: int = 2,

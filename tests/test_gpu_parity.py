@@ -124,10 +124,12 @@ def test_one_substep_matches_oracle(scene):
         assert e <= 1e-5, (k, e)
 
 
-def test_fp64_clamp_is_closer_to_the_fp64_oracle():
-    """Sand (Drucker-Prager) and snow particles at an active clamp redone in FP64 (MPM_OPT_FP64_CLAMP): one
-    substep stays within 1e-5 of the FP32 oracle and its F, Jp and x are no further from the FP64 oracle than
-    the FP32 build's."""
+@pytest.mark.parametrize("mode", [1, 2])
+def test_fp64_clamp_is_closer_to_the_fp64_oracle(mode):
+    """Sand (Drucker-Prager) and snow particles with the return mapping redone in FP64 (MPM_OPT_FP64_CLAMP):
+    mode 1 redoes the lanes whose FP32 decision was marginal, mode 2 every lane whose clamp was active. One
+    substep stays within 1e-5 of the FP32 oracle, and F, Jp and x are no further from the FP64 oracle than the
+    FP32 build's; mode 1 redoes a small share of what mode 2 redoes."""
     from mpm_plugin_gb300 import _abi
 
     d = domain(res=32)
@@ -135,7 +137,7 @@ def test_fp64_clamp_is_closer_to_the_fp64_oracle():
     groups = [(box_particles((0.1 + 0.4 * i, 0.3, 0.05), (0.45 + 0.4 * i, 0.6, 0.4), d.dx, seed=i), i, (0, 0, 0))
               for i in range(2)]
     gs = [gpu_solver(d, mats), gpu_solver(d, mats)]
-    gs[1].set_option(_abi.OPT_FP64_CLAMP, 1)
+    gs[1].set_option(_abi.OPT_FP64_CLAMP, mode)
     o32, o64 = _oracle(d, mats), _oracle(d, mats, precision="f64")
     for pos, m, vel in groups:
         add(gs[0], pos, m, m, vel)
@@ -155,9 +157,15 @@ def test_fp64_clamp_is_closer_to_the_fp64_oracle():
         assert rel_err(redo[k], r32[k]) <= 1e-5, k
     e_plain = {k: rel_err(plain[k], r64[k]) for k in ("x", "F", "Jp")}
     e_redo = {k: rel_err(redo[k], r64[k]) for k in ("x", "F", "Jp")}
-    print({k: f"{e_plain[k]:.2e} -> {e_redo[k]:.2e}" for k in e_plain})
+    lanes = gs[1].fp64_redo_lanes()
+    print(mode, lanes, "of", len(state["x"]), {k: f"{e_plain[k]:.2e} -> {e_redo[k]:.2e}" for k in e_plain})
     for k in e_plain:
         assert e_redo[k] <= 1.05 * e_plain[k] + 1e-9, (k, e_plain[k], e_redo[k])
+    assert gs[0].fp64_redo_lanes() == 0
+    if mode == 2:
+        assert lanes >= snow_clamped.sum()
+    else:
+        assert lanes < 0.1 * len(state["x"])
 
 
 def _invariants(s: dict, pmass: np.ndarray) -> dict:
