@@ -194,18 +194,23 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
         torch.cuda.synchronize()
         return out, time.perf_counter() - t0
 
-    # plain: one scene at a time (each scene's frames back to back, as separate bake jobs would run)
-    plain_ps, plain_s, plain_frame_ms = 0.0, 0.0, []
+    from mpm_plugin_gb300 import tune
+
+    # plain: one scene at a time (each scene's frames back to back, as separate bake jobs would run), each
+    # with launch choices tuned for it (the autotuner's cache serves scenes of one workload class)
+    plain_ps, plain_s, plain_frame_ms, plain_steps = 0.0, 0.0, [], []
     for s, n in zip(solvers, counts):
-        s.advance(BATCH_FRAME_DT)
+        st0 = s.advance(BATCH_FRAME_DT)
+        snapshot = s.save_state()
+        tune.tune_solver(s, st0.dt, BATCH_FRAME_DT, substeps=10)
+        s.load_state(snapshot)
+        plain_steps.append(st0.substeps)
         for _ in range(frames):
             st, el = timed(lambda: s.advance(BATCH_FRAME_DT))
             plain_ps += n * st.substeps
             plain_s += el
             plain_frame_ms.append(1e3 * el)
     batch = Gb300Batch(solvers)
-    from mpm_plugin_gb300 import tune
-
     tuned = tune.tune_batch(batch, BATCH_FRAME_DT, frames=1)
     batch.advance(BATCH_FRAME_DT)
     launches0 = batch.launch_count()
@@ -216,6 +221,10 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
         batch_s += el
         batch_frame_ms.append(1e3 * el)
     launches = batch.launch_count() - launches0
+    # the batch replays max(steps) substeps a frame; a scene whose own substeps are done idles (its work
+    # lists and particle chunks drop out of every kernel): the share of scene-substeps that idle
+    last = [st.substeps for st in stats]
+    idle_share = 1.0 - sum(last) / (len(last) * max(max(last), 1))
     batch.close()
     for s in solvers:
         s.close()
@@ -228,6 +237,8 @@ def run_batched(device: str, frames: int, n_hi: float = 2e6) -> dict:
             "plain_scene_frame_ms": {"p50": float(np.percentile(plain_frame_ms, 50)),
                                      "p99": float(np.percentile(plain_frame_ms, 99))},
             "gpu_launches_per_frame": launches / frames, "tuned": tuned,
+            "substeps_per_frame": {"min": int(min(last)), "max": int(max(last))},
+            "idle_scene_substep_share": idle_share,
             "timing": "host clock around advance calls with device synchronisation; state resident in HBM"}
 
 
@@ -241,8 +252,9 @@ class _FrameSink:
         self.bytes += particles.positions.nbytes + particles.velocities.nbytes
 
 
-def serve_trace(seconds: float, rate: float, seed: int = 0):
-    """Poisson arrivals (mean `rate` per second) over `seconds`; each request one seeded pour job."""
+def serve_trace(seconds: float, rate: float, seed: int = 0, frames: int = 8, res: int = 128):
+    """Poisson arrivals (mean `rate` per second) over `seconds`; each request one seeded pour job of `frames`
+    frames at resolution `res`."""
     from mpm_plugin_gb300.serve import BakeJob
     from mpm_plugin_gb300.workloads import pour_job as pour_job_spec
 
@@ -252,32 +264,34 @@ def serve_trace(seconds: float, rate: float, seed: int = 0):
         t += float(rng.exponential(1.0 / rate))
         if t > seconds:
             return trace
-        d, mats, setup, before, frames, fps, max_n, tris = pour_job_spec(seed * 1000 + i, res=128, frames=16,
-                                                                         side_range=(0.25, 0.45))
-        trace.append((t, BakeJob(f"job{i}", d, mats, frames, fps, setup=setup, before_frame=before,
+        d, mats, setup, before, nf, fps, max_n, tris = pour_job_spec(seed * 1000 + i, res=res, frames=frames,
+                                                                     side_range=(0.25, 0.45))
+        trace.append((t, BakeJob(f"job{i}", d, mats, nf, fps, setup=setup, before_frame=before,
                                  writer=_FrameSink(), max_particles=max_n, collider_triangles=tris)))
         i += 1
 
 
-def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float = 150.0) -> dict:
+def run_serving(device: str, seconds: float, rate: float = 3.0, budget_gb: float = 6.0, frames: int = 8) -> dict:
     """Serving: a Poisson trace of pour jobs (128^3, a pile of 130k-760k particles plus a 2 m/s disc inflow, a
-    2,048-triangle torus turning at 1 rev/s, 16 frames at 24 fps each; at 4 requests per second the GPU is
-    the bottleneck) served by the bake server with a 150 GB admission budget, against the same trace served
-    sequentially by the plain solver (each job alone, in arrival order, starting when it has arrived and
-    the one before has finished)."""
+    2,048-triangle torus turning at 1 rev/s, `frames` frames at 24 fps each) served by the bake server with an
+    admission budget of `budget_gb` (a few jobs' worth, so admission waits on memory), against the same trace
+    served sequentially by the plain solver (each job alone, in arrival order, starting when it has arrived
+    and the one before has finished). The metric's trace (8M-particle pours, 48 frames, 4 per second for 10
+    minutes, 150 GB) is two orders of magnitude beyond one GPU; this one keeps its shape: Poisson arrivals at
+    about the GPU's capacity, so queues form, with memory the binding limit on admission."""
     import torch
 
     from mpm_plugin_gb300.serve import BakeServer
     from mpm_plugin_gb300.solver import Gb300Solver
 
-    trace = serve_trace(seconds, rate)
+    trace = serve_trace(seconds, rate, frames=frames)
     srv = BakeServer(int(budget_gb * (1 << 30)), device=device)
     rep = srv.run(trace)
     srv.close()
     served = rep.summary()
 
     # the same trace, sequentially through the plain solver
-    trace = serve_trace(seconds, rate)
+    trace = serve_trace(seconds, rate, frames=frames)
     clock, frame_ms, job_s, ps = 0.0, [], [], 0.0
     for arrival, job in trace:
         clock = max(clock, arrival)
@@ -306,7 +320,8 @@ def run_serving(device: str, seconds: float, rate: float = 4.0, budget_gb: float
     return {"requests": len(trace), "rate_per_s": rate, "seconds": seconds, "budget_gb": budget_gb,
             "served": served, "plain_sequential": plain,
             "ratio": served["particle_substeps_per_s"] / plain["particle_substeps_per_s"],
-            "workload": "Poisson pour jobs, 128^3, 16 frames at 24 fps, inflow + rotating 2,048-triangle torus; "
+            "frames_per_job": frames,
+            "workload": f"Poisson pour jobs, 128^3, {frames} frames at 24 fps, inflow + rotating 2,048-triangle torus; "
                         "frames handed to an in-memory sink in place of the cache writer"}
 
 
@@ -747,7 +762,8 @@ def run_gpu(args, world, rank, local):
         solver.close()
         batched = run_batched(device, args.batched_frames)
         batched["small_scenes"] = run_batched(device, args.batched_frames, n_hi=1e5)
-    serving = run_serving(device, args.serve_seconds) if args.serve_seconds > 0 else None
+    serving = (run_serving(device, args.serve_seconds, args.serve_rate, args.serve_budget_gb, args.serve_frames)
+               if args.serve_seconds > 0 else None)
     large = None
     if args.large_frames > 0:
         large, final, tmesh, pose_end = run_large(device, args.large_frames)
@@ -844,8 +860,11 @@ def main():
     ap.add_argument("--small", type=int, default=1, help="measure the 32k-particle jelly workload (0: skip)")
     ap.add_argument("--large-frames", type=int, default=1,
                     help="24 fps frames of the 256^3 inflow workload (0: skip)")
-    ap.add_argument("--serve-seconds", type=float, default=4.0,
-                    help="seconds of Poisson bake requests (4 per second) for the serving measurement (0: skip)")
+    ap.add_argument("--serve-seconds", type=float, default=120.0,
+                    help="seconds of Poisson bake requests for the serving measurement (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=3.0, help="bake requests per second")
+    ap.add_argument("--serve-frames", type=int, default=8, help="frames per bake request")
+    ap.add_argument("--serve-budget-gb", type=float, default=6.0, help="admission budget of the bake server")
     ap.add_argument("--batched-frames", type=int, default=3,
                     help="frames of the 64-scene batched workload, plain and batched (0: skip)")
     ap.add_argument("--surface", type=int, default=1, help="measure the surfacer (0: skip)")

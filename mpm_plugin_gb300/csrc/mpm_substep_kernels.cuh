@@ -316,13 +316,32 @@ __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
 
 // Five CTAs of 256 per SM (48 registers, a few spilled values): the warps it adds hide more of P2G's memory
 // latency than the spills cost (P2G 2-3 % faster than at 64 registers on the mixed and the 256^3 workloads).
+// Chunks of 256 particles of a scene (the work items of the batched particle kernels).
+__device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
+    return (unsigned int)((a.n + 255) / 256);
+}
+
+// A batch's particle kernels walk the flattened (scene, chunk) list of the scenes that run this substep
+// (scene_offsets over the chunk counts), grid-stride, so a scene that has finished its substeps for the
+// frame costs no CTAs. One scene: one CTA per chunk.
 template <class Scenes>
 __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
     pdl_begin();
-    const int s = sc.scene_of_cta(blockIdx.x);
-    const SubstepArgs a = sc.get(s);
-    if (!sc.active(a) || a.sp->p2g_skip) return;
-    p2g_cta(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
+    if constexpr (!Scenes::kTable) {
+        const SubstepArgs a = sc.get(0);
+        if (a.sp->p2g_skip) return;
+        p2g_cta(a, (int64_t)blockIdx.x * blockDim.x);
+    } else {
+        __shared__ unsigned int off[kMaxBatchScenes + 1];
+        const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
+            return a.sp->p2g_skip ? 0u : particle_chunks(a);
+        }, off);
+#pragma unroll 1
+        for (unsigned int q = blockIdx.x; q < total; q += gridDim.x) {
+            const int s = scene_of_item(off, sc.count(), q);
+            p2g_cta(sc.scenes[s], (int64_t)(q - off[s]) * blockDim.x);  // the table entry in place
+        }
+    }
 }
 
 // P2G through shared-memory tiles. The CTA's 256 particles (a contiguous range of the particle order) are
@@ -599,10 +618,18 @@ __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
 template <class Scenes, int kMinCtas, bool kFp64Clamp = false, bool kScatter = false>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     pdl_begin();
-    const int s = sc.scene_of_cta(blockIdx.x);
-    const SubstepArgs a = sc.get(s);
-    if (!sc.active(a)) return;
-    g2p_cta<kFp64Clamp, GlobalSource, kScatter>(a, (int64_t)(blockIdx.x - sc.first_cta(s)) * blockDim.x);
+    if constexpr (!Scenes::kTable) {
+        g2p_cta<kFp64Clamp, GlobalSource, kScatter>(sc.get(0), (int64_t)blockIdx.x * blockDim.x);
+    } else {  // (scene, chunk) list of the running scenes, as in k_p2g_scatter
+        __shared__ unsigned int off[kMaxBatchScenes + 1];
+        const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) { return particle_chunks(a); }, off);
+#pragma unroll 1
+        for (unsigned int q = blockIdx.x; q < total; q += gridDim.x) {
+            const int s = scene_of_item(off, sc.count(), q);
+            // the scene's entry is read in place from the table (a copy of the whole record would be spilled)
+            g2p_cta<kFp64Clamp, GlobalSource, kScatter>(sc.scenes[s], (int64_t)(q - off[s]) * blockDim.x);
+        }
+    }
 }
 
 // Projection of one listed particle (the same two shapes as for the nodes); where the substep scatters for

@@ -89,6 +89,8 @@ class ServeReport:
     wall_s: float = 0.0
     max_resident: int = 0
     max_reserved: int = 0
+    admit_wait_s: list = field(default_factory=list)  # per admitted job: admission time - arrival
+    max_queue: int = 0                                 # most jobs that had arrived and waited for admission
 
     def summary(self) -> dict:
         lat = self.frame_latency_ms
@@ -98,7 +100,11 @@ class ServeReport:
                 "jobs": len(self.job_latency_s), "rejected": len(self.rejected), "failed": len(self.failed),
                 "particle_substeps_per_s": self.particle_substeps / self.wall_s if self.wall_s else 0.0,
                 "busy_particle_substeps_per_s": self.particle_substeps / self.busy_s if self.busy_s else 0.0,
-                "max_resident_jobs": self.max_resident, "max_reserved_bytes": self.max_reserved}
+                "max_resident_jobs": self.max_resident, "max_reserved_bytes": self.max_reserved,
+                "admission_wait_s": {"p50": float(np.percentile(self.admit_wait_s, 50)) if self.admit_wait_s else None,
+                                     "p99": float(np.percentile(self.admit_wait_s, 99)) if self.admit_wait_s else None,
+                                     "max": float(max(self.admit_wait_s)) if self.admit_wait_s else None},
+                "max_queue": self.max_queue}
 
 
 class _Writer(threading.Thread):
@@ -175,7 +181,9 @@ class BakeServer:
                 self.report.rejected.append(job.name)
                 continue
             if self.reserved + need > self.budget:
-                return  # FIFO: wait until resident jobs finish and free their memory
+                # FIFO: wait until resident jobs finish and free their memory
+                self.report.max_queue = max(self.report.max_queue, sum(1 for a, _ in self.pending if a <= now))
+                return
             self.pending.popleft()
             solver = self.make_solver(job)
             if job.setup:
@@ -183,6 +191,7 @@ class BakeServer:
             self.batch.add(solver)
             t = self.now()
             self.runs.append(_Run(job, solver, need, arrival, t, last=t))
+            self.report.admit_wait_s.append(t - arrival)
             self.reserved += need
         self.report.max_resident = max(self.report.max_resident, len(self.runs))
         self.report.max_reserved = max(self.report.max_reserved, self.reserved)

@@ -109,3 +109,28 @@ def test_batch_errors():
     with pytest.raises(ValueError, match="positive"):
         b1.advance(0.0)
     assert b2.advance(1 / 24) == []
+
+
+def test_one_batched_substep_matches_the_scenes_alone_within_1e_5():
+    """One substep per scene (a frame shorter than every scene's CFL step): the batched launches against each
+    scene's own within 1e-5, the bar of the one-substep parity tests (C against |v| / dx)."""
+    from mpm_plugin_gb300.batch import Gb300Batch
+
+    alone, batched = _scenes(), _scenes()
+    batch = Gb300Batch(batched)
+    fdt = [2e-5, 1e-5, 2e-5, 2e-5]
+    st_alone = [s.advance(f) for s, f in zip(alone, fdt)]
+    st_batch = batch.advance(fdt)
+    for a, b in zip(st_alone, st_batch):
+        assert a.substeps == b.substeps
+    assert [st.substeps for st in st_batch[:3]] == [1, 1, 1]
+    for a, b in zip(alone, batched):
+        sa, sb = a.save_state(), b.save_state()
+        if len(sa["x"]) == 0:
+            continue
+        dx = 1.0 / a.domain.resolution
+        gnorm = float(np.linalg.norm(sa["v"]) / dx)
+        for k in ("x", "v", "C", "F", "Jp"):
+            e = rel_err(sb[k], sa[k], floor=gnorm if k == "C" else 0.0)
+            assert e <= 1e-5, (k, e)
+    batch.close()

@@ -87,3 +87,38 @@ def test_each_job_same_alone_and_in_the_mix():
             assert pa.shape == pm.shape, (a.name, k)
             assert rel_err(pm, pa) <= 1e-4, (a.name, k, rel_err(pm, pa))
     assert len(rep.frame_latency_ms) == sum(j.frames for j in mixed)
+
+
+def test_deterministic_jobs_are_bit_identical_alone_and_in_the_mix():
+    """In deterministic mode (fixed-point P2G and occupancy) a job's frames do not depend on what else is in
+    the batch: bit-identical to the job baked alone."""
+    from mpm_plugin_gb300 import _abi
+    from mpm_plugin_gb300.solver import Gb300Solver
+
+    def make(job):
+        s = Gb300Solver(job.domain, job.materials, job.gravity, job.particles_per_cell, device="cuda:0")
+        s.set_option(_abi.OPT_DETERMINISTIC, 1)
+        return s
+
+    alone, mixed = _jobs(), _jobs()
+    for job in alone:
+        s = make(job)
+        if job.setup:
+            job.setup(s)
+        for k in range(1, job.frames + 1):
+            if job.before_frame:
+                job.before_frame(s, k)
+            s.advance(1.0 / job.fps)
+            job.writer.write_frame(k, s.get_particles())
+        s.close()
+    srv = BakeServer(8 << 30, make_solver=make)
+    srv.submit(mixed[0])
+    srv.submit(mixed[1])
+    srv.tick()
+    srv.submit(mixed[2])
+    rep = srv.run()
+    srv.close()
+    assert rep.max_resident == 3 and not rep.failed
+    for a, m in zip(alone, mixed):
+        for k in range(1, m.frames + 1):
+            np.testing.assert_array_equal(m.writer.frames[k], a.writer.frames[k], err_msg=f"{a.name} frame {k}")
