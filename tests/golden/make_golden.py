@@ -324,6 +324,53 @@ def geometry_cases(only):
     print("geometry: written")
 
 
+def surface_cases(only):
+    """The surfacer's field stage (mpm_surface/field.py): the reference's unchanged surface_particles on a
+    seeded particle blob, with its splat, normalize and sample_velocity kernels run by the emulator. Warp's
+    MarchingCubes (not in the reference's sources) is replaced by a stand-in that keeps the density field it
+    is given and hands back a set of sample points, so the reference's own code samples its velocity field at
+    them (field.py:131-136)."""
+    if only and "surface_field" not in only:
+        return
+    import warp as wp
+    from mpm_surface import field
+    from mpm_surface.settings import SurfaceSettings
+
+    rng = np.random.default_rng(41)
+    spacing = 0.01
+    g = (np.stack(np.meshgrid(*[np.arange(8)] * 3, indexing="ij"), -1).reshape(-1, 3) + 0.5) * spacing
+    c = g.mean(0)
+    pts = g[np.linalg.norm(g - c, axis=1) < 3.6 * spacing]
+    pts = (pts + rng.uniform(-0.25, 0.25, pts.shape) * spacing + np.array([0.3, 0.5, 0.2])).astype(np.float32)
+    vel = (np.cross(np.array([0.0, 0.0, 2.0]), pts - pts.mean(0)) + rng.normal(0, 0.05, pts.shape)).astype(np.float32)
+    captured = {}
+
+    class SampleOnly:  # in place of wp.MarchingCubes
+        def __init__(self, nx, ny, nz, device=None):
+            self.dims = (nx, ny, nz)
+            r = np.random.default_rng(42)
+            self.verts = wp.array(r.uniform(0.0, 1.0, (400, 3)) * (np.array(self.dims) - 1), dtype=wp.vec3)
+            self.indices = wp.array(np.zeros(3, np.int32), dtype=int)
+
+        def surface(self, density, iso):
+            captured["density"] = density.numpy()
+            captured["verts"] = self.verts.numpy()
+
+    wp.MarchingCubes = SampleOnly
+    out = {}
+    for name, st in (("d1_s2", SurfaceSettings(detail=1.0, smoothing=2.0, iso=0.35)),
+                     ("d15_s15", SurfaceSettings(detail=1.5, smoothing=1.5, iso=0.5))):
+        mesh = field.surface_particles(pts, vel, spacing, st, device="cpu", max_bytes=1 << 40)
+        out[f"{name}_density"] = captured["density"]   # normalised density field (field.py:123)
+        out[f"{name}_sample_grid"] = captured["verts"]  # sample points, grid index units
+        out[f"{name}_sample_world"] = mesh.verts        # the same points in world space (field.py:139)
+        out[f"{name}_sample_vel"] = mesh.vel            # velocity field sampled there (field.py:135-136)
+        out[f"{name}_settings"] = np.array([st.detail, st.smoothing, st.iso])
+    np.savez_compressed(HERE / "surface_field.npz", positions=pts, velocities=vel, spacing=np.float64(spacing),
+                        meta=np.array(json.dumps({"case": "surface_field", "cases": ["d1_s2", "d15_s15"]})), **out)
+    print("surface_field: written")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     env = os.environ.get("MPM_PLUGIN_REFERENCE")
@@ -334,6 +381,7 @@ def main() -> None:
     _install(args.reference)
     geometry_cases(set(args.only))
     solver_cases(set(args.only))
+    surface_cases(set(args.only))
 
 
 if __name__ == "__main__":

@@ -310,6 +310,10 @@ def floor(x):
     return f32(np.floor(f32(x)))
 
 
+def ceil(x):
+    return f32(np.ceil(f32(x)))
+
+
 def round(x):  # noqa: A001 - Warp's name; halfway cases go away from zero
     x = f32(x)
     return f32(math.copysign(math.floor(builtins.abs(float(x)) + 0.5), float(x)))
@@ -331,17 +335,27 @@ def abs(x):  # noqa: A001
     return f32(np.abs(f32(x)))
 
 
-def min(a, b):  # noqa: A001
+def _ints(*xs):
+    return all(isinstance(x, (int, np.integer)) and not isinstance(x, bool) for x in xs)
+
+
+def min(a, b):  # noqa: A001 - integer arguments give an integer, as in Warp
+    if _ints(a, b):
+        return builtins.min(int(a), int(b))
     a, b = f32(a), f32(b)
     return a if a < b else b
 
 
 def max(a, b):  # noqa: A001
+    if _ints(a, b):
+        return builtins.max(int(a), int(b))
     a, b = f32(a), f32(b)
     return a if a > b else b
 
 
 def clamp(x, lo, hi):
+    if _ints(x, lo, hi):
+        return builtins.min(builtins.max(int(x), int(lo)), int(hi))
     x, lo, hi = f32(x), f32(lo), f32(hi)
     return lo if x < lo else (hi if x > hi else x)
 
