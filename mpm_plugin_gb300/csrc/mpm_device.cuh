@@ -377,7 +377,8 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     T e[3] = {safe_log_dev(sig[0], d[0]), safe_log_dev(sig[1], d[1]), safe_log_dev(sig[2], d[2])};
     T tr = e[0] + e[1] + e[2];
     const T size = fabs(e[0]) + fabs(e[1]) + fabs(e[2]);
-    if (marginal) *marginal = fabs(tr) <= T(kMarginalRel) * size;
+    // (strict comparisons: an undeformed particle, all e exactly 0, has no decision to make)
+    if (marginal) *marginal = fabs(tr) < T(kMarginalRel) * size;
     if (tr >= T(0)) {  // separation: stress-free, singular values back to 1
 #pragma unroll
         for (int i = 0; i < 3; ++i) delta[i] = -d[i];
@@ -387,7 +388,7 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     T dev[3] = {e[0] - third, e[1] - third, e[2] - third};
     T n = sqrt_t(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
     const T cone = (T(3) * lam + T(2) * mu) / (T(2) * mu) * tr * alpha;
-    if (marginal) *marginal = *marginal || n <= T(kMarginalRel) * size || fabs(n + cone) <= T(kMarginalRel) * (n - cone);
+    if (marginal) *marginal = *marginal || n < T(kMarginalRel) * size || fabs(n + cone) < T(kMarginalRel) * (n - cone);
     if (n < T(1.0e-10f)) return false;
     T dgamma = n + cone;
     if (dgamma <= T(0)) return false;
@@ -409,7 +410,7 @@ MPM_HD bool project_snow(const T sig[3], const T d[3], T clamp_lo, T clamp_hi, T
         T ns = min_t(max_t(sig[i], clamp_lo), clamp_hi);
         delta[i] = ns == sig[i] ? T(0) : (ns - T(1)) - d[i];
         any |= delta[i] != T(0);
-        near |= fabs(sig[i] - clamp_lo) <= T(kMarginalRel) * clamp_lo || fabs(sig[i] - clamp_hi) <= T(kMarginalRel) * clamp_hi;
+        near |= fabs(sig[i] - clamp_lo) < T(kMarginalRel) * clamp_lo || fabs(sig[i] - clamp_hi) < T(kMarginalRel) * clamp_hi;
         num *= sig[i];
         den *= ns;
     }
