@@ -124,7 +124,9 @@ enum {
     MPM_OPT_DETERMINISTIC = 4, /* 1: bit-reproducible runs. P2G and the occupancy splat sum in 64-bit fixed point
                                   (exact integer additions, independent of particle order and atomic timing);
                                   results agree with the default mode within float rounding. 0 (default) */
-    MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 80 registers, 3 CTAs of 256 per SM; 1 uncapped */
+    MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 80 registers, 3 CTAs of 256 per SM; 1 uncapped;
+                                  2 the tile build (TMA loads of particle planes and grid boxes). With
+                                  MPM_OPT_FP64_CLAMP on: 0 and 2 the FP64 build at 80 registers, 1 at 128 */
     MPM_OPT_LIST_CTAS = 6,     /* CTAs of the kernels that walk the active-block and candidate lists (default:
                                   8 per SM of the device, from cudaDevAttrMultiProcessorCount) */
     MPM_OPT_P2G_GROUP = 7,     /* P2G sums same-cell lanes within aligned groups of this many lanes before one
@@ -132,10 +134,11 @@ enum {
     MPM_OPT_PDL = 8,           /* 1 (default): the substep kernels use programmatic dependent launch, so each
                                   kernel's launch overlaps the tail of the one before; 0: plain stream order */
     MPM_OPT_FP64_CLAMP = 9,    /* FP64 in the Drucker-Prager and snow return mapping: 1 a particle whose FP32
-                                  decision is marginal (the cone or separation test, a snow bound within a
-                                  relative 2e-5, or nearly equal log singular values) is redone in FP64 (SVD,
-                                  projection, hardening, stress); 2 every particle whose clamp is active is;
-                                  0 (default): FP32, with the FP64 redo only for SVDs that did not converge */
+                                  decision is marginal where the outcome jumps (the Drucker-Prager separation
+                                  test: |tr log sigma| within a relative 1e-6 of the strain, the strain above
+                                  1e-6) is redone in FP64 (SVD, projection, hardening, stress); 2 every
+                                  particle whose clamp is active is; 0 (default): FP32, with the FP64 redo only
+                                  for SVDs that did not converge */
     MPM_OPT_P2G_TILE = 10,     /* 1: P2G sums each CTA's contributions in shared-memory tiles of the nodes its
                                   particles touch, then adds them to the grid; 0 (default): warp segments
                                   (shuffle sums of same-cell lanes) only. Deterministic mode uses segments */
@@ -156,7 +159,12 @@ enum {
                                   update; 0 (default): P2G lists a block itself the first time it touches it
                                   (an atomic exchange on the flag and an atomic add on the list's length).
                                   One grid only (two-grid mode, cooperative launches and batches list
-                                  blocks in P2G) */
+                                  blocks in P2G) */,
+    MPM_OPT_PARTICLES_PER_THREAD = 14 /* 1 (default), 2, 4 or 8: particles per thread of the plain solver's
+                                  P2G and G2P kernels. Their grid holds ceil(chunks / k) CTAs of 256 threads that
+                                  walk the 256-particle chunks grid-stride, so each thread takes about k
+                                  particles one after another. (Batches walk their scenes' chunks with at most
+                                  8 CTAs per SM whatever this is; the tile builds keep their own grids.) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

@@ -28,7 +28,7 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
     if (b.any_colliders) launch_step_kernel(k_grid_colliders<SceneTable>, list_ctas, 128, st, pdl, sc);
     if (b.particle_ctas > 0) {
         if (b.any_fp64_clamp)
-            launch_step_kernel(k_g2p<SceneTable, 1, true>, walk_ctas, 256, st, pdl, sc);
+            launch_step_kernel(k_g2p<SceneTable, 2, true>, walk_ctas, 256, st, pdl, sc);
         else if (b.shape.g2p_variant == 1)
             launch_step_kernel(k_g2p<SceneTable, 1>, walk_ctas, 256, st, pdl, sc);
         else

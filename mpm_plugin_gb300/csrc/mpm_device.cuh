@@ -151,6 +151,11 @@ MPM_HD void swap_cols(T M[3][3], int a, int b, bool negate) {
     }
 }
 
+// An off-diagonal of E = A^T A - I below this after two Jacobi sweeps moves the reconstructed U diag(sigma)
+// V^T by about half of it (sigma ~ 1), below an FP32 ulp of 1, and the QR factor's off-diagonals stay far
+// inside the 4e-6 convergence bound: the third sweep is skipped for such a lane.
+constexpr float kSweepSkip = 1.0e-8f;
+
 // ---------------------------------------------------------------------------------------------------------
 // SVD in deviation form, for the MPM regime F ~ I. The eigenvalues of E = A^T A - I, formed as
 // G + G^T + G^T G from G = A - I (exact in FP32 near I), give d = sigma - 1 to full relative accuracy,
@@ -159,7 +164,7 @@ MPM_HD void swap_cols(T M[3][3], int a, int b, bool negate) {
 // U: Givens QR of A V (proper rotation; the QR factor's last diagonal carries sign(det A)).
 // Returns the largest off-diagonal of the QR factor relative to sigma_0 (a convergence measure).
 // ---------------------------------------------------------------------------------------------------------
-template <typename T, int SWEEPS>
+template <typename T, int SWEEPS, bool kLastIfNeeded = false>
 MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) {
     T G[3][3], E[3][3];
 #pragma unroll
@@ -175,7 +180,14 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) 
             U[i][j] = i == j ? T(1) : T(0);
         }
 #pragma unroll
-    for (int sw = 0; sw < SWEEPS; ++sw) {
+    for (int sw = 0; sw < (kLastIfNeeded ? SWEEPS - 1 : SWEEPS); ++sw) {
+        jacobi_rotate(E, V, 0, 1);
+        jacobi_rotate(E, V, 0, 2);
+        jacobi_rotate(E, V, 1, 2);
+    }
+    // kLastIfNeeded: the last sweep only where an off-diagonal of E is still above kSweepSkip. The lane's own
+    // E decides, so a particle's result does not depend on its neighbours in the warp.
+    if (kLastIfNeeded && fmax(fmax(fabs(E[0][1]), fabs(E[0][2])), fabs(E[1][2])) > T(kSweepSkip)) {
         jacobi_rotate(E, V, 0, 1);
         jacobi_rotate(E, V, 0, 2);
         jacobi_rotate(E, V, 1, 2);
@@ -215,13 +227,14 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) 
     return scale > T(0) ? off / scale : T(0);
 }
 
-// FP32 deviation-form SVD, three cyclic Jacobi sweeps; lanes whose sweeps did not diagonalise E to 4e-6
-// (relative to sigma_0) are redone in FP64 and counted when a counter is given. Measured on the mixed
-// workload: three sweeps leave no lane to the FP64 path over thousands of substeps and make G2P 14 % faster
-// than four; two sweeps sent millions of lanes to FP64 within three frames.
+// FP32 deviation-form SVD, two cyclic Jacobi sweeps and a third where E is not yet diagonal to kSweepSkip;
+// lanes whose sweeps did not diagonalise E to 4e-6 (relative to sigma_0) are redone in FP64 and counted when
+// a counter is given. Measured on the mixed workload: three sweeps leave no lane to the FP64 path over
+// thousands of substeps and make G2P 14 % faster than four; two sweeps for every lane sent millions of lanes
+// to FP64 within three frames.
 MPM_HD void svd3(const float A[3][3], float U[3][3], float sig[3], float d[3], float V[3][3],
                  unsigned int* fp64_lanes) {
-    float off = svd3_dev_core<float, 3>(A, U, sig, d, V);
+    float off = svd3_dev_core<float, 3, true>(A, U, sig, d, V);
     if (!(off <= 4e-6f)) {  // also taken for NaN input, which then stays NaN
         double Ad[3][3], Ud[3][3], sd[3], dd[3], Vd[3][3];
 #pragma unroll
@@ -361,16 +374,25 @@ MPM_HD bool project_von_mises(const T sig[3], const T d[3], T mu, T yield_stress
     return true;
 }
 
-// Relative width of the band around a return-mapping decision inside which an FP32 evaluation may decide
-// differently from an exact one (about eight FP32 ulps of the terms compared; the log singular values and
-// their sums carry a few): the FP32 call reports such a marginal decision, and the G2P build with the FP64
-// option redoes those lanes in FP64. (A band of 2e-5 flagged 5 % of the lanes of a settled Drucker-Prager
-// pile, whose plastic flow keeps it on the cone, and through warp divergence doubled G2P's time.)
+// A return-mapping decision is marginal when an FP32 evaluation may take it differently from an exact one
+// AND the two outcomes differ by more than the FP32 rounding of the result; the FP32 call reports it, and
+// the G2P build with the FP64 option redoes those lanes in FP64.
+//
+// Only the Drucker-Prager separation test is such a decision: tr eps >= 0 sends the log singular values eps
+// to 0, just below it they stay or go towards the cone, a jump of at most |eps|_1 (the deviatoric part, n,
+// is no larger). It is marginal when |tr eps| lies within kMarginalRel of |eps|_1 (about eight FP32 ulps of
+// the terms summed; in the deviation form eps keeps full relative accuracy) and |eps|_1 exceeds
+// kMarginalFloor (eight FP32 ulps of 1: below it the jump is at the rounding of the stored F). The cone and
+// the snow clamps are continuous in the singular values, and so is the cone projection where n is tiny (the
+// projection then moves eps by at most n): a flipped decision there changes the result by rounding.
+// Measured on the 256^3 pile: flagging the cone and snow bounds, and then the separation test without the
+// floor (settled grains whose strains are a few ulps, where opposite ulps cancel in tr exactly), each marked
+// 5 % of the lanes, doubled G2P's time through warp divergence and moved the error against the FP64 oracle
+// by nothing.
 constexpr float kMarginalRel = 1.0e-6f;
+constexpr float kMarginalFloor = 1.0e-6f;
 
-// marginal (optional): set when the decision is within kMarginalRel of flipping (the sign of tr eps at the
-// separation test, the sign of dgamma at the cone) or the deviatoric direction is ill-conditioned (the three
-// log singular values nearly equal, n below kMarginalRel of their size).
+// marginal (optional): set when the separation decision is marginal (above).
 template <typename T>
 MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T alpha, T delta[3],
                                    bool* marginal = nullptr) {
@@ -378,7 +400,7 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     T tr = e[0] + e[1] + e[2];
     const T size = fabs(e[0]) + fabs(e[1]) + fabs(e[2]);
     // (strict comparisons: an undeformed particle, all e exactly 0, has no decision to make)
-    if (marginal) *marginal = fabs(tr) < T(kMarginalRel) * size;
+    if (marginal) *marginal = fabs(tr) < T(kMarginalRel) * size && size > T(kMarginalFloor);
     if (tr >= T(0)) {  // separation: stress-free, singular values back to 1
 #pragma unroll
         for (int i = 0; i < 3; ++i) delta[i] = -d[i];
@@ -388,7 +410,6 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     T dev[3] = {e[0] - third, e[1] - third, e[2] - third};
     T n = sqrt_t(dev[0] * dev[0] + dev[1] * dev[1] + dev[2] * dev[2]);
     const T cone = (T(3) * lam + T(2) * mu) / (T(2) * mu) * tr * alpha;
-    if (marginal) *marginal = *marginal || n < T(kMarginalRel) * size || fabs(n + cone) < T(kMarginalRel) * (n - cone);
     if (n < T(1.0e-10f)) return false;
     T dgamma = n + cone;
     if (dgamma <= T(0)) return false;
@@ -398,24 +419,22 @@ MPM_HD bool project_drucker_prager(const T sig[3], const T d[3], T mu, T lam, T 
     return true;
 }
 
-// marginal (optional): set when a singular value lies within kMarginalRel of a clamp bound (whether it is
-// clamped could change with its last bits).
+// marginal (optional): always false, the clamp being continuous (kept for the callers' symmetry).
 template <typename T>
 MPM_HD bool project_snow(const T sig[3], const T d[3], T clamp_lo, T clamp_hi, T delta[3], T* jp_ratio,
                          bool* marginal = nullptr) {
-    bool any = false, near = false;
+    bool any = false;
     T num = T(1), den = T(1);
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         T ns = min_t(max_t(sig[i], clamp_lo), clamp_hi);
         delta[i] = ns == sig[i] ? T(0) : (ns - T(1)) - d[i];
         any |= delta[i] != T(0);
-        near |= fabs(sig[i] - clamp_lo) < T(kMarginalRel) * clamp_lo || fabs(sig[i] - clamp_hi) < T(kMarginalRel) * clamp_hi;
         num *= sig[i];
         den *= ns;
     }
     *jp_ratio = num / den;
-    if (marginal) *marginal = near;
+    if (marginal) *marginal = false;
     return any;
 }
 

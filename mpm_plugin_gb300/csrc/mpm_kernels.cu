@@ -529,6 +529,11 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
         if (ev) cudaEventRecordWithFlags(ev[i], st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
     };
     const bool pdl = shape.pdl != 0;
+    // P2G and the plain G2P builds: one CTA per chunk of 256 particles, or (particles per thread above one)
+    // one per ppt chunks, walking them; the FP64 and two-grid G2P builds always take one chunk per CTA
+    const unsigned int chunks = blocks_for(a.n, 256);
+    const bool walk = shape.ppt > 1;
+    const unsigned int wctas = walk ? blocks_for(chunks, shape.ppt) : chunks;
     mark(0);
     launch_step_kernel(k_step_begin<OneScene>, 1, 1, st, pdl, sc);
     launch_step_kernel(k_clear_blocks<OneScene>, list_ctas, 256, st, pdl, sc);
@@ -537,7 +542,7 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
         if (shape.p2g_tile && !a.fixed)
             launch_step_kernel_smem(k_p2g_tile<OneScene>, blocks_for(a.n, 256), 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(k_p2g_scatter<OneScene>, blocks_for(a.n, 256), 256, st, pdl, sc);
+            launch_step_kernel(walk ? k_p2g_scatter<OneScene, true> : k_p2g_scatter<OneScene>, wctas, 256, st, pdl, sc);
         if (a.block_sweep) {
             const int64_t nblk = (int64_t)a.g.nb[0] * a.g.nb[1] * a.g.nb[2];
             launch_step_kernel(k_list_blocks<OneScene>,
@@ -551,17 +556,21 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
     mark(3);
     if (a.n > 0) {
         if (a.grid2 && shape.g2p_variant == 1)  // two-grid mode (never with the FP64 clamp build)
-            launch_step_kernel(k_g2p<OneScene, 1, false, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
+            launch_step_kernel(k_g2p<OneScene, 1, false, true>, chunks, 256, st, pdl, sc);
         else if (a.grid2)
-            launch_step_kernel(k_g2p<OneScene, 3, false, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
-        else if (a.fp64_clamp)
-            launch_step_kernel(k_g2p<OneScene, 1, true>, blocks_for(a.n, 256), 256, st, pdl, sc);
+            launch_step_kernel(k_g2p<OneScene, 3, false, true>, chunks, 256, st, pdl, sc);
+        else if (a.fp64_clamp && shape.g2p_variant == 1)  // the FP64 build at 128 registers
+            launch_step_kernel(k_g2p<OneScene, 2, true>, chunks, 256, st, pdl, sc);
+        else if (a.fp64_clamp)  // the FP64 build at 80 registers (the redo's working set spills)
+            launch_step_kernel(k_g2p<OneScene, 3, true>, chunks, 256, st, pdl, sc);
         else if (shape.g2p_variant == 1)
-            launch_step_kernel(k_g2p<OneScene, 1>, blocks_for(a.n, 256), 256, st, pdl, sc);
+            launch_step_kernel(walk ? k_g2p<OneScene, 1, false, false, true> : k_g2p<OneScene, 1>, wctas, 256, st, pdl,
+                               sc);
         else if (shape.g2p_variant == 2 && g2p_tile_launch(st, a, pdl, sc))
             ;  // the tile G2P (its maps could not be made otherwise: then the plain build below)
         else
-            launch_step_kernel(k_g2p<OneScene, 3>, blocks_for(a.n, 256), 256, st, pdl, sc);
+            launch_step_kernel(walk ? k_g2p<OneScene, 3, false, false, true> : k_g2p<OneScene, 3>, wctas, 256, st, pdl,
+                               sc);
     }
     if (a.cd.n_col > 0) launch_step_kernel(k_project_particles<OneScene>, list_ctas, 128, st, pdl, sc);
     mark(4);

@@ -323,14 +323,22 @@ __device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
 
 // A batch's particle kernels walk the flattened (scene, chunk) list of the scenes that run this substep
 // (scene_offsets over the chunk counts), grid-stride, so a scene that has finished its substeps for the
-// frame costs no CTAs. One scene: one CTA per chunk.
-template <class Scenes>
+// frame costs no CTAs. One scene: one CTA per chunk, or with kWalk (the particles-per-thread launch choice)
+// fewer CTAs that walk the chunks grid-stride. The walk is its own build: its loop costs the single-chunk
+// kernels registers (G2P's spills grew from 152 to 252 bytes with it).
+template <class Scenes, bool kWalk = false>
 __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         if (a.sp->p2g_skip) return;
-        p2g_cta(a, (int64_t)blockIdx.x * blockDim.x);
+        if constexpr (kWalk) {
+            const unsigned int chunks = particle_chunks(a);
+#pragma unroll 1
+            for (unsigned int q = blockIdx.x; q < chunks; q += gridDim.x) p2g_cta(a, (int64_t)q * blockDim.x);
+        } else {
+            p2g_cta(a, (int64_t)blockIdx.x * blockDim.x);
+        }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
@@ -615,11 +623,18 @@ __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
     }
 }
 
-template <class Scenes, int kMinCtas, bool kFp64Clamp = false, bool kScatter = false>
+template <class Scenes, int kMinCtas, bool kFp64Clamp = false, bool kScatter = false, bool kWalk = false>
 __global__ void __launch_bounds__(256, kMinCtas) k_g2p(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
-        g2p_cta<kFp64Clamp, GlobalSource, kScatter>(sc.get(0), (int64_t)blockIdx.x * blockDim.x);
+        if constexpr (kWalk) {  // the chunks grid-stride, as in k_p2g_scatter
+            const unsigned int chunks = particle_chunks(sc.a);
+#pragma unroll 1
+            for (unsigned int q = blockIdx.x; q < chunks; q += gridDim.x)
+                g2p_cta<kFp64Clamp, GlobalSource, kScatter>(sc.get(0), (int64_t)q * blockDim.x);
+        } else {
+            g2p_cta<kFp64Clamp, GlobalSource, kScatter>(sc.get(0), (int64_t)blockIdx.x * blockDim.x);
+        }
     } else {  // (scene, chunk) list of the running scenes, as in k_p2g_scatter
         __shared__ unsigned int off[kMaxBatchScenes + 1];
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) { return particle_chunks(a); }, off);

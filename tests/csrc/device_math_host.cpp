@@ -257,6 +257,24 @@ void host_collider_matrix(const float* start16, const float* end16, double dx, f
         for (int c = 0; c < 4; ++c) M12[r * 4 + c] = pose.M[r][c];
 }
 
+// The FP32 return-mapping projections of n singular-value triples (sig = 1 + d): model 2 Drucker-Prager with
+// p = (mu, lam, alpha), model 3 snow with p = (clamp_lo, clamp_hi); out delta (n, 3), whether the projection
+// changed the triple and whether the call reported its decision as marginal (n each)
+void host_project(int model, int n, const float* sig, const float* d, const float* p, float* delta, int* changed,
+                  int* marginal) {
+    for (int k = 0; k < n; ++k) {
+        bool m = true, c;
+        if (model == 2) {
+            c = project_drucker_prager(&sig[3 * k], &d[3 * k], p[0], p[1], p[2], &delta[3 * k], &m);
+        } else {
+            float jp;
+            c = project_snow(&sig[3 * k], &d[3 * k], p[0], p[1], &delta[3 * k], &jp, &m);
+        }
+        changed[k] = c;
+        marginal[k] = m;
+    }
+}
+
 void emu_read_grid(void* ev, float* out) {
     Emu* e = static_cast<Emu*>(ev);
     const GridDesc& g = e->g;

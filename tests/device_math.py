@@ -55,6 +55,7 @@ def lib():
     L.emu_collider_sdf.argtypes = [P, C.c_int, C.c_float, C.c_int, C.c_int, P, P]
     L.host_decompose.argtypes = [P, P, P, P]
     L.host_collider_matrix.argtypes = [P, P, C.c_double, C.c_float, P]
+    L.host_project.argtypes = [C.c_int, C.c_int, P, P, P, P, P, P]
     _lib = L
     return L
 
@@ -94,6 +95,19 @@ def collider_matrix(start, end, s, dx=1.0):
     out = np.zeros(12, np.float32)
     lib().host_collider_matrix(_p(a), _p(b), dx, s, _p(out))
     return out.reshape(3, 4)
+
+
+def project(model, d, params):
+    """The FP32 return-mapping projection of singular-value deviations d (n, 3), sig = 1 + d: model 2
+    Drucker-Prager with params (mu, lam, alpha), 3 snow with (clamp_lo, clamp_hi). Returns (delta, changed,
+    marginal)."""
+    d = np.ascontiguousarray(np.asarray(d, np.float32).reshape(-1, 3))
+    sig = np.ascontiguousarray(np.float32(1) + d)
+    p = np.ascontiguousarray(np.asarray(params, np.float32))
+    n = len(d)
+    delta, changed, marginal = np.zeros((n, 3), np.float32), np.zeros(n, np.int32), np.zeros(n, np.int32)
+    lib().host_project(model, n, _p(sig), _p(d), _p(p), _p(delta), _p(changed), _p(marginal))
+    return delta, changed.astype(bool), marginal.astype(bool)
 
 
 class HostMesh:

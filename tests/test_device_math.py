@@ -206,3 +206,33 @@ def test_collider_pose_matches_reference_interpolation():
             M = collider_matrix(a, b, s)
             scale = np.abs(ref[:3]).max()
             np.testing.assert_allclose(M, ref[:3], rtol=0, atol=1e-6 * scale, err_msg=f"pair {i} s {s}")
+
+
+def test_return_mapping_marginal_decisions():
+    """The FP32 projections report as marginal only the decisions whose two outcomes differ by more than
+    rounding: the Drucker-Prager separation test near tr eps = 0 with a strain above the floor. The cone, the
+    snow clamps and nearly equal log singular values are continuous and never marginal; an undeformed particle
+    has no decision to make, nor one whose strains are a few ulps that cancel in tr."""
+    from device_math import project
+
+    mu, lam, alpha = 4.0e5, 6.0e5, 0.3
+    e_tr0 = -2.0 * np.log1p(1e-3) - 1e-9  # tr eps about -1e-9 against |eps| of 4e-3
+    d = np.array([[0.0, 0.0, 0.0],  # undeformed
+                  [1e-3, 1e-3, np.expm1(e_tr0)],  # at the separation test
+                  [-0.05, 0.02, 0.01],  # compressed and sheared: projected onto the cone
+                  [-0.05 * (1 + 1e-7), -0.05, -0.05 * (1 - 1e-7)],  # hydrostatic: no deviatoric direction
+                  [0.01, 0.02, 0.005],  # stretched: separation
+                  [2 ** -23, -(2 ** -23), 0.0]])  # strains of an ulp, cancelling in tr
+    delta, changed, marginal = project(2, d, (mu, lam, alpha))
+    assert marginal.tolist() == [False, True, False, False, False, False]
+    assert changed[2] and changed[4] and not changed[3]
+    np.testing.assert_array_equal(delta[4], -np.float32(d[4]))
+    # the cone projection continuous in d: a rounding-sized change of d moves delta by about as much
+    d2 = d[2:3] * np.float32(1 + 2 ** -22)
+    np.testing.assert_allclose(project(2, d2, (mu, lam, alpha))[0], delta[2:3], rtol=0, atol=1e-7)
+
+    lo, hi = 1 - 0.025, 1 + 0.0045
+    ds = np.array([[0.0, 0.0, 0.0], [0.0045, 0.0, 0.0], [-0.025, 0.001, 0.0], [0.01, -0.03, 0.002]])
+    delta, changed, marginal = project(3, ds, (lo, hi))
+    assert not marginal.any()
+    assert changed.tolist() == [False, False, False, True]

@@ -1,6 +1,6 @@
 """Launch variants that must not change the physics (GPU): the TMA tile G2P (MPM_OPT_G2P_VARIANT 2) against
-the plain G2P build and the oracle, and P2G's block flags listed by a sweep (MPM_OPT_BLOCK_SWEEP) against P2G
-listing the blocks itself.
+the plain G2P build and the oracle, P2G's block flags listed by a sweep (MPM_OPT_BLOCK_SWEEP) against P2G
+listing the blocks itself, and several particles per thread (MPM_OPT_PARTICLES_PER_THREAD) against one.
 
 Both builds run the same per-particle arithmetic in the same order; only where the inputs come from differs
 (shared-memory tiles filled by cp.async.bulk.tensor, or global memory). In deterministic mode (P2G sums in
@@ -22,7 +22,7 @@ from mpm_plugin_gb300 import _abi
 pytestmark = pytest.mark.gpu
 
 
-def _mix(variant, sort_interval, res=128, deterministic=True, block_sweep=0):
+def _mix(variant, sort_interval, res=128, deterministic=True, block_sweep=0, ppt=1):
     from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
 
@@ -36,6 +36,7 @@ def _mix(variant, sort_interval, res=128, deterministic=True, block_sweep=0):
     s.set_option(_abi.OPT_SORT_INTERVAL, sort_interval)
     s.set_option(_abi.OPT_G2P_VARIANT, variant)
     s.set_option(_abi.OPT_BLOCK_SWEEP, block_sweep)
+    s.set_option(_abi.OPT_PARTICLES_PER_THREAD, ppt)
     return s, d
 
 
@@ -129,3 +130,34 @@ def test_block_sweep_is_bit_identical_to_listing_in_p2g(variant, sort_interval):
     np.testing.assert_array_equal(ga, gb)
     for k in ("x", "v", "C", "F", "Jp"):
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+@pytest.mark.parametrize("ppt,fused", [(2, 0), (4, 0), (8, 0), (4, 1)])
+def test_particles_per_thread_do_not_change_the_state(ppt, fused):
+    """Deterministic mode: P2G and G2P with CTAs that take several chunks each give the state of one CTA per
+    chunk, bit for bit, over graph-replayed substeps, explicit substeps and an advance; in the default mode
+    (float atomics, any order) and in two-grid mode, within 1e-5 after one substep."""
+    out = []
+    for k in (1, ppt):
+        s, _ = _mix(0, 4, ppt=k)
+        s.run_substeps(5e-5, 12)
+        for _ in range(3):
+            s.substep(5e-5, 1.0, 1 / 24)
+        st = s.advance(1 / 24)
+        out.append((s.save_state(), (st.substeps, st.dt, st.removed)))
+        s.close()
+    (a, sa), (b, sb) = out
+    assert sa == sb
+    for k in ("x", "v", "C", "F", "Jp"):
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    out = []
+    for k in (1, ppt):
+        s, d = _mix(0, 0, deterministic=False, ppt=k)
+        s.set_option(_abi.OPT_FUSED_P2G, fused)
+        s.run_substeps(5e-5, 3)
+        out.append(s.save_state())
+        s.close()
+    # C against the velocity-gradient scale (|v| / dx): near rest it is the rounding of sums in any order
+    gnorm = float(np.linalg.norm(out[0]["v"])) / d.dx
+    for k in ("x", "v", "C", "F", "Jp"):
+        assert rel_err(out[1][k], out[0][k], floor=gnorm if k == "C" else 0.0) <= 1e-5, k
