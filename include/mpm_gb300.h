@@ -214,7 +214,9 @@ int mpm_conservation(void *handle, double *out);
 /* Device memory the handle holds now, in bytes (no counterpart in the reference; serving admission). */
 int mpm_device_bytes(void *handle, int64_t *bytes);
 
-/* Number of SVD lanes that took the FP64 path since the handle was created. */
+/* Number of SVD lanes whose FP32 Jacobi sweeps (up to eight) did not diagonalise F^T F - I to 4e-6 since
+   the handle was created: redone in FP64 by the G2P build of MPM_OPT_FP64_CLAMP and by the stress of
+   particles that enter; the other G2P builds keep the FP32 result. */
 int mpm_fp64_lanes(void *handle, int64_t *lanes);
 /* Number of Drucker-Prager / snow lanes whose return mapping G2P redid in FP64 under MPM_OPT_FP64_CLAMP since the
  * handle was created (no counterpart in the reference; it reports how far FP64 is confined). */

@@ -153,8 +153,10 @@ MPM_HD void swap_cols(T M[3][3], int a, int b, bool negate) {
 
 // An off-diagonal of E = A^T A - I below this after two Jacobi sweeps moves the reconstructed U diag(sigma)
 // V^T by about half of it (sigma ~ 1), below an FP32 ulp of 1, and the QR factor's off-diagonals stay far
-// inside the 4e-6 convergence bound: the third sweep is skipped for such a lane.
+// inside the 4e-6 convergence bound: no further sweep runs for such a lane.
 constexpr float kSweepSkip = 1.0e-8f;
+// Sweeps after the first two, at most, for a lane whose E is not yet diagonal to kSweepSkip.
+constexpr int kMaxExtraSweeps = 6;
 
 // ---------------------------------------------------------------------------------------------------------
 // SVD in deviation form, for the MPM regime F ~ I. The eigenvalues of E = A^T A - I, formed as
@@ -163,8 +165,11 @@ constexpr float kSweepSkip = 1.0e-8f;
 // come from the QR diagonal instead, where sqrt(1 + e) would cancel). V: Jacobi eigenvectors of E;
 // U: Givens QR of A V (proper rotation; the QR factor's last diagonal carries sign(det A)).
 // Returns the largest off-diagonal of the QR factor relative to sigma_0 (a convergence measure).
+// kAdaptive: two sweeps, then further sweeps (one copy of the code, a loop) while an off-diagonal of E is
+// above kSweepSkip, at most kMaxExtraSweeps; SWEEPS is then unused. The lane's own E decides, so a
+// particle's result does not depend on its neighbours in the warp.
 // ---------------------------------------------------------------------------------------------------------
-template <typename T, int SWEEPS, bool kLastIfNeeded = false>
+template <typename T, int SWEEPS, bool kAdaptive = false>
 MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) {
     T G[3][3], E[3][3];
 #pragma unroll
@@ -180,17 +185,19 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) 
             U[i][j] = i == j ? T(1) : T(0);
         }
 #pragma unroll
-    for (int sw = 0; sw < (kLastIfNeeded ? SWEEPS - 1 : SWEEPS); ++sw) {
+    for (int sw = 0; sw < (kAdaptive ? 2 : SWEEPS); ++sw) {
         jacobi_rotate(E, V, 0, 1);
         jacobi_rotate(E, V, 0, 2);
         jacobi_rotate(E, V, 1, 2);
     }
-    // kLastIfNeeded: the last sweep only where an off-diagonal of E is still above kSweepSkip. The lane's own
-    // E decides, so a particle's result does not depend on its neighbours in the warp.
-    if (kLastIfNeeded && fmax(fmax(fabs(E[0][1]), fabs(E[0][2])), fabs(E[1][2])) > T(kSweepSkip)) {
-        jacobi_rotate(E, V, 0, 1);
-        jacobi_rotate(E, V, 0, 2);
-        jacobi_rotate(E, V, 1, 2);
+    if constexpr (kAdaptive) {
+#pragma unroll 1
+        for (int sw = 0; sw < kMaxExtraSweeps && fmax(fmax(fabs(E[0][1]), fabs(E[0][2])), fabs(E[1][2])) > T(kSweepSkip);
+             ++sw) {
+            jacobi_rotate(E, V, 0, 1);
+            jacobi_rotate(E, V, 0, 2);
+            jacobi_rotate(E, V, 1, 2);
+        }
     }
     T e0 = E[0][0], e1 = E[1][1], e2 = E[2][2];
     // descending eigenvalues; a swap negates one column so det(V) stays +1
@@ -227,14 +234,27 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) 
     return scale > T(0) ? off / scale : T(0);
 }
 
-// FP32 deviation-form SVD, two cyclic Jacobi sweeps and a third where E is not yet diagonal to kSweepSkip;
-// lanes whose sweeps did not diagonalise E to 4e-6 (relative to sigma_0) are redone in FP64 and counted when
-// a counter is given. Measured on the mixed workload: three sweeps leave no lane to the FP64 path over
-// thousands of substeps and make G2P 14 % faster than four; two sweeps for every lane sent millions of lanes
-// to FP64 within three frames.
+// FP32 deviation-form SVD: two cyclic Jacobi sweeps, then more (up to eight in all) while E is not diagonal
+// to kSweepSkip. kFp64: lanes whose sweeps did not diagonalise E to 4e-6 (relative to sigma_0) are redone in
+// FP64; either way they are counted when a counter is given. The default G2P builds take kFp64 = false: the
+// FP64 code in line with the FP32 path made the compiler spill the FP32 path's registers (152 against 32
+// bytes of spill stores at 80 registers; G2P 35.3 against 31.2 us on the mixed workload, measured) although
+// no lane took it there. Measured on the mixed workload with a fixed sweep count: three sweeps left no lane
+// unconverged over thousands of substeps, two sweeps for every lane left millions within three frames.
+template <bool kFp64 = true>
 MPM_HD void svd3(const float A[3][3], float U[3][3], float sig[3], float d[3], float V[3][3],
                  unsigned int* fp64_lanes) {
     float off = svd3_dev_core<float, 3, true>(A, U, sig, d, V);
+    if (!kFp64) {
+        if (!(off <= 4e-6f) && fp64_lanes) {  // NaN input stays NaN
+#ifdef __CUDA_ARCH__
+            atomicAdd(fp64_lanes, 1u);
+#else
+            *fp64_lanes += 1u;
+#endif
+        }
+        return;
+    }
     if (!(off <= 4e-6f)) {  // also taken for NaN input, which then stays NaN
         double Ad[3][3], Ud[3][3], sd[3], dd[3], Vd[3][3];
 #pragma unroll

@@ -663,7 +663,7 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const In& in, const
     // P2G would get from decomposing the stored F again.
     const Material m = mats[in.mat()];
     float U[3][3], sig[3], d[3], V[3][3];
-    svd3(Fn, U, sig, d, V, fp64);
+    svd3<kFp64Clamp>(Fn, U, sig, d, V, fp64);  // the FP64 SVD fallback only in the FP64-clamp build
     const float jp_old = in.Jp();
     float jp = jp_old;
     bool redo = false;  // FP64 redo of a marginal Drucker-Prager or snow decision (or of every active clamp)

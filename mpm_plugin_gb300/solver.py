@@ -331,6 +331,7 @@ class Gb300Solver(Solver):
         return n.value
 
     def fp64_lanes(self) -> int:
+        """SVD lanes whose FP32 sweeps did not converge (mpm_fp64_lanes)."""
         v = C.c_int64()
         self._check(self._lib.mpm_fp64_lanes(self._h, C.byref(v)))
         return v.value

@@ -117,3 +117,12 @@ def test_joint_overrides_are_tried_from_the_best_of_the_descent():
                                   joint=({"a": 2, "b": 4},))
     assert best == {"a": 2, "b": 4} and t == 0.5  # one knob at a time stops at (1, 0)
     assert len(trials) == 5
+
+
+def test_joint_overrides_need_the_larger_gain():
+    """A joint override within JOINT_MIN_GAIN of the descent's best is not taken (its window is noisier than
+    the gain)."""
+    times = {(0, 0): 1.0, (1, 0): 0.9, (2, 4): 0.9 * (1.0 - tune.JOINT_MIN_GAIN / 2)}
+    best, t, _ = tune.search(lambda cfg: times.get((cfg["a"], cfg["b"]), 2.0), {"a": (0, 1), "b": (0,)},
+                             {"a": 0, "b": 0}, ("a", "b"), joint=({"a": 2, "b": 4},))
+    assert best == {"a": 1, "b": 0} and t == 0.9
