@@ -1247,6 +1247,7 @@ struct Batch {
     unsigned int particle_ctas = 0;
     bool any_colliders = false;
     bool any_fp64_clamp = false;
+    bool any_fixed = false;  // some scene in deterministic mode (the P2G build with the fixed-point path)
     std::vector<int64_t> layout;             // what the captured graphs depend on
     cudaGraphExec_t graph = nullptr;         // one batched substep
     cudaGraphExec_t graph_many = nullptr;    // kGraphReps batched substeps
@@ -1291,7 +1292,7 @@ Status batch_upload(Batch* b) {
     std::vector<SubstepArgs> table(n);
     std::vector<int64_t> layout{n};
     int64_t ctas = 0;
-    bool cols = false, clamp = false;
+    bool cols = false, clamp = false, fixed = false;
     for (int s = 0; s < n; ++s) {
         Handle* h = b->live[s];
         TRY(prepare_grids(h, false, false));  // a batch runs its scenes in one-grid mode
@@ -1303,9 +1304,11 @@ Status batch_upload(Batch* b) {
         ctas += (h->P.cap + 255) / 256;
         cols = cols || h->n_col > 0;
         clamp = clamp || h->fp64_clamp;
+        fixed = fixed || table[s].fixed != nullptr;
     }
     layout.push_back(cols ? 1 : 0);
     layout.push_back(clamp ? 1 : 0);
+    layout.push_back(fixed ? 1 : 0);
     if (layout != b->layout) {
         CK(cudaStreamSynchronize(b->stream));
         batch_invalidate(b);
@@ -1327,6 +1330,7 @@ Status batch_upload(Batch* b) {
         b->particle_ctas = (unsigned int)ctas;
         b->any_colliders = cols;
         b->any_fp64_clamp = clamp;
+        b->any_fixed = fixed;
         b->layout = layout;
     }
     // a pageable source is staged by the driver before the call returns, so `table` may go out of scope
@@ -1337,7 +1341,7 @@ Status batch_upload(Batch* b) {
 // reps (1 or kGraphReps) batched substeps in one graph launch.
 Status batch_replay(Batch* b, int reps = 1) {
     BatchLaunch bl{b->d_table, b->d_cta, b->d_cta + b->particle_ctas, (int)b->live.size(), b->particle_ctas,
-                   b->any_colliders, b->any_fp64_clamp, b->shape};
+                   b->any_colliders, b->any_fp64_clamp, b->any_fixed, b->shape};
     cudaGraphExec_t& g = reps == 1 ? b->graph : b->graph_many;
     if (!g) {
         cudaGraph_t graph;

@@ -87,6 +87,7 @@ struct BatchLaunch {
     unsigned int particle_ctas;
     bool any_colliders;
     bool any_fp64_clamp;  // some scene redoes the plastic clamp in FP64 (the G2P build with the redo)
+    bool any_fixed;       // some scene is in deterministic mode (the P2G build with the fixed-point path)
     LaunchShape shape;
 };
 void launch_batch_substep(cudaStream_t st, const BatchLaunch& b);

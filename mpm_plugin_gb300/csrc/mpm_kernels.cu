@@ -542,7 +542,9 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
         if (shape.p2g_tile && !a.fixed)
             launch_step_kernel_smem(k_p2g_tile<OneScene>, blocks_for(a.n, 256), 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(walk ? k_p2g_scatter<OneScene, true> : k_p2g_scatter<OneScene>, wctas, 256, st, pdl, sc);
+            launch_step_kernel(a.fixed ? (walk ? k_p2g_scatter<OneScene, true> : k_p2g_scatter<OneScene>)
+                                       : (walk ? k_p2g_scatter<OneScene, true, false> : k_p2g_scatter<OneScene, false, false>),
+                               wctas, 256, st, pdl, sc);
         if (a.block_sweep) {
             const int64_t nblk = (int64_t)a.g.nb[0] * a.g.nb[1] * a.g.nb[2];
             launch_step_kernel(k_list_blocks<OneScene>,

@@ -264,6 +264,9 @@ __device__ __forceinline__ void p2g_segment_sums(float4* grid, const P2gTerms& t
 // rounds for more reductions (the autotuner picks the group). Lanes past the end or with a stencil outside
 // the grid are single-lane segments that add nothing. The segment's first lane lists the blocks it touches.
 // grid / parity: the grid and the active list scattered into. All 32 lanes of the warp take part.
+// kMaybeFixed = false: a build for scenes outside deterministic mode, without the fixed-point path (in line,
+// though not taken, it cost the float path registers: 328 against 112 bytes of spill loads).
+template <bool kMaybeFixed = true>
 __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* grid, unsigned int parity,
                                                   const P2gTerms& t, bool valid) {
     const int lane = (int)(threadIdx.x & 31u);
@@ -284,9 +287,11 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
         else
             mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, parity), &a.wl.counts[parity]);
     }
-    if (a.fixed) {
-        p2g_fixed_warp(a, t, valid, leader, tail, span);
-        return;
+    if constexpr (kMaybeFixed) {
+        if (a.fixed) {
+            p2g_fixed_warp(a, t, valid, leader, tail, span);
+            return;
+        }
     }
     const StencilIndex at = stencil_index(g, t.base);
     // shuffle rounds needed by the longest segment of the warp: 0, 1, 2, 3 or 5 (4 takes 5)
@@ -304,6 +309,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
 }
 
 // P2G of the 256 particles from `first` (one CTA's share; the warps past the end return).
+template <bool kMaybeFixed = true>
 __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     const int64_t p = first + threadIdx.x;
     if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end
@@ -311,7 +317,7 @@ __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     P2gTerms t;
     const bool valid = p < a.n && p2g_terms(P, p, a.mats, a.g, a.sp->dt, t);
     const unsigned int cur = a.sp->seq & 1u;
-    p2g_warp_segments(a, grid_of(a, cur), cur, t, valid);
+    p2g_warp_segments<kMaybeFixed>(a, grid_of(a, cur), cur, t, valid);
 }
 
 // Five CTAs of 256 per SM (48 registers, a few spilled values): the warps it adds hide more of P2G's memory
@@ -325,8 +331,9 @@ __device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
 // (scene_offsets over the chunk counts), grid-stride, so a scene that has finished its substeps for the
 // frame costs no CTAs. One scene: one CTA per chunk, or with kWalk (the particles-per-thread launch choice)
 // fewer CTAs that walk the chunks grid-stride. The walk is its own build: its loop costs the single-chunk
-// kernels registers (G2P's spills grew from 152 to 252 bytes with it).
-template <class Scenes, bool kWalk = false>
+// kernels registers (G2P's spills grew from 152 to 252 bytes with it). kMaybeFixed = false: the build for a
+// scene outside deterministic mode (a batch keeps the check per scene).
+template <class Scenes, bool kWalk = false, bool kMaybeFixed = true>
 __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
@@ -335,9 +342,10 @@ __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
         if constexpr (kWalk) {
             const unsigned int chunks = particle_chunks(a);
 #pragma unroll 1
-            for (unsigned int q = blockIdx.x; q < chunks; q += gridDim.x) p2g_cta(a, (int64_t)q * blockDim.x);
+            for (unsigned int q = blockIdx.x; q < chunks; q += gridDim.x)
+                p2g_cta<kMaybeFixed>(a, (int64_t)q * blockDim.x);
         } else {
-            p2g_cta(a, (int64_t)blockIdx.x * blockDim.x);
+            p2g_cta<kMaybeFixed>(a, (int64_t)blockIdx.x * blockDim.x);
         }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
@@ -520,10 +528,16 @@ __global__ void __launch_bounds__(256) k_grid_update(Scenes sc) {
 }
 
 // Contact work lists run in one of two shapes, chosen per launch from the list's length (identical
-// results): up to kWarpItemsPerWarp items per warp of the launch, one warp per item, whose lanes share the
-// item's mesh queries (32 candidate triangles at a time), so a few slow queries do not hold up the kernel;
-// beyond that, one thread per item, for throughput when contact is widespread.
-constexpr unsigned int kWarpItemsPerWarp = 4;
+// results): up to warp_shape_items() items, one warp per item, whose lanes share the item's mesh queries
+// (32 candidate triangles at a time), so a few slow queries do not hold up the kernel; beyond that, one
+// thread per item, for throughput when contact is widespread. The bound is 128 items per SM of the device,
+// not a share of the launch: tied to the launch, a tuned 16 work-list CTAs per SM kept the 256^3 pour's
+// widespread contact in the warp shape (grid slot 0.15 -> 0.37 ms per substep, measured).
+__device__ __forceinline__ unsigned int warp_shape_items() {
+    unsigned int sms;
+    asm("mov.u32 %0, %%nsmid;" : "=r"(sms));
+    return 128u * sms;
+}
 
 // Mesh-collider contact of one listed node.
 template <bool kWarp>
@@ -549,7 +563,7 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[2];
-        if (n <= warps * kWarpItemsPerWarp) {
+        if (n <= warp_shape_items()) {
             for (unsigned int i = warp; i < n; i += warps) grid_collider_node<true>(a, i);
         } else {
             for (unsigned int i = tid; i < n; i += threads) grid_collider_node<false>(a, i);
@@ -559,7 +573,7 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
             return a.cd.n_col > 0 ? a.wl.counts[2] : 0u;
         }, off);
-        if (total <= warps * kWarpItemsPerWarp) {
+        if (total <= warp_shape_items()) {
             for (unsigned int q = warp; q < total; q += warps) {
                 const int s = scene_of_item(off, sc.count(), q);
                 grid_collider_node<true>(sc.get(s), q - off[s]);
@@ -618,7 +632,7 @@ __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
             P2gTerms t;
             const bool valid = live && !listed && p2g_terms_of(ScatterFields{P, p, tau}, a.mats, a.g, a.sp->dt, t);
             const unsigned int next = cur ^ 1u;
-            p2g_warp_segments(a, grid_of(a, next), next, t, valid);
+            p2g_warp_segments<false>(a, grid_of(a, next), next, t, valid);  // two grids: never fixed point
         }
     }
 }
@@ -671,7 +685,7 @@ __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[3];
-        if (n <= warps * kWarpItemsPerWarp) {
+        if (n <= warp_shape_items()) {
             for (unsigned int i = warp; i < n; i += warps) project_candidate<true>(a, i);
         } else {
             for (unsigned int i = tid; i < n; i += threads) project_candidate<false>(a, i);
@@ -681,7 +695,7 @@ __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
         const unsigned int total = scene_offsets(sc, [](const SubstepArgs& a) {
             return a.cd.n_col > 0 ? a.wl.counts[3] : 0u;
         }, off);
-        if (total <= warps * kWarpItemsPerWarp) {
+        if (total <= warp_shape_items()) {
             for (unsigned int q = warp; q < total; q += warps) {
                 const int s = scene_of_item(off, sc.count(), q);
                 project_candidate<true>(sc.get(s), q - off[s]);
@@ -759,7 +773,7 @@ __global__ void __launch_bounds__(256, kMinCtas) k_substeps_coop(OneScene sc, in
         if (!grid_barrier(bar, err)) return;
         if (a.cd.n_col > 0) {
             const unsigned int n = a.wl.counts[2];
-            if (n <= warps * kWarpItemsPerWarp) {
+            if (n <= warp_shape_items()) {
                 for (unsigned int i = warp; i < n; i += warps) grid_collider_node<true>(a, i);
             } else {
                 for (unsigned int i = tid; i < n; i += threads) grid_collider_node<false>(a, i);
@@ -770,7 +784,7 @@ __global__ void __launch_bounds__(256, kMinCtas) k_substeps_coop(OneScene sc, in
         if (!grid_barrier(bar, err)) return;
         if (a.cd.n_col > 0) {
             const unsigned int n = a.wl.counts[3];
-            if (n <= warps * kWarpItemsPerWarp) {
+            if (n <= warp_shape_items()) {
                 for (unsigned int i = warp; i < n; i += warps) project_candidate<true>(a, i);
             } else {
                 for (unsigned int i = tid; i < n; i += threads) project_candidate<false>(a, i);
