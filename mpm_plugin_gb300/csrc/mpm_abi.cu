@@ -1698,7 +1698,7 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
         case MPM_OPT_DETERMINISTIC:
             return finish(h, set_deterministic(h, value != 0));
         case MPM_OPT_G2P_VARIANT:
-            if (value < 0 || value > 2) return finish(h, {MPM_ERR_VALUE, "G2P variant must be 0, 1 or 2"});
+            if (value < 0 || value > 3) return finish(h, {MPM_ERR_VALUE, "G2P variant must be 0, 1, 2 or 3"});
             h->shape.g2p_variant = (int)value;
             return MPM_OK;
         case MPM_OPT_LIST_CTAS:

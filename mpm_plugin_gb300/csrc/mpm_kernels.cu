@@ -520,6 +520,14 @@ static bool g2p_tile_launch(cudaStream_t st, const SubstepArgs& a, bool pdl, con
     return true;
 }
 
+// The P2G build for a scene: chunk walk or not, with the fixed-point path (deterministic mode) or not, blocks
+// flagged for the sweep or listed.
+static void (*p2g_build(bool walk, bool fixed, bool sweep))(OneScene) {
+    if (fixed) return walk ? k_p2g_scatter<OneScene, true, true, 2> : k_p2g_scatter<OneScene, false, true, 2>;
+    if (sweep) return walk ? k_p2g_scatter<OneScene, true, false, 1> : k_p2g_scatter<OneScene, false, false, 1>;
+    return walk ? k_p2g_scatter<OneScene, true, false, 0> : k_p2g_scatter<OneScene, false, false, 0>;
+}
+
 void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& shape, cudaEvent_t* ev, bool capturing) {
     const unsigned int list_ctas = shape.list_ctas ? shape.list_ctas : sm_count() * kCtasPerSm;
     const OneScene sc{a};
@@ -542,9 +550,7 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
         if (shape.p2g_tile && !a.fixed)
             launch_step_kernel_smem(k_p2g_tile<OneScene>, blocks_for(a.n, 256), 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(a.fixed ? (walk ? k_p2g_scatter<OneScene, true> : k_p2g_scatter<OneScene>)
-                                       : (walk ? k_p2g_scatter<OneScene, true, false> : k_p2g_scatter<OneScene, false, false>),
-                               wctas, 256, st, pdl, sc);
+            launch_step_kernel(p2g_build(walk, a.fixed != nullptr, a.block_sweep != 0), wctas, 256, st, pdl, sc);
         if (a.block_sweep) {
             const int64_t nblk = (int64_t)a.g.nb[0] * a.g.nb[1] * a.g.nb[2];
             launch_step_kernel(k_list_blocks<OneScene>,
@@ -570,6 +576,8 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
                                sc);
         else if (shape.g2p_variant == 2 && g2p_tile_launch(st, a, pdl, sc))
             ;  // the tile G2P (its maps could not be made otherwise: then the plain build below)
+        else if (shape.g2p_variant == 3)  // 64 registers, 4 CTAs of 256 per SM
+            launch_step_kernel(k_g2p<OneScene, 4>, chunks, 256, st, pdl, sc);
         else
             launch_step_kernel(walk ? k_g2p<OneScene, 3, false, false, true> : k_g2p<OneScene, 3>, wctas, 256, st, pdl,
                                sc);

@@ -265,8 +265,10 @@ __device__ __forceinline__ void p2g_segment_sums(float4* grid, const P2gTerms& t
 // the grid are single-lane segments that add nothing. The segment's first lane lists the blocks it touches.
 // grid / parity: the grid and the active list scattered into. All 32 lanes of the warp take part.
 // kMaybeFixed = false: a build for scenes outside deterministic mode, without the fixed-point path (in line,
-// though not taken, it cost the float path registers: 328 against 112 bytes of spill loads).
-template <bool kMaybeFixed = true>
+// though not taken, it cost the float path registers: 328 against 112 bytes of spill loads). kSweep: 0 the
+// leaders list the blocks (no block-sweep code), 1 they only flag them (a.block_sweep set), 2 either, by
+// a.block_sweep (the block-sweep branch in line cost another 112 -> 36 bytes of spill loads).
+template <bool kMaybeFixed = true, int kSweep = 2>
 __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* grid, unsigned int parity,
                                                   const P2gTerms& t, bool valid) {
     const int lane = (int)(threadIdx.x & 31u);
@@ -282,7 +284,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
     const int span = (int)__reduce_max_sync(0xffffffffu, (unsigned int)tail);
     const bool leader = valid && seg_first;
     if (leader) {
-        if (a.block_sweep)
+        if (kSweep == 1 || (kSweep == 2 && a.block_sweep))
             flag_stencil_blocks(g, t.base, a.wl.block_flag);
         else
             mark_stencil_blocks(g, t.base, a.wl.block_flag, active_blocks(a.wl, parity), &a.wl.counts[parity]);
@@ -309,7 +311,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
 }
 
 // P2G of the 256 particles from `first` (one CTA's share; the warps past the end return).
-template <bool kMaybeFixed = true>
+template <bool kMaybeFixed = true, int kSweep = 2>
 __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     const int64_t p = first + threadIdx.x;
     if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end
@@ -317,7 +319,7 @@ __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     P2gTerms t;
     const bool valid = p < a.n && p2g_terms(P, p, a.mats, a.g, a.sp->dt, t);
     const unsigned int cur = a.sp->seq & 1u;
-    p2g_warp_segments<kMaybeFixed>(a, grid_of(a, cur), cur, t, valid);
+    p2g_warp_segments<kMaybeFixed, kSweep>(a, grid_of(a, cur), cur, t, valid);
 }
 
 // Five CTAs of 256 per SM (48 registers, a few spilled values): the warps it adds hide more of P2G's memory
@@ -332,8 +334,8 @@ __device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
 // frame costs no CTAs. One scene: one CTA per chunk, or with kWalk (the particles-per-thread launch choice)
 // fewer CTAs that walk the chunks grid-stride. The walk is its own build: its loop costs the single-chunk
 // kernels registers (G2P's spills grew from 152 to 252 bytes with it). kMaybeFixed = false: the build for a
-// scene outside deterministic mode (a batch keeps the check per scene).
-template <class Scenes, bool kWalk = false, bool kMaybeFixed = true>
+// scene outside deterministic mode (a batch keeps the check per scene); kSweep as in p2g_warp_segments.
+template <class Scenes, bool kWalk = false, bool kMaybeFixed = true, int kSweep = 2>
 __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
@@ -343,9 +345,9 @@ __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
             const unsigned int chunks = particle_chunks(a);
 #pragma unroll 1
             for (unsigned int q = blockIdx.x; q < chunks; q += gridDim.x)
-                p2g_cta<kMaybeFixed>(a, (int64_t)q * blockDim.x);
+                p2g_cta<kMaybeFixed, kSweep>(a, (int64_t)q * blockDim.x);
         } else {
-            p2g_cta<kMaybeFixed>(a, (int64_t)blockIdx.x * blockDim.x);
+            p2g_cta<kMaybeFixed, kSweep>(a, (int64_t)blockIdx.x * blockDim.x);
         }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];
@@ -632,7 +634,7 @@ __device__ __forceinline__ void g2p_cta(const SubstepArgs& a, int64_t first) {
             P2gTerms t;
             const bool valid = live && !listed && p2g_terms_of(ScatterFields{P, p, tau}, a.mats, a.g, a.sp->dt, t);
             const unsigned int next = cur ^ 1u;
-            p2g_warp_segments<false>(a, grid_of(a, next), next, t, valid);  // two grids: never fixed point
+            p2g_warp_segments<false, 0>(a, grid_of(a, next), next, t, valid);  // two grids: no fixed point, no sweep
         }
     }
 }

@@ -51,7 +51,7 @@ JOINT_MIN_GAIN = 0.05
 # the tuned one-grid choice. (Searched first, on the 256^3 pour it beat the untuned defaults, the descent
 # then never reached the reorder that makes one grid faster, and a frame took 1.3x as long: measured.)
 SOLVER_DEFAULTS = {**DEFAULTS, "block_sweep": 0, "ppt": 1, "fused_p2g": 0}
-SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2), "block_sweep": (0, 1), "ppt": (1, 2, 4),
+SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2, 3), "block_sweep": (0, 1), "ppt": (1, 2, 4),
                      "fused_p2g": (0, 1)}
 SOLVER_ORDER = KNOB_ORDER + ("block_sweep", "ppt", "fused_p2g")
 # The tile G2P (g2p_variant 2) stages a chunk's grid boxes in shared memory, which pays when the particles are

@@ -40,10 +40,12 @@ def _mix(variant, sort_interval, res=128, deterministic=True, block_sweep=0, ppt
     return s, d
 
 
-@pytest.mark.parametrize("sort_interval", [1, 4, 0])
-def test_tile_g2p_is_bit_identical_to_the_plain_build(sort_interval):
+@pytest.mark.parametrize("variant,sort_interval", [(2, 1), (2, 4), (2, 0), (1, 4), (3, 0)])
+def test_tile_g2p_is_bit_identical_to_the_plain_build(variant, sort_interval):
+    """The tile build (2), and the uncapped (1) and 64-register (3) plain builds, against the 80-register
+    plain build."""
     out = []
-    for variant in (0, 2):
+    for variant in (0, variant):
         s, _ = _mix(variant, sort_interval)
         s.run_substeps(5e-5, 12)
         for _ in range(3):
