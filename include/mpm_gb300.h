@@ -124,9 +124,9 @@ enum {
     MPM_OPT_DETERMINISTIC = 4, /* 1: bit-reproducible runs. P2G and the occupancy splat sum in 64-bit fixed point
                                   (exact integer additions, independent of particle order and atomic timing);
                                   results agree with the default mode within float rounding. 0 (default) */
-    MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 80 registers, 3 CTAs of 256 per SM; 1 uncapped;
+    MPM_OPT_G2P_VARIANT = 5,   /* G2P build: 0 (default) capped at 64 registers, 4 CTAs of 256 per SM; 1 uncapped;
                                   2 the tile build (TMA loads of particle planes and grid boxes); 3 capped at
-                                  64 registers, 4 CTAs per SM. With MPM_OPT_FP64_CLAMP on: 0, 2 and 3 the
+                                  80 registers, 3 CTAs per SM. With MPM_OPT_FP64_CLAMP on: 0, 2 and 3 the
                                   FP64 build at 80 registers, 1 at 128 */
     MPM_OPT_LIST_CTAS = 6,     /* CTAs of the kernels that walk the active-block and candidate lists (default:
                                   8 per SM of the device, from cudaDevAttrMultiProcessorCount) */

@@ -576,11 +576,11 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
                                sc);
         else if (shape.g2p_variant == 2 && g2p_tile_launch(st, a, pdl, sc))
             ;  // the tile G2P (its maps could not be made otherwise: then the plain build below)
-        else if (shape.g2p_variant == 3)  // 64 registers, 4 CTAs of 256 per SM
-            launch_step_kernel(k_g2p<OneScene, 4>, chunks, 256, st, pdl, sc);
-        else
+        else if (shape.g2p_variant == 3 || walk)  // 80 registers, 3 CTAs of 256 per SM (the walk: this cap)
             launch_step_kernel(walk ? k_g2p<OneScene, 3, false, false, true> : k_g2p<OneScene, 3>, wctas, 256, st, pdl,
                                sc);
+        else  // 64 registers, 4 CTAs of 256 per SM
+            launch_step_kernel(k_g2p<OneScene, 4>, chunks, 256, st, pdl, sc);
     }
     if (a.cd.n_col > 0) launch_step_kernel(k_project_particles<OneScene>, list_ctas, 128, st, pdl, sc);
     mark(4);

@@ -589,11 +589,12 @@ __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
     }
 }
 
-// G2P; particles that end inside a collider's margin box are listed for k_project_particles. kMinCtas = 3
-// caps it at 80 registers (3 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra
-// resident warps outweighed the few spilled values on the mixed workload (10 % faster than kMinCtas = 1).
-// Caps of 128 and 64 registers were slower on the mixed and the 256^3 workloads (measured on a GB300). Both
-// builds are kept; the autotuner picks one per workload. kFp64Clamp: the build with the FP64 redo at the
+// G2P; particles that end inside a collider's margin box are listed for k_project_particles. kMinCtas = 4
+// caps it at 64 registers (4 CTAs of 256 per SM): the kernel is bound by instruction latency, and the extra
+// resident warps outweigh the spilled values (112 bytes) on the mixed workload (substep 1.2 % faster than at
+// 80 registers, 3 CTAs; kernel 5 % faster under ncu; measured on a GB300). While the FP64 SVD fallback was
+// in line, 80 registers was the best cap (10 % faster than kMinCtas = 1; 64 and 128 slower). The 80- and
+// uncapped builds are kept; the autotuner picks one per workload. kFp64Clamp: the build with the FP64 redo at the
 // Drucker-Prager and snow clamp (MPM_OPT_FP64_CLAMP), launched only when a scene has the option set.
 // kScatter: the two-grid build. Where the substep scatters (StepParams::scatter), each warp then adds its
 // particles to the next substep's grid, as k_p2g_scatter would at the start of that substep, from the

@@ -42,8 +42,8 @@ def _mix(variant, sort_interval, res=128, deterministic=True, block_sweep=0, ppt
 
 @pytest.mark.parametrize("variant,sort_interval", [(2, 1), (2, 4), (2, 0), (1, 4), (3, 0)])
 def test_tile_g2p_is_bit_identical_to_the_plain_build(variant, sort_interval):
-    """The tile build (2), and the uncapped (1) and 64-register (3) plain builds, against the 80-register
-    plain build."""
+    """The tile build (2), and the uncapped (1) and 80-register (3) plain builds, against the default
+    64-register plain build."""
     out = []
     for variant in (0, variant):
         s, _ = _mix(variant, sort_interval)
