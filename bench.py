@@ -853,6 +853,8 @@ def run_profile_case(args) -> None:
     s.set_option(_abi.OPT_G2P_VARIANT, args.g2p_variant)
     s.set_option(_abi.OPT_SORT_INTERVAL, args.sort_interval)
     s.set_option(_abi.OPT_BLOCK_SWEEP, args.block_sweep)
+    s.set_option(_abi.OPT_P2G_TILE, args.p2g_tile)
+    s.set_option(_abi.OPT_P2G_GROUP, args.p2g_group)
     s.set_option(_abi.OPT_FP64_CLAMP, args.fp64_clamp)
     for k in range(args.profile_substeps):
         s.substep(dt, (k + 1) / args.profile_substeps, 1 / 96)
@@ -886,6 +888,8 @@ def main():
     ap.add_argument("--g2p-variant", type=int, default=0)
     ap.add_argument("--sort-interval", type=int, default=0)
     ap.add_argument("--block-sweep", type=int, default=0)
+    ap.add_argument("--p2g-tile", type=int, default=0)
+    ap.add_argument("--p2g-group", type=int, default=32)
     ap.add_argument("--fp64-clamp", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:
