@@ -17,7 +17,7 @@ MPM_OK, MPM_ERR_VALUE, MPM_ERR_NOT_IMPLEMENTED, MPM_ERR_CUDA, MPM_ERR_ARGUMENT, 
 MODEL_IDS = {"elastic": 0, "von_mises": 1, "drucker_prager": 2, "snow": 3}
 (OPT_USE_GRAPH, OPT_KERNEL_TIMING, OPT_SORT_INTERVAL, OPT_DETERMINISTIC, OPT_G2P_VARIANT, OPT_LIST_CTAS,
  OPT_P2G_GROUP, OPT_PDL, OPT_FP64_CLAMP, OPT_P2G_TILE, OPT_COOP, OPT_FUSED_P2G, OPT_BLOCK_SWEEP,
- OPT_PARTICLES_PER_THREAD) = range(1, 15)
+ OPT_PARTICLES_PER_THREAD, OPT_P2G_MERGE) = range(1, 16)
 KERNEL_SLOTS = ("p2g", "grid_update", "g2p", "other")
 
 # every symbol declared in include/mpm_gb300.h

@@ -532,9 +532,10 @@ Status run_substep(Handle* h, int reps = 1) {
     int64_t key[GraphCache::kKey] = {h->P.n, h->P.cap, h->n_col, (int64_t)(intptr_t)h->arena,
                                      (int64_t)(intptr_t)h->d_poses, (int64_t)(intptr_t)h->wl.part_cand,
                                      (int64_t)h->shape.list_ctas,
-                                     ((((((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
+                                     (((((((((int64_t)h->shape.g2p_variant * 64 + h->shape.p2g_group) * 2 + h->shape.pdl) *
                                                 2 + (h->fp64_clamp ? 1 : 0)) * 2 + h->shape.p2g_tile) * 2 +
-                                              (a.grid2 ? 1 : 0)) * 2 + a.block_sweep) * 16 + h->shape.ppt) * 64 + reps};
+                                              (a.grid2 ? 1 : 0)) * 2 + a.block_sweep) * 16 + h->shape.ppt) * 2 +
+                                            h->shape.p2g_merge) * 64 + reps};
     if (!h->use_graph) {
         if (h->timing) {
             std::vector<cudaEvent_t> ev(5);
@@ -1713,6 +1714,9 @@ int mpm_set_option(void* handle, int32_t option, int64_t value) {
             return MPM_OK;
         case MPM_OPT_BLOCK_SWEEP:
             h->shape.block_sweep = value != 0;
+            return MPM_OK;
+        case MPM_OPT_P2G_MERGE:
+            h->shape.p2g_merge = value != 0;
             return MPM_OK;
         case MPM_OPT_PARTICLES_PER_THREAD:
             if (value != 1 && value != 2 && value != 4 && value != 8)

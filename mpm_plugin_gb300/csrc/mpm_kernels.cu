@@ -521,10 +521,12 @@ static bool g2p_tile_launch(cudaStream_t st, const SubstepArgs& a, bool pdl, con
 }
 
 // The P2G build for a scene: chunk walk or not, with the fixed-point path (deterministic mode) or not, blocks
-// flagged for the sweep or listed.
-static void (*p2g_build(bool walk, bool fixed, bool sweep))(OneScene) {
+// flagged for the sweep or listed, leader sums merged along z or not.
+static void (*p2g_build(bool walk, bool fixed, bool sweep, bool merge))(OneScene) {
     if (fixed) return walk ? k_p2g_scatter<OneScene, true, true, 2> : k_p2g_scatter<OneScene, false, true, 2>;
     if (sweep) return walk ? k_p2g_scatter<OneScene, true, false, 1> : k_p2g_scatter<OneScene, false, false, 1>;
+    if (merge)
+        return walk ? k_p2g_scatter<OneScene, true, false, 0, true> : k_p2g_scatter<OneScene, false, false, 0, true>;
     return walk ? k_p2g_scatter<OneScene, true, false, 0> : k_p2g_scatter<OneScene, false, false, 0>;
 }
 
@@ -550,7 +552,8 @@ void launch_substep(cudaStream_t st, const SubstepArgs& a, const LaunchShape& sh
         if (shape.p2g_tile && !a.fixed)
             launch_step_kernel_smem(k_p2g_tile<OneScene>, blocks_for(a.n, 256), 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(p2g_build(walk, a.fixed != nullptr, a.block_sweep != 0), wctas, 256, st, pdl, sc);
+            launch_step_kernel(p2g_build(walk, a.fixed != nullptr, a.block_sweep != 0, shape.p2g_merge != 0), wctas, 256,
+                               st, pdl, sc);
         if (a.block_sweep) {
             const int64_t nblk = (int64_t)a.g.nb[0] * a.g.nb[1] * a.g.nb[2];
             launch_step_kernel(k_list_blocks<OneScene>,

@@ -256,6 +256,63 @@ __device__ __forceinline__ void p2g_segment_sums(float4* grid, const P2gTerms& t
             }
 }
 
+// Where a segment's leader adds its sums when the warp's segments are merged along z (p2g_column_sums):
+// src1 / src2 the lanes of the previous two leaders, d1 the z distance to the previous leader when it shares
+// the leader's x and y base (1 or 2, else 0), ok2 whether the one before that sits at z distance 2 (with
+// d1 = 1), ws the z distance to the next leader when it shares x and y (1 or 2, else 0).
+struct ColumnMerge {
+    int src1, src2, d1, ws;
+    bool ok2;
+};
+
+// The segment sums of p2g_segment_sums, then merged along z between the leaders of one x-y column: stencils
+// whose bases differ by one or two nodes in z share nodes, and each shared node is added to the grid once,
+// by the leader with the larger base, which takes the earlier leaders' sums for it by shuffles (three
+// values per (i, j) node column instead of one reduction per node and leader). In the particle orders used
+// here (the sampler's z-ascending columns, the reorder's z-fastest node order) runs of consecutive
+// particles climb in z, so most of a warp's leaders chain this way. A leader writes node (i, j, k) unless
+// the next leader's base is within k (that leader covers it); it adds the previous leader's sum for
+// (i, j, k + d1) and, when the one before sits at distance 2, its sum for (i, j, 2) to node k = 0.
+template <int kRounds>
+__device__ __forceinline__ void p2g_column_sums(float4* grid, const P2gTerms& t, bool valid, bool leader, int tail,
+                                                const StencilIndex& at, const ColumnMerge& m) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float v[3][4];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) v[k][c] = 0.f;
+                if (valid) p2g_node(t, i, j, k, v[k]);
+#pragma unroll
+                for (int r = 0; r < kRounds; ++r) {
+                    const int d = 1 << r;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float o = __shfl_down_sync(0xffffffffu, v[k][c], d);
+                        if (d <= tail) v[k][c] += o;
+                    }
+                }
+            }
+            float o0[4], o1[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const float a1 = __shfl_sync(0xffffffffu, v[1][c], m.src1);  // previous leader, k = 1
+                const float a2 = __shfl_sync(0xffffffffu, v[2][c], m.src1);  // previous leader, k = 2
+                const float b2 = __shfl_sync(0xffffffffu, v[2][c], m.src2);  // the one before, k = 2
+                o0[c] = v[0][c] + (m.d1 == 1 ? a1 : (m.d1 == 2 ? a2 : 0.f)) + (m.ok2 ? b2 : 0.f);
+                o1[c] = v[1][c] + (m.d1 == 1 ? a2 : 0.f);
+            }
+            if (leader) {
+                grid_add(&grid[at(i, j, 0)], o0[0], o0[1], o0[2], o0[3]);
+                if (m.ws != 1) grid_add(&grid[at(i, j, 1)], o1[0], o1[1], o1[2], o1[3]);
+                if (m.ws == 0) grid_add(&grid[at(i, j, 2)], v[2][0], v[2][1], v[2][2], v[2][3]);
+            }
+        }
+}
+
 // P2G with warp-level aggregation: lanes whose stencils start at the same grid node (neighbours in the
 // particle order after the reorder by grid node) form a segment; each of the 27 x 4 contributions is summed
 // over the segment with shuffles (after round r a lane holds the sum of the next 2^r lanes of its segment)
@@ -267,8 +324,9 @@ __device__ __forceinline__ void p2g_segment_sums(float4* grid, const P2gTerms& t
 // kMaybeFixed = false: a build for scenes outside deterministic mode, without the fixed-point path (in line,
 // though not taken, it cost the float path registers: 328 against 112 bytes of spill loads). kSweep: 0 the
 // leaders list the blocks (no block-sweep code), 1 they only flag them (a.block_sweep set), 2 either, by
-// a.block_sweep (the block-sweep branch in line cost another 112 -> 36 bytes of spill loads).
-template <bool kMaybeFixed = true, int kSweep = 2>
+// a.block_sweep (the block-sweep branch in line cost another 112 -> 36 bytes of spill loads). kMerge: the
+// float sums merged along z between leaders (p2g_column_sums).
+template <bool kMaybeFixed = true, int kSweep = 2, bool kMerge = false>
 __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* grid, unsigned int parity,
                                                   const P2gTerms& t, bool valid) {
     const int lane = (int)(threadIdx.x & 31u);
@@ -298,6 +356,38 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
     const StencilIndex at = stencil_index(g, t.base);
     // shuffle rounds needed by the longest segment of the warp: 0, 1, 2, 3 or 5 (4 takes 5)
     const int rounds = span == 0 ? 0 : 32 - __clz(span);
+    if constexpr (kMerge) {
+        // the previous two leaders and the next one; a lane with none names itself (and merges nothing)
+        const unsigned int leaders = __ballot_sync(0xffffffffu, leader);
+        const unsigned int below = leaders & ((1u << lane) - 1u);
+        const int p1 = below ? 31 - __clz(below) : lane;
+        const unsigned int below2 = below & ((1u << p1) - 1u);
+        const int p2 = below2 ? 31 - __clz(below2) : lane;
+        const unsigned int above = lane == 31 ? 0u : leaders & ~((2u << lane) - 1u);
+        const int s1 = above ? __ffs(above) - 1 : lane;
+        const int xy = valid ? t.base[0] * 65536 + t.base[1] : -1 - lane;  // x, y base (grid dims < 65536)
+        const int z = t.base[2];
+        const int xy1 = __shfl_sync(0xffffffffu, xy, p1), z1 = __shfl_sync(0xffffffffu, z, p1);
+        const int xy2 = __shfl_sync(0xffffffffu, xy, p2), z2 = __shfl_sync(0xffffffffu, z, p2);
+        const int xys = __shfl_sync(0xffffffffu, xy, s1), zs = __shfl_sync(0xffffffffu, z, s1);
+        ColumnMerge m;
+        m.src1 = p1;
+        m.src2 = p2;
+        m.d1 = (p1 != lane && xy1 == xy && (z - z1 == 1 || z - z1 == 2)) ? z - z1 : 0;
+        m.ok2 = m.d1 == 1 && p2 != p1 && xy2 == xy && z - z2 == 2;
+        m.ws = (s1 != lane && xys == xy && (zs - z == 1 || zs - z == 2)) ? zs - z : 0;
+        if (rounds == 0)
+            p2g_column_sums<0>(grid, t, valid, leader, tail, at, m);
+        else if (rounds == 1)
+            p2g_column_sums<1>(grid, t, valid, leader, tail, at, m);
+        else if (rounds == 2)
+            p2g_column_sums<2>(grid, t, valid, leader, tail, at, m);
+        else if (rounds == 3)
+            p2g_column_sums<3>(grid, t, valid, leader, tail, at, m);
+        else
+            p2g_column_sums<5>(grid, t, valid, leader, tail, at, m);
+        return;
+    }
     if (rounds == 0)
         p2g_segment_sums<0>(grid, t, valid, leader, tail, at);
     else if (rounds == 1)
@@ -311,7 +401,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
 }
 
 // P2G of the 256 particles from `first` (one CTA's share; the warps past the end return).
-template <bool kMaybeFixed = true, int kSweep = 2>
+template <bool kMaybeFixed = true, int kSweep = 2, bool kMerge = false>
 __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     const int64_t p = first + threadIdx.x;
     if (first + (threadIdx.x & ~31u) >= a.n) return;  // whole warp past the end
@@ -319,7 +409,7 @@ __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     P2gTerms t;
     const bool valid = p < a.n && p2g_terms(P, p, a.mats, a.g, a.sp->dt, t);
     const unsigned int cur = a.sp->seq & 1u;
-    p2g_warp_segments<kMaybeFixed, kSweep>(a, grid_of(a, cur), cur, t, valid);
+    p2g_warp_segments<kMaybeFixed, kSweep, kMerge>(a, grid_of(a, cur), cur, t, valid);
 }
 
 // Five CTAs of 256 per SM (48 registers, a few spilled values): the warps it adds hide more of P2G's memory
@@ -334,8 +424,9 @@ __device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
 // frame costs no CTAs. One scene: one CTA per chunk, or with kWalk (the particles-per-thread launch choice)
 // fewer CTAs that walk the chunks grid-stride. The walk is its own build: its loop costs the single-chunk
 // kernels registers (G2P's spills grew from 152 to 252 bytes with it). kMaybeFixed = false: the build for a
-// scene outside deterministic mode (a batch keeps the check per scene); kSweep as in p2g_warp_segments.
-template <class Scenes, bool kWalk = false, bool kMaybeFixed = true, int kSweep = 2>
+// scene outside deterministic mode (a batch keeps the check per scene); kSweep, kMerge as in
+// p2g_warp_segments.
+template <class Scenes, bool kWalk = false, bool kMaybeFixed = true, int kSweep = 2, bool kMerge = false>
 __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
@@ -345,9 +436,9 @@ __global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
             const unsigned int chunks = particle_chunks(a);
 #pragma unroll 1
             for (unsigned int q = blockIdx.x; q < chunks; q += gridDim.x)
-                p2g_cta<kMaybeFixed, kSweep>(a, (int64_t)q * blockDim.x);
+                p2g_cta<kMaybeFixed, kSweep, kMerge>(a, (int64_t)q * blockDim.x);
         } else {
-            p2g_cta<kMaybeFixed, kSweep>(a, (int64_t)blockIdx.x * blockDim.x);
+            p2g_cta<kMaybeFixed, kSweep, kMerge>(a, (int64_t)blockIdx.x * blockDim.x);
         }
     } else {
         __shared__ unsigned int off[kMaxBatchScenes + 1];

@@ -163,3 +163,28 @@ def test_particles_per_thread_do_not_change_the_state(ppt, fused):
     gnorm = float(np.linalg.norm(out[0]["v"])) / d.dx
     for k in ("x", "v", "C", "F", "Jp"):
         assert rel_err(out[1][k], out[0][k], floor=gnorm if k == "C" else 0.0) <= 1e-5, k
+
+
+@pytest.mark.parametrize("sort_interval", [0, 4])
+def test_p2g_merge_along_z_matches_one_reduction_per_leader(sort_interval):
+    """P2G with the leaders' sums merged along z (MPM_OPT_P2G_MERGE 1) against one reduction per node and
+    leader (0): the grid after a substep (each node's mass, and the total against the particles' mass: no
+    contribution lost or added twice) and the particle state after three agree within float summation order
+    (1e-5), in the sampler's order and after reorders."""
+    out = []
+    for merge in (0, 1):
+        s, d = _mix(0, sort_interval, deterministic=False)
+        s.set_option(_abi.OPT_P2G_MERGE, merge)
+        mass = s.conservation()["mass"]
+        s.substep(5e-5, 1.0, 1 / 24)
+        grid = s.read_grid()
+        assert abs(grid[..., 3].astype(np.float64).sum() - mass) <= 1e-5 * mass
+        s.run_substeps(5e-5, 2)
+        out.append((grid, s.save_state()))
+        s.close()
+    (g0, a), (g1, b) = out
+    assert rel_err(g1[..., 3], g0[..., 3]) <= 1e-5
+    assert rel_err(g1, g0) <= 1e-5
+    gnorm = float(np.linalg.norm(a["v"])) / d.dx
+    for k in ("x", "v", "C", "F", "Jp"):
+        assert rel_err(b[k], a[k], floor=gnorm if k == "C" else 0.0) <= 1e-5, k
