@@ -350,7 +350,7 @@ def run_large(device: str, frames: int, fp64_mode: int = 0, tuned_cfg: dict | No
     s.set_colliders([ColliderGeometry(MeshData(tv, tt), True, 0.4)])
     s.set_collider_transforms(pose(0.0)[None], pose(0.0)[None])
     if tuned_cfg is None:
-        tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=40)
+        tuned = tune.tune_solver(s, 8e-5, 1 / 96, substeps=100)
     else:  # the FP64 run keeps the FP32 run's launch choices
         tune.apply(s, tuned_cfg, tune.gpu_key(device)[1], solver=True)
         tuned = {**tuned_cfg, "cached": True}

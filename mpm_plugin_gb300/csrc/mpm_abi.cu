@@ -25,7 +25,7 @@ using namespace mpm;
 namespace {
 
 constexpr double kCFL = 0.4;  // warp/solver.py:19
-constexpr int kFields = kParticleFields;    // x3 v3 C9 F9 Jp tau6 mat emitter id
+constexpr int kFields = kParticleFields;    // x3 v3 C9 F9 Jp tau6 mat emitter id Vq4
 
 thread_local std::string g_last_error;
 
@@ -211,20 +211,7 @@ struct DeviceGuard {
 // ---- particles -------------------------------------------------------------------------------------
 
 Particles bind_arena(void* base, int64_t cap, int64_t n) {
-    Particles P{};
-    float* f = static_cast<float*>(base);
-    for (int a = 0; a < 3; ++a) P.x[a] = f + (int64_t)a * cap;
-    for (int a = 0; a < 3; ++a) P.v[a] = f + (int64_t)(3 + a) * cap;
-    for (int e = 0; e < 9; ++e) P.C[e] = f + (int64_t)(6 + e) * cap;
-    for (int e = 0; e < 9; ++e) P.F[e] = f + (int64_t)(15 + e) * cap;
-    P.Jp = f + (int64_t)24 * cap;
-    for (int e = 0; e < 6; ++e) P.tau[e] = f + (int64_t)(25 + e) * cap;
-    P.mat = reinterpret_cast<int32_t*>(f + (int64_t)31 * cap);
-    P.emitter = reinterpret_cast<int32_t*>(f + (int64_t)32 * cap);
-    P.id = reinterpret_cast<int32_t*>(f + (int64_t)33 * cap);
-    P.n = n;
-    P.cap = cap;
-    return P;
+    return make_particles(static_cast<float*>(base), cap, n);
 }
 
 void invalidate_graph(Handle* h) {

@@ -169,8 +169,10 @@ constexpr int kMaxExtraSweeps = 6;
 // above kSweepSkip, at most kMaxExtraSweeps; SWEEPS is then unused. The lane's own E decides, so a
 // particle's result does not depend on its neighbours in the warp.
 // ---------------------------------------------------------------------------------------------------------
-template <typename T, int SWEEPS, bool kAdaptive = false>
-MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) {
+// kWarm: the sweeps start from the basis V0 (a rotation: the previous substep's V), on V0^T E V0, which is
+// nearly diagonal when the particle deformed little since; one sweep is then mandatory instead of two.
+template <typename T, int SWEEPS, bool kAdaptive = false, bool kWarm = false>
+MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3], const T (*V0)[3] = nullptr) {
     T G[3][3], E[3][3];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
@@ -184,8 +186,26 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) 
             V[i][j] = i == j ? T(1) : T(0);
             U[i][j] = i == j ? T(1) : T(0);
         }
+    if constexpr (kWarm) {  // E <- V0^T E V0 (symmetric), V <- V0
+        T W[3][3];
 #pragma unroll
-    for (int sw = 0; sw < (kAdaptive ? 2 : SWEEPS); ++sw) {
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) W[i][j] = E[i][0] * V0[0][j] + E[i][1] * V0[1][j] + E[i][2] * V0[2][j];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                E[i][j] = V0[0][i] * W[0][j] + V0[1][i] * W[1][j] + V0[2][i] * W[2][j];
+                E[j][i] = E[i][j];
+            }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) V[i][j] = V0[i][j];
+    }
+#pragma unroll
+    for (int sw = 0; sw < (kAdaptive ? (kWarm ? 1 : 2) : SWEEPS); ++sw) {
         jacobi_rotate(E, V, 0, 1);
         jacobi_rotate(E, V, 0, 2);
         jacobi_rotate(E, V, 1, 2);
@@ -234,17 +254,19 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3]) 
     return scale > T(0) ? off / scale : T(0);
 }
 
-// FP32 deviation-form SVD: two cyclic Jacobi sweeps, then more (up to eight in all) while E is not diagonal
-// to kSweepSkip. kFp64: lanes whose sweeps did not diagonalise E to 4e-6 (relative to sigma_0) are redone in
-// FP64; either way they are counted when a counter is given. The default G2P builds take kFp64 = false: the
+// FP32 deviation-form SVD: two cyclic Jacobi sweeps (one when started from V0, the previous basis), then
+// more (up to eight in all) while E is not diagonal to kSweepSkip. kFp64: lanes whose sweeps did not
+// diagonalise E to 4e-6 (relative to sigma_0) are redone in FP64 (from scratch); either way they are counted
+// when a counter is given. The default G2P builds take kFp64 = false: the
 // FP64 code in line with the FP32 path made the compiler spill the FP32 path's registers (152 against 32
 // bytes of spill stores at 80 registers; G2P 35.3 against 31.2 us on the mixed workload, measured) although
 // no lane took it there. Measured on the mixed workload with a fixed sweep count: three sweeps left no lane
 // unconverged over thousands of substeps, two sweeps for every lane left millions within three frames.
 template <bool kFp64 = true>
 MPM_HD void svd3(const float A[3][3], float U[3][3], float sig[3], float d[3], float V[3][3],
-                 unsigned int* fp64_lanes) {
-    float off = svd3_dev_core<float, 3, true>(A, U, sig, d, V);
+                 unsigned int* fp64_lanes, const float (*V0)[3] = nullptr) {
+    const float off = V0 ? svd3_dev_core<float, 3, true, true>(A, U, sig, d, V, V0)
+                         : svd3_dev_core<float, 3, true>(A, U, sig, d, V);
     if (!kFp64) {
         if (!(off <= 4e-6f) && fp64_lanes) {  // NaN input stays NaN
 #ifdef __CUDA_ARCH__
@@ -278,6 +300,61 @@ MPM_HD void svd3(const float A[3][3], float U[3][3], float sig[3], float d[3], f
         if (fp64_lanes) *fp64_lanes += 1u;
 #endif
     }
+}
+
+// A rotation matrix as a unit quaternion (x, y, z, w), by Shepperd's method (1978): the square root is taken
+// of the largest of 1 + trace and the 1 + 2 R_ii - trace, so it never cancels.
+MPM_HD void rotation_to_quat(const float R[3][3], float q[4]) {
+    const float tr = R[0][0] + R[1][1] + R[2][2];
+    if (tr > 0.0f) {
+        const float s = 2.0f * sqrtf(1.0f + tr), inv = 1.0f / s;
+        q[3] = 0.25f * s;
+        q[0] = (R[2][1] - R[1][2]) * inv;
+        q[1] = (R[0][2] - R[2][0]) * inv;
+        q[2] = (R[1][0] - R[0][1]) * inv;
+    } else if (R[0][0] > R[1][1] && R[0][0] > R[2][2]) {
+        const float s = 2.0f * sqrtf(1.0f + R[0][0] - R[1][1] - R[2][2]), inv = 1.0f / s;
+        q[3] = (R[2][1] - R[1][2]) * inv;
+        q[0] = 0.25f * s;
+        q[1] = (R[0][1] + R[1][0]) * inv;
+        q[2] = (R[0][2] + R[2][0]) * inv;
+    } else if (R[1][1] > R[2][2]) {
+        const float s = 2.0f * sqrtf(1.0f + R[1][1] - R[0][0] - R[2][2]), inv = 1.0f / s;
+        q[3] = (R[0][2] - R[2][0]) * inv;
+        q[0] = (R[0][1] + R[1][0]) * inv;
+        q[1] = 0.25f * s;
+        q[2] = (R[1][2] + R[2][1]) * inv;
+    } else {
+        const float s = 2.0f * sqrtf(1.0f + R[2][2] - R[0][0] - R[1][1]), inv = 1.0f / s;
+        q[3] = (R[1][0] - R[0][1]) * inv;
+        q[0] = (R[0][2] + R[2][0]) * inv;
+        q[1] = (R[1][2] + R[2][1]) * inv;
+        q[2] = 0.25f * s;
+    }
+}
+
+// The rotation of a quaternion (x, y, z, w), normalised first; the identity for one that is not finite or
+// far from unit length (a particle whose basis was never set, or a blown-up one).
+MPM_HD void quat_to_rotation(const float q[4], float R[3][3]) {
+    const float n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    if (!(n2 > 0.5f && n2 < 2.0f)) {
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) R[i][j] = i == j ? 1.0f : 0.0f;
+        return;
+    }
+    const float k = 2.0f / n2;
+    const float x = q[0], y = q[1], z = q[2], w = q[3];
+    R[0][0] = 1.0f - k * (y * y + z * z);
+    R[0][1] = k * (x * y - z * w);
+    R[0][2] = k * (x * z + y * w);
+    R[1][0] = k * (x * y + z * w);
+    R[1][1] = 1.0f - k * (x * x + z * z);
+    R[1][2] = k * (y * z - x * w);
+    R[2][0] = k * (x * z - y * w);
+    R[2][1] = k * (y * z + x * w);
+    R[2][2] = 1.0f - k * (x * x + y * y);
 }
 
 // ---------------------------------------------------------------------------------------------------------

@@ -261,6 +261,8 @@ __global__ void k_compact(Particles src, Particles dst, const int32_t* __restric
     dst.mat[q] = src.mat[p];
     dst.emitter[q] = src.emitter[p];
     dst.id[q] = new_id[src.id[p]];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) dst.Vq[e][q] = src.Vq[e][p];
 }
 
 

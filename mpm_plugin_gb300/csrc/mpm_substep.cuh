@@ -165,6 +165,7 @@ MPM_HD void tau_from_svd(const Material& m, float jp, const float U[3][3], const
 }
 
 // The stress of particle p from its stored F and Jp, for particles that enter the arena (added or loaded).
+// Also stores the SVD's right basis V, from which the particle's next SVD starts (when the arena has it).
 MPM_HD void particle_stress(const Particles& P, int64_t p, const Material* __restrict__ mats, unsigned int* fp64) {
     const Material m = mats[P.mat[p]];
     float F[3][3], U[3][3], sig[3], d[3], V[3][3], t[6];
@@ -173,6 +174,12 @@ MPM_HD void particle_stress(const Particles& P, int64_t p, const Material* __res
     tau_from_svd(m, P.Jp[p], U, sig, d, t);
 #pragma unroll
     for (int e = 0; e < 6; ++e) P.tau[e][p] = t[e];
+    if (P.Vq[0]) {
+        float q[4];
+        rotation_to_quat(V, q);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) P.Vq[e][p] = q[e];
+    }
 }
 
 // Node index of the stencil nodes base + (i, j, k): the blocked layout's index is a sum of one term per
@@ -572,6 +579,8 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const In& in, const
         for (int e = 0; e < 9; ++e) prefetch_l1(&P.F[e][p]);
         prefetch_l1(&P.Jp[p]);
         prefetch_l1(&P.mat[p]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) prefetch_l1(&P.Vq[e][p]);
     }
     float xo[3];
     int base[3];
@@ -663,7 +672,16 @@ MPM_HD void g2p_particle_from(const Particles& P, int64_t p, const In& in, const
     // P2G would get from decomposing the stored F again.
     const Material m = mats[in.mat()];
     float U[3][3], sig[3], d[3], V[3][3];
-    svd3<kFp64Clamp>(Fn, U, sig, d, V, fp64);  // the FP64 SVD fallback only in the FP64-clamp build
+    {  // the SVD starts from the particle's previous right basis V0, and V is kept for the next substep
+        float q[4], V0[3][3];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) q[e] = P.Vq[e][p];
+        quat_to_rotation(q, V0);
+        svd3<kFp64Clamp>(Fn, U, sig, d, V, fp64, V0);  // the FP64 SVD fallback only in the FP64-clamp build
+        rotation_to_quat(V, q);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) P.Vq[e][p] = q[e];
+    }
     const float jp_old = in.Jp();
     float jp = jp_old;
     bool redo = false;  // FP64 redo of a marginal Drucker-Prager or snow decision (or of every active clamp)

@@ -36,8 +36,8 @@ struct Material {
 };
 
 // Particle state, structure of arrays; every component is its own array of `cap` entries.
-// Words per particle in the arena: x3 v3 C9 F9 Jp tau6 mat emitter id, one plane of `cap` words each.
-constexpr int kParticleFields = 34;
+// Words per particle in the arena: x3 v3 C9 F9 Jp tau6 mat emitter id Vq4, one plane of `cap` words each.
+constexpr int kParticleFields = 38;
 
 struct Particles {
     float* x[3];
@@ -49,6 +49,9 @@ struct Particles {
     int32_t* mat;
     int32_t* emitter;
     int32_t* id;  // insertion rank: the reference's particle order, restored on every download
+    // The right singular vectors of the particle's last SVD as a unit quaternion (x, y, z, w): the next
+    // substep's SVD starts from them (set by G2P and when particles enter; null: every SVD starts cold)
+    float* Vq[4];
     int64_t n, cap;
 };
 
@@ -185,7 +188,7 @@ struct SubstepArgs {
 };
 
 // The field pointers of a particle arena: plane f starts at arena + f * cap (x3 v3 C9 F9 Jp tau6 mat
-// emitter id). Computed, not stored, so kernels that take a scene from a table keep two values live
+// emitter id Vq4). Computed, not stored, so kernels that take a scene from a table keep two values live
 // instead of 34 pointers.
 __host__ __device__ __forceinline__ Particles make_particles(float* arena, int64_t cap, int64_t n) {
     Particles P;
@@ -198,6 +201,7 @@ __host__ __device__ __forceinline__ Particles make_particles(float* arena, int64
     P.mat = reinterpret_cast<int32_t*>(arena + (int64_t)31 * cap);
     P.emitter = reinterpret_cast<int32_t*>(arena + (int64_t)32 * cap);
     P.id = reinterpret_cast<int32_t*>(arena + (int64_t)33 * cap);
+    for (int e = 0; e < 4; ++e) P.Vq[e] = arena + (int64_t)(34 + e) * cap;
     P.n = n;
     P.cap = cap;
     return P;

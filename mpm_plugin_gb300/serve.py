@@ -29,7 +29,7 @@ import numpy as np
 
 from mpm_plugin_gb300.interface import ParticleData, domain_grid_dims
 
-PARTICLE_BYTES = 136  # arena words per particle x 4 B (x v C F Jp stress mat emitter id)
+PARTICLE_BYTES = 152  # arena words per particle x 4 B (x v C F Jp stress mat emitter id, SVD basis)
 
 
 @dataclass

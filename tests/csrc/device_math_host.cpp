@@ -184,6 +184,10 @@ unsigned int emu_substep(void* ev, int64_t n, float* x, float* v, float* C, floa
     P.Jp = Jp;
     for (int k = 0; k < 6; ++k) P.tau[k] = tau + k * n;
     P.mat = mat;
+    // the SVD bases G2P starts from: the identity, or those of the stress computed below
+    std::vector<float> vq(4 * (size_t)n, 0.0f);
+    for (int64_t p = 0; p < n; ++p) vq[3 * (size_t)n + p] = 1.0f;
+    for (int k = 0; k < 4; ++k) P.Vq[k] = vq.data() + k * n;
     P.n = n;
     P.cap = n;
     if (!stress_valid)
