@@ -488,7 +488,7 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-// The tile G2P's tensor maps for one scene: the arena as a 2-D tensor of floats (particle, plane: cap x 34,
+// The tile G2P's tensor maps for one scene: the arena as a 2-D tensor of floats (particle, plane: cap x 38,
 // rows cap * 4 bytes apart), boxes of 256 x 1; the grid as a 4-D tensor (256 floats of a block, then the
 // blocks along k, j, i), boxes of 2 x 2 x 2 blocks. Out-of-range box parts read as zero.
 static bool encode_tile_maps(const SubstepArgs& a, TileMaps* m) {
