@@ -155,6 +155,8 @@ MPM_HD void swap_cols(T M[3][3], int a, int b, bool negate) {
 // V^T by about half of it (sigma ~ 1), below an FP32 ulp of 1, and the QR factor's off-diagonals stay far
 // inside the 4e-6 convergence bound: no further sweep runs for such a lane.
 constexpr float kSweepSkip = 1.0e-8f;
+// ... or below this fraction of E's largest diagonal entry (about three FP32 ulps of it).
+constexpr float kSweepSkipRel = 4.0e-7f;
 // Sweeps after the first two, at most, for a lane whose E is not yet diagonal to kSweepSkip.
 constexpr int kMaxExtraSweeps = 6;
 
@@ -211,9 +213,11 @@ MPM_HD T svd3_dev_core(const T A[3][3], T U[3][3], T sig[3], T d[3], T V[3][3], 
         jacobi_rotate(E, V, 1, 2);
     }
     if constexpr (kAdaptive) {
+        // the bound grows with E where kSweepSkip is below its rounding (a strain of 0.2 keeps off-diagonals of
+        // a few 1e-8 whatever the sweeps do)
+        const T skip = fmax(T(kSweepSkip), T(kSweepSkipRel) * fmax(fmax(fabs(E[0][0]), fabs(E[1][1])), fabs(E[2][2])));
 #pragma unroll 1
-        for (int sw = 0; sw < kMaxExtraSweeps && fmax(fmax(fabs(E[0][1]), fabs(E[0][2])), fabs(E[1][2])) > T(kSweepSkip);
-             ++sw) {
+        for (int sw = 0; sw < kMaxExtraSweeps && fmax(fmax(fabs(E[0][1]), fabs(E[0][2])), fabs(E[1][2])) > skip; ++sw) {
             jacobi_rotate(E, V, 0, 1);
             jacobi_rotate(E, V, 0, 2);
             jacobi_rotate(E, V, 1, 2);
