@@ -32,32 +32,23 @@ BYTES_PER_CELL = 56  # the reference's budget per field cell (field.py:18-20)
 try:  # the reference's records when its package is importable
     from mpm_surface.meshcache import SurfaceMesh
     from mpm_surface.settings import SurfaceSettings
-except ImportError:
+except ImportError:  # data-only stand-ins with the same fields (mpm_surface/meshcache.py, settings.py)
     @dataclass
-    class SurfaceMesh:  # mpm_surface/meshcache.py:28-35
+    class SurfaceMesh:
         verts: np.ndarray
         tris: np.ndarray
         vel: np.ndarray
 
-        @staticmethod
-        def empty() -> "SurfaceMesh":
-            return SurfaceMesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32),
-                               np.zeros((0, 3), np.float32))
-
     @dataclass(frozen=True)
-    class SurfaceSettings:  # mpm_surface/settings.py:21-36
+    class SurfaceSettings:
         enabled: bool = True
         detail: float = 1.0
         smoothing: float = 2.0
         iso: float = 0.35
 
-        def __post_init__(self):
-            if not self.detail > 0:
-                raise ValueError("detail must be > 0")
-            if not self.smoothing > 0:
-                raise ValueError("smoothing must be > 0")
-            if not 0 < self.iso < 1:
-                raise ValueError("iso must be in (0, 1)")
+
+def _empty_mesh() -> "SurfaceMesh":
+    return SurfaceMesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32), np.zeros((0, 3), np.float32))
 
 
 def _kernel(q):
@@ -170,7 +161,7 @@ def surface_particles(positions: np.ndarray, velocities: np.ndarray, spacing: fl
     """max_bytes defaults to 70% of the device's currently free memory (field.py:104-142)."""
     positions = np.asarray(positions, np.float32).reshape(-1, 3)
     if len(positions) == 0:
-        return SurfaceMesh.empty()
+        return _empty_mesh()
     index = _device_index(device)
     surfacer = _surfacer(index)
     # the particles go to the device once; their bounds come back from there (numpy's min and max over
@@ -191,7 +182,7 @@ def surface_particles(positions: np.ndarray, velocities: np.ndarray, spacing: fl
                          f"lower the detail or split the emitter")
     verts, tris, vel = surfacer.build(origin, dims, cell, h, 1.0 / rest_density(spacing, h), settings.iso)
     if len(verts) == 0:
-        return SurfaceMesh.empty()
+        return _empty_mesh()
     world = (origin + verts.astype(np.float64) * cell).astype(np.float32)
     return SurfaceMesh(world, np.ascontiguousarray(tris), vel)
 
