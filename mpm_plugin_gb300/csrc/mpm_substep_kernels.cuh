@@ -412,8 +412,6 @@ __device__ __forceinline__ void p2g_cta(const SubstepArgs& a, int64_t first) {
     p2g_warp_segments<kMaybeFixed, kSweep, kMerge>(a, grid_of(a, cur), cur, t, valid);
 }
 
-// Five CTAs of 256 per SM (48 registers, a few spilled values): the warps it adds hide more of P2G's memory
-// latency than the spills cost (P2G 2-3 % faster than at 64 registers on the mixed and the 256^3 workloads).
 // Chunks of 256 particles of a scene (the work items of the batched particle kernels).
 __device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
     return (unsigned int)((a.n + 255) / 256);
@@ -426,8 +424,11 @@ __device__ __forceinline__ unsigned int particle_chunks(const SubstepArgs& a) {
 // kernels registers (G2P's spills grew from 152 to 252 bytes with it). kMaybeFixed = false: the build for a
 // scene outside deterministic mode (a batch keeps the check per scene); kSweep, kMerge as in
 // p2g_warp_segments.
+// Four CTAs of 256 per SM (64 registers, no spills): with the z-merge's live values, five CTAs at 48
+// registers spilled (488 bytes of loads) and ran P2G at 33.4-34.6 against 31.8 us (same box, alternating;
+// substep 4.35-4.38e9 against 4.50e9). (Five CTAs had won by 2-3 % before the cold paths left the kernel.)
 template <class Scenes, bool kWalk = false, bool kMaybeFixed = true, int kSweep = 2, bool kMerge = false>
-__global__ void __launch_bounds__(256, 5) k_p2g_scatter(Scenes sc) {
+__global__ void __launch_bounds__(256, 4) k_p2g_scatter(Scenes sc) {
     pdl_begin();
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
