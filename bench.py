@@ -904,7 +904,7 @@ def main():
     ap.add_argument("--block-sweep", type=int, default=0)
     ap.add_argument("--p2g-tile", type=int, default=0)
     ap.add_argument("--p2g-group", type=int, default=32)
-    ap.add_argument("--p2g-merge", type=int, default=0)
+    ap.add_argument("--p2g-merge", type=int, default=1)
     ap.add_argument("--fp64-clamp", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:

@@ -166,10 +166,10 @@ enum {
                                   walk the 256-particle chunks grid-stride, so each thread takes about k
                                   particles one after another. (Batches walk their scenes' chunks with at most
                                   8 CTAs per SM whatever this is; the tile builds keep their own grids.) */,
-    MPM_OPT_P2G_MERGE = 15     /* 1: P2G also merges the sums of segment leaders whose stencils share an x-y
-                                  column and differ by one or two nodes in z, so a shared node gets one
-                                  reduction; 0 (default): one reduction per node and leader. Outside
-                                  deterministic mode, one scene (not batches) */
+    MPM_OPT_P2G_MERGE = 15     /* 1 (default): P2G also merges the sums of segment leaders whose stencils share
+                                  an x-y column and differ by one or two nodes in z, so a shared node gets one
+                                  reduction; 0: one reduction per node and leader. Outside deterministic
+                                  mode, one scene (not batches) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

@@ -50,8 +50,8 @@ JOINT_MIN_GAIN = 0.05
 # A single solver also chooses between the one- and two-grid substeps, last: the two-grid mode has to beat
 # the tuned one-grid choice. (Searched first, on the 256^3 pour it beat the untuned defaults, the descent
 # then never reached the reorder that makes one grid faster, and a frame took 1.3x as long: measured.)
-SOLVER_DEFAULTS = {**DEFAULTS, "p2g_merge": 0, "block_sweep": 0, "ppt": 1, "fused_p2g": 0}
-SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2, 3), "p2g_merge": (0, 1), "block_sweep": (0, 1),
+SOLVER_DEFAULTS = {**DEFAULTS, "p2g_merge": 1, "block_sweep": 0, "ppt": 1, "fused_p2g": 0}
+SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2, 3), "p2g_merge": (1, 0), "block_sweep": (0, 1),
                      "ppt": (1, 2, 4), "fused_p2g": (0, 1)}
 SOLVER_ORDER = KNOB_ORDER + ("p2g_merge", "block_sweep", "ppt", "fused_p2g")
 # The tile G2P (g2p_variant 2) stages a chunk's grid boxes in shared memory, which pays when the particles are
@@ -107,7 +107,7 @@ def apply(target, cfg: dict, sms: int, solver: bool = False) -> None:
     if solver:
         target.set_option(_abi.OPT_BLOCK_SWEEP, int(cfg.get("block_sweep", 0)))
         target.set_option(_abi.OPT_PARTICLES_PER_THREAD, int(cfg.get("ppt", 1)))
-        target.set_option(_abi.OPT_P2G_MERGE, int(cfg.get("p2g_merge", 0)))
+        target.set_option(_abi.OPT_P2G_MERGE, int(cfg.get("p2g_merge", 1)))
         target.set_option(_abi.OPT_FUSED_P2G, int(cfg.get("fused_p2g", 0)))
 
 
