@@ -169,7 +169,7 @@ enum {
     MPM_OPT_P2G_MERGE = 15     /* 1 (default): P2G also merges the sums of segment leaders whose stencils share
                                   an x-y column and differ by one or two nodes in z, so a shared node gets one
                                   reduction; 0: one reduction per node and leader. Outside deterministic
-                                  mode, one scene (not batches) */
+                                  mode (a batch with a deterministic scene does not merge) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 
@@ -257,8 +257,8 @@ int mpm_batch_size(void *batch, int32_t *n);
 /* One frame of every scene, in the order they were added: frame_dt[i] for scene i (its advance(frame_dt),
  * mpm_core/solver.py:67-68), stats[i] as mpm_advance returns them. */
 int mpm_batch_advance(void *batch, const double *frame_dt, MpmAdvanceStats *stats);
-/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP, MPM_OPT_PDL, MPM_OPT_P2G_TILE
-   for the batch */
+/* MPM_OPT_SORT_INTERVAL, MPM_OPT_G2P_VARIANT, MPM_OPT_LIST_CTAS, MPM_OPT_P2G_GROUP, MPM_OPT_PDL, MPM_OPT_P2G_TILE,
+   MPM_OPT_P2G_MERGE for the batch */
 int mpm_batch_set_option(void *batch, int32_t option, int64_t value);
 int mpm_batch_get_stream(void *batch, void **stream);
 /* Kernels launched by the batch and its scenes so far. */

@@ -1982,6 +1982,11 @@ int mpm_batch_set_option(void* batch, int32_t option, int64_t value) {
         batch_invalidate(b);
         return MPM_OK;
     }
+    if (option == MPM_OPT_P2G_MERGE) {
+        b->shape.p2g_merge = value != 0;
+        batch_invalidate(b);
+        return MPM_OK;
+    }
     if (option == MPM_OPT_P2G_GROUP) {
         if (value < 1 || value > 32 || (value & (value - 1)))
             return finish_batch(b, {MPM_ERR_VALUE, "P2G group must be a power of two from 1 to 32"});

@@ -22,7 +22,9 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
         if (b.shape.p2g_tile)
             launch_step_kernel_smem(k_p2g_tile<SceneTable>, b.particle_ctas, 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(b.any_fixed ? k_p2g_scatter<SceneTable> : k_p2g_scatter<SceneTable, false, false>,
+            launch_step_kernel(b.any_fixed            ? k_p2g_scatter<SceneTable>
+                               : b.shape.p2g_merge ? k_p2g_scatter<SceneTable, false, false, 2, true>
+                                                   : k_p2g_scatter<SceneTable, false, false>,
                                walk_ctas, 256, st, pdl, sc);
     }
     launch_step_kernel(k_grid_update<SceneTable>, list_ctas, 256, st, pdl, sc);

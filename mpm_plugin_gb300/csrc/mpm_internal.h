@@ -39,7 +39,7 @@ struct LaunchShape {
     int p2g_tile = 0;    // 1: P2G through shared-memory tiles per CTA (k_p2g_tile); 0: warp segments only
     int block_sweep = 0; // 1: P2G flags blocks with plain stores, k_list_blocks lists them (one grid only)
     int ppt = 1;         // particles per thread of the plain P2G and G2P (grid = ceil(chunks / ppt) CTAs)
-    int p2g_merge = 1;   // 1: P2G merges its leaders' sums along z before the reductions (one scene)
+    int p2g_merge = 1;   // 1: P2G merges its leaders' sums along z before the reductions
 };
 
 // Launch of a substep kernel: with shape.pdl the launch carries the programmatic-stream-serialization

@@ -39,10 +39,10 @@ from pathlib import Path
 
 from mpm_plugin_gb300 import _abi
 
-DEFAULTS = {"sort_interval": 0, "g2p_variant": 0, "list_ctas_per_sm": 8, "p2g_group": 32, "pdl": 1}
+DEFAULTS = {"sort_interval": 0, "g2p_variant": 0, "list_ctas_per_sm": 8, "p2g_group": 32, "pdl": 1, "p2g_merge": 1}
 CANDIDATES = {"sort_interval": (0, 2, 4, 8, 16), "g2p_variant": (0, 1), "list_ctas_per_sm": (2, 4, 8, 16),
-              "p2g_group": (1, 4, 8, 32), "pdl": (0, 1)}
-KNOB_ORDER = ("g2p_variant", "sort_interval", "p2g_group", "list_ctas_per_sm", "pdl")
+              "p2g_group": (1, 4, 8, 32), "pdl": (0, 1), "p2g_merge": (1, 0)}
+KNOB_ORDER = ("g2p_variant", "sort_interval", "p2g_group", "list_ctas_per_sm", "pdl", "p2g_merge")
 MIN_GAIN = 0.02
 # A joint override (the tile G2P with a sort interval) has to win by more: on the 256^3 pour a 12-substep
 # window preferred the tile build by 2-3 % and the frame then ran 12 % slower (measured).
@@ -50,10 +50,10 @@ JOINT_MIN_GAIN = 0.05
 # A single solver also chooses between the one- and two-grid substeps, last: the two-grid mode has to beat
 # the tuned one-grid choice. (Searched first, on the 256^3 pour it beat the untuned defaults, the descent
 # then never reached the reorder that makes one grid faster, and a frame took 1.3x as long: measured.)
-SOLVER_DEFAULTS = {**DEFAULTS, "p2g_merge": 1, "block_sweep": 0, "ppt": 1, "fused_p2g": 0}
-SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2, 3), "p2g_merge": (1, 0), "block_sweep": (0, 1),
-                     "ppt": (1, 2, 4), "fused_p2g": (0, 1)}
-SOLVER_ORDER = KNOB_ORDER + ("p2g_merge", "block_sweep", "ppt", "fused_p2g")
+SOLVER_DEFAULTS = {**DEFAULTS, "block_sweep": 0, "ppt": 1, "fused_p2g": 0}
+SOLVER_CANDIDATES = {**CANDIDATES, "g2p_variant": (0, 1, 2, 3), "block_sweep": (0, 1), "ppt": (1, 2, 4),
+                     "fused_p2g": (0, 1)}
+SOLVER_ORDER = KNOB_ORDER + ("block_sweep", "ppt", "fused_p2g")
 # The tile G2P (g2p_variant 2) stages a chunk's grid boxes in shared memory, which pays when the particles are
 # in grid-block order, i.e. with a periodic reorder: the two knobs are also tried together, from the best
 # configuration of the descent (one knob at a time would try the tile G2P only at the sort interval then set).
@@ -104,10 +104,10 @@ def apply(target, cfg: dict, sms: int, solver: bool = False) -> None:
     target.set_option(_abi.OPT_P2G_GROUP, int(cfg.get("p2g_group", 32)))
     target.set_option(_abi.OPT_PDL, int(cfg.get("pdl", 1)))
     target.set_option(_abi.OPT_P2G_TILE, int(cfg.get("p2g_tile", 0)))
+    target.set_option(_abi.OPT_P2G_MERGE, int(cfg.get("p2g_merge", 1)))
     if solver:
         target.set_option(_abi.OPT_BLOCK_SWEEP, int(cfg.get("block_sweep", 0)))
         target.set_option(_abi.OPT_PARTICLES_PER_THREAD, int(cfg.get("ppt", 1)))
-        target.set_option(_abi.OPT_P2G_MERGE, int(cfg.get("p2g_merge", 1)))
         target.set_option(_abi.OPT_FUSED_P2G, int(cfg.get("fused_p2g", 0)))
 
 

@@ -6,10 +6,11 @@ from mpm_plugin_gb300 import tune
 
 
 def test_search_finds_the_separable_optimum_and_keeps_defaults_on_ties():
-    best_cfg = {"sort_interval": 8, "g2p_variant": 1, "list_ctas_per_sm": 4, "p2g_group": 8, "pdl": 1}
+    best_cfg = {"sort_interval": 8, "g2p_variant": 1, "list_ctas_per_sm": 4, "p2g_group": 8, "pdl": 1,
+                "p2g_merge": 0}
     cost = {"sort_interval": {0: 3.0, 2: 1.5, 4: 1.0, 8: 0.5, 16: 0.9},
             "g2p_variant": {0: 1.0, 1: 0.6}, "list_ctas_per_sm": {2: 0.25, 4: 0.2, 8: 0.3, 16: 0.5},
-            "p2g_group": {1: 0.9, 4: 0.5, 8: 0.4, 32: 0.6}, "pdl": {0: 0.3, 1: 0.1}}
+            "p2g_group": {1: 0.9, 4: 0.5, 8: 0.4, 32: 0.6}, "pdl": {0: 0.3, 1: 0.1}, "p2g_merge": {0: 0.1, 1: 0.3}}
     calls = []
 
     def measure(cfg):
