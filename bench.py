@@ -869,6 +869,7 @@ def run_profile_case(args) -> None:
     s.set_option(_abi.OPT_P2G_TILE, args.p2g_tile)
     s.set_option(_abi.OPT_P2G_GROUP, args.p2g_group)
     s.set_option(_abi.OPT_P2G_MERGE, args.p2g_merge)
+    s.set_option(_abi.OPT_DETERMINISTIC, args.deterministic)
     s.set_option(_abi.OPT_FP64_CLAMP, args.fp64_clamp)
     for k in range(args.profile_substeps):
         s.substep(dt, (k + 1) / args.profile_substeps, 1 / 96)
@@ -905,6 +906,7 @@ def main():
     ap.add_argument("--p2g-tile", type=int, default=0)
     ap.add_argument("--p2g-group", type=int, default=32)
     ap.add_argument("--p2g-merge", type=int, default=1)
+    ap.add_argument("--deterministic", type=int, default=0, help="profiling case in deterministic mode")
     ap.add_argument("--fp64-clamp", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:

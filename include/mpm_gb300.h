@@ -168,8 +168,8 @@ enum {
                                   8 CTAs per SM whatever this is; the tile builds keep their own grids.) */,
     MPM_OPT_P2G_MERGE = 15     /* 1 (default): P2G also merges the sums of segment leaders whose stencils share
                                   an x-y column and differ by one or two nodes in z, so a shared node gets one
-                                  reduction; 0: one reduction per node and leader. Outside deterministic
-                                  mode (a batch with a deterministic scene does not merge) */
+                                  reduction; 0: one reduction per node and leader. In deterministic mode the
+                                  merged sums are the same integers, so results stay bit-identical */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

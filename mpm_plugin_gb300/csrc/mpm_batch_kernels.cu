@@ -19,12 +19,13 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
     launch_step_kernel(k_step_begin<SceneTable>, 1, 128, st, pdl, sc);
     launch_step_kernel(k_clear_blocks<SceneTable>, list_ctas, 256, st, pdl, sc);
     if (b.particle_ctas > 0) {  // a deterministic scene takes the warp-segment path inside k_p2g_tile
+        const bool merge = b.shape.p2g_merge != 0;
         if (b.shape.p2g_tile)
             launch_step_kernel_smem(k_p2g_tile<SceneTable>, b.particle_ctas, 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(b.any_fixed            ? k_p2g_scatter<SceneTable>
-                               : b.shape.p2g_merge ? k_p2g_scatter<SceneTable, false, false, 2, true>
-                                                   : k_p2g_scatter<SceneTable, false, false>,
+            launch_step_kernel(b.any_fixed ? (merge ? k_p2g_scatter<SceneTable, false, true, 2, true> : k_p2g_scatter<SceneTable>)
+                                           : (merge ? k_p2g_scatter<SceneTable, false, false, 2, true>
+                                                    : k_p2g_scatter<SceneTable, false, false>),
                                walk_ctas, 256, st, pdl, sc);
     }
     launch_step_kernel(k_grid_update<SceneTable>, list_ctas, 256, st, pdl, sc);

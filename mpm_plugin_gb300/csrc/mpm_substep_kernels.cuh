@@ -163,15 +163,106 @@ __device__ __forceinline__ void clear_block(const SubstepArgs& a, unsigned int p
     if ((threadIdx.x & 63) == 0) a.wl.block_flag[b] = 0u;
 }
 
+// Where a segment's leader adds its sums when the warp's segments are merged along z (p2g_column_sums):
+// src1 / src2 the lanes of the previous two leaders, d1 the z distance to the previous leader when it shares
+// the leader's x and y base (1 or 2, else 0), ok2 whether the one before that sits at z distance 2 (with
+// d1 = 1), ws the z distance to the next leader when it shares x and y (1 or 2, else 0).
+struct ColumnMerge {
+    int src1, src2, d1, ws;
+    bool ok2;
+};
+
+// The merge bookkeeping of one lane (meaningful for leaders; a lane with no earlier or later leader names
+// itself and merges nothing).
+__device__ __forceinline__ ColumnMerge column_merge_of(const P2gTerms& t, bool valid, bool leader, int lane) {
+    const unsigned int leaders = __ballot_sync(0xffffffffu, leader);
+    const unsigned int below = leaders & ((1u << lane) - 1u);
+    const int p1 = below ? 31 - __clz(below) : lane;
+    const unsigned int below2 = below & ((1u << p1) - 1u);
+    const int p2 = below2 ? 31 - __clz(below2) : lane;
+    const unsigned int above = lane == 31 ? 0u : leaders & ~((2u << lane) - 1u);
+    const int s1 = above ? __ffs(above) - 1 : lane;
+    const int xy = valid ? t.base[0] * 65536 + t.base[1] : -1 - lane;  // x, y base (grid dims < 65536)
+    const int z = t.base[2];
+    const int xy1 = __shfl_sync(0xffffffffu, xy, p1), z1 = __shfl_sync(0xffffffffu, z, p1);
+    const int xy2 = __shfl_sync(0xffffffffu, xy, p2), z2 = __shfl_sync(0xffffffffu, z, p2);
+    const int xys = __shfl_sync(0xffffffffu, xy, s1), zs = __shfl_sync(0xffffffffu, z, s1);
+    ColumnMerge m;
+    m.src1 = p1;
+    m.src2 = p2;
+    m.d1 = (p1 != lane && xy1 == xy && (z - z1 == 1 || z - z1 == 2)) ? z - z1 : 0;
+    m.ok2 = m.d1 == 1 && p2 != p1 && xy2 == xy && z - z2 == 2;
+    m.ws = (s1 != lane && xys == xy && (zs - z == 1 || zs - z == 2)) ? zs - z : 0;
+    return m;
+}
+
 // Deterministic-mode P2G of one warp (k_p2g_scatter's arguments): every contribution becomes a 64-bit
 // fixed-point integer (the float times 2^fixed_exp, exact, then rounded to an integer) before it is summed,
 // so the warp sums and the global atomics are exact integer additions and the node totals do not depend on
 // particle order or atomic timing. A non-finite or out-of-range contribution poisons its node instead (the
-// grid update then makes that node NaN, as a float sum would).
+// grid update then makes that node NaN, as a float sum would). kMerge: the leaders' sums merged along z as in
+// p2g_column_sums (integer sums in any grouping are exact, so the totals stay the same bit for bit).
+template <bool kMerge = false>
 __device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTerms& t, bool valid, bool leader,
                                                int tail, int span) {
     const GridDesc& g = a.g;
     const float scale = __int_as_float((127 + a.fixed_exp) << 23);  // 2^fixed_exp
+    if constexpr (kMerge) {
+        const ColumnMerge m = column_merge_of(t, valid, leader, (int)(threadIdx.x & 31u));
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                long long q[3][4];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float val[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (valid) p2g_node(t, i, j, k, val);
+                    bool bad = false;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        const float x = val[c] * scale;
+                        const bool ok = fabsf(x) < 4.0e18f;  // false for NaN and inf too
+                        bad |= !ok;
+                        q[k][c] = ok ? __float2ll_rn(x) : 0ll;
+                    }
+#pragma unroll
+                    for (int d = 1; d < 32; d <<= 1) {
+                        if (d <= span) {  // warp-uniform
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                const long long o = __shfl_down_sync(0xffffffffu, q[k][c], d);
+                                if (d <= tail) q[k][c] += o;
+                            }
+                        }
+                    }
+                    if (valid && bad)
+                        atomicOr(&a.poison[node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k)], 1u);
+                }
+                long long o0[4], o1[4];
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    const long long a1 = __shfl_sync(0xffffffffu, q[1][c], m.src1);
+                    const long long a2 = __shfl_sync(0xffffffffu, q[2][c], m.src1);
+                    const long long b2 = __shfl_sync(0xffffffffu, q[2][c], m.src2);
+                    o0[c] = q[0][c] + (m.d1 == 1 ? a1 : (m.d1 == 2 ? a2 : 0ll)) + (m.ok2 ? b2 : 0ll);
+                    o1[c] = q[1][c] + (m.d1 == 1 ? a2 : 0ll);
+                }
+                if (leader) {
+                    const int64_t n0 = node_index(g, t.base[0] + i, t.base[1] + j, t.base[2]);
+                    unsigned long long* f0 = a.fixed + n0 * 4;
+                    unsigned long long* f1 = a.fixed + node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + 1) * 4;
+                    unsigned long long* f2 = a.fixed + node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + 2) * 4;
+#pragma unroll
+                    for (int c = 0; c < 4; ++c) {
+                        if (o0[c] != 0) atomicAdd(&f0[c], (unsigned long long)o0[c]);
+                        if (m.ws != 1 && o1[c] != 0) atomicAdd(&f1[c], (unsigned long long)o1[c]);
+                        if (m.ws == 0 && q[2][c] != 0) atomicAdd(&f2[c], (unsigned long long)q[2][c]);
+                    }
+                }
+            }
+        return;
+    }
 #pragma unroll
     for (int n = 0; n < 27; ++n) {
         const int i = n / 9, j = (n / 3) % 3, k = n % 3;
@@ -256,14 +347,6 @@ __device__ __forceinline__ void p2g_segment_sums(float4* grid, const P2gTerms& t
             }
 }
 
-// Where a segment's leader adds its sums when the warp's segments are merged along z (p2g_column_sums):
-// src1 / src2 the lanes of the previous two leaders, d1 the z distance to the previous leader when it shares
-// the leader's x and y base (1 or 2, else 0), ok2 whether the one before that sits at z distance 2 (with
-// d1 = 1), ws the z distance to the next leader when it shares x and y (1 or 2, else 0).
-struct ColumnMerge {
-    int src1, src2, d1, ws;
-    bool ok2;
-};
 
 // The segment sums of p2g_segment_sums, then merged along z between the leaders of one x-y column: stencils
 // whose bases differ by one or two nodes in z share nodes, and each shared node is added to the grid once,
@@ -349,7 +432,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
     }
     if constexpr (kMaybeFixed) {
         if (a.fixed) {
-            p2g_fixed_warp(a, t, valid, leader, tail, span);
+            p2g_fixed_warp<kMerge>(a, t, valid, leader, tail, span);
             return;
         }
     }
@@ -357,25 +440,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
     // shuffle rounds needed by the longest segment of the warp: 0, 1, 2, 3 or 5 (4 takes 5)
     const int rounds = span == 0 ? 0 : 32 - __clz(span);
     if constexpr (kMerge) {
-        // the previous two leaders and the next one; a lane with none names itself (and merges nothing)
-        const unsigned int leaders = __ballot_sync(0xffffffffu, leader);
-        const unsigned int below = leaders & ((1u << lane) - 1u);
-        const int p1 = below ? 31 - __clz(below) : lane;
-        const unsigned int below2 = below & ((1u << p1) - 1u);
-        const int p2 = below2 ? 31 - __clz(below2) : lane;
-        const unsigned int above = lane == 31 ? 0u : leaders & ~((2u << lane) - 1u);
-        const int s1 = above ? __ffs(above) - 1 : lane;
-        const int xy = valid ? t.base[0] * 65536 + t.base[1] : -1 - lane;  // x, y base (grid dims < 65536)
-        const int z = t.base[2];
-        const int xy1 = __shfl_sync(0xffffffffu, xy, p1), z1 = __shfl_sync(0xffffffffu, z, p1);
-        const int xy2 = __shfl_sync(0xffffffffu, xy, p2), z2 = __shfl_sync(0xffffffffu, z, p2);
-        const int xys = __shfl_sync(0xffffffffu, xy, s1), zs = __shfl_sync(0xffffffffu, z, s1);
-        ColumnMerge m;
-        m.src1 = p1;
-        m.src2 = p2;
-        m.d1 = (p1 != lane && xy1 == xy && (z - z1 == 1 || z - z1 == 2)) ? z - z1 : 0;
-        m.ok2 = m.d1 == 1 && p2 != p1 && xy2 == xy && z - z2 == 2;
-        m.ws = (s1 != lane && xys == xy && (zs - z == 1 || zs - z == 2)) ? zs - z : 0;
+        const ColumnMerge m = column_merge_of(t, valid, leader, lane);
         if (rounds == 0)
             p2g_column_sums<0>(grid, t, valid, leader, tail, at, m);
         else if (rounds == 1)
