@@ -168,8 +168,8 @@ enum {
                                   8 CTAs per SM whatever this is; the tile builds keep their own grids.) */,
     MPM_OPT_P2G_MERGE = 15     /* 1 (default): P2G also merges the sums of segment leaders whose stencils share
                                   an x-y column and differ by one or two nodes in z, so a shared node gets one
-                                  reduction; 0: one reduction per node and leader. In deterministic mode the
-                                  merged sums are the same integers, so results stay bit-identical */
+                                  reduction; 0: one reduction per node and leader. Not in deterministic
+                                  mode (its fixed-point sums do not merge) */
 };
 int mpm_set_option(void *handle, int32_t option, int64_t value);
 

@@ -23,7 +23,7 @@ void launch_batch_substep(cudaStream_t st, const BatchLaunch& b) {
         if (b.shape.p2g_tile)
             launch_step_kernel_smem(k_p2g_tile<SceneTable>, b.particle_ctas, 256, kP2gTileBytes, st, pdl, sc);
         else
-            launch_step_kernel(b.any_fixed ? (merge ? k_p2g_scatter<SceneTable, false, true, 2, true> : k_p2g_scatter<SceneTable>)
+            launch_step_kernel(b.any_fixed ? k_p2g_scatter<SceneTable>  // (the fixed-point path does not merge)
                                            : (merge ? k_p2g_scatter<SceneTable, false, false, 2, true>
                                                     : k_p2g_scatter<SceneTable, false, false>),
                                walk_ctas, 256, st, pdl, sc);

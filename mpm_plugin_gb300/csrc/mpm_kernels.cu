@@ -525,8 +525,6 @@ static bool g2p_tile_launch(cudaStream_t st, const SubstepArgs& a, bool pdl, con
 // The P2G build for a scene: chunk walk or not, with the fixed-point path (deterministic mode) or not, blocks
 // flagged for the sweep or listed, leader sums merged along z or not.
 static void (*p2g_build(bool walk, bool fixed, bool sweep, bool merge))(OneScene) {
-    if (fixed && merge)
-        return walk ? k_p2g_scatter<OneScene, true, true, 2, true> : k_p2g_scatter<OneScene, false, true, 2, true>;
     if (fixed) return walk ? k_p2g_scatter<OneScene, true, true, 2> : k_p2g_scatter<OneScene, false, true, 2>;
     if (sweep) return walk ? k_p2g_scatter<OneScene, true, false, 1> : k_p2g_scatter<OneScene, false, false, 1>;
     if (merge)

@@ -200,69 +200,13 @@ __device__ __forceinline__ ColumnMerge column_merge_of(const P2gTerms& t, bool v
 // fixed-point integer (the float times 2^fixed_exp, exact, then rounded to an integer) before it is summed,
 // so the warp sums and the global atomics are exact integer additions and the node totals do not depend on
 // particle order or atomic timing. A non-finite or out-of-range contribution poisons its node instead (the
-// grid update then makes that node NaN, as a float sum would). kMerge: the leaders' sums merged along z as in
-// p2g_column_sums (integer sums in any grouping are exact, so the totals stay the same bit for bit).
-template <bool kMerge = false>
+// grid update then makes that node NaN, as a float sum would). (Merging the leaders' sums along z here, as
+// the float path does, kept the totals bit-identical but spilled the 64-bit values: P2G 94.6 against 80.0 us
+// in the deterministic profiling case, measured, so this path does not merge.)
 __device__ __forceinline__ void p2g_fixed_warp(const SubstepArgs& a, const P2gTerms& t, bool valid, bool leader,
                                                int tail, int span) {
     const GridDesc& g = a.g;
     const float scale = __int_as_float((127 + a.fixed_exp) << 23);  // 2^fixed_exp
-    if constexpr (kMerge) {
-        const ColumnMerge m = column_merge_of(t, valid, leader, (int)(threadIdx.x & 31u));
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                long long q[3][4];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    float val[4] = {0.f, 0.f, 0.f, 0.f};
-                    if (valid) p2g_node(t, i, j, k, val);
-                    bool bad = false;
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        const float x = val[c] * scale;
-                        const bool ok = fabsf(x) < 4.0e18f;  // false for NaN and inf too
-                        bad |= !ok;
-                        q[k][c] = ok ? __float2ll_rn(x) : 0ll;
-                    }
-#pragma unroll
-                    for (int d = 1; d < 32; d <<= 1) {
-                        if (d <= span) {  // warp-uniform
-#pragma unroll
-                            for (int c = 0; c < 4; ++c) {
-                                const long long o = __shfl_down_sync(0xffffffffu, q[k][c], d);
-                                if (d <= tail) q[k][c] += o;
-                            }
-                        }
-                    }
-                    if (valid && bad)
-                        atomicOr(&a.poison[node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + k)], 1u);
-                }
-                long long o0[4], o1[4];
-#pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    const long long a1 = __shfl_sync(0xffffffffu, q[1][c], m.src1);
-                    const long long a2 = __shfl_sync(0xffffffffu, q[2][c], m.src1);
-                    const long long b2 = __shfl_sync(0xffffffffu, q[2][c], m.src2);
-                    o0[c] = q[0][c] + (m.d1 == 1 ? a1 : (m.d1 == 2 ? a2 : 0ll)) + (m.ok2 ? b2 : 0ll);
-                    o1[c] = q[1][c] + (m.d1 == 1 ? a2 : 0ll);
-                }
-                if (leader) {
-                    const int64_t n0 = node_index(g, t.base[0] + i, t.base[1] + j, t.base[2]);
-                    unsigned long long* f0 = a.fixed + n0 * 4;
-                    unsigned long long* f1 = a.fixed + node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + 1) * 4;
-                    unsigned long long* f2 = a.fixed + node_index(g, t.base[0] + i, t.base[1] + j, t.base[2] + 2) * 4;
-#pragma unroll
-                    for (int c = 0; c < 4; ++c) {
-                        if (o0[c] != 0) atomicAdd(&f0[c], (unsigned long long)o0[c]);
-                        if (m.ws != 1 && o1[c] != 0) atomicAdd(&f1[c], (unsigned long long)o1[c]);
-                        if (m.ws == 0 && q[2][c] != 0) atomicAdd(&f2[c], (unsigned long long)q[2][c]);
-                    }
-                }
-            }
-        return;
-    }
 #pragma unroll
     for (int n = 0; n < 27; ++n) {
         const int i = n / 9, j = (n / 3) % 3, k = n % 3;
@@ -432,7 +376,7 @@ __device__ __forceinline__ void p2g_warp_segments(const SubstepArgs& a, float4* 
     }
     if constexpr (kMaybeFixed) {
         if (a.fixed) {
-            p2g_fixed_warp<kMerge>(a, t, valid, leader, tail, span);
+            p2g_fixed_warp(a, t, valid, leader, tail, span);
             return;
         }
     }
