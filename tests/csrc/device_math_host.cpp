@@ -15,6 +15,24 @@ using namespace mpm;
 
 extern "C" {
 
+// The G2P path of the SVD: the FP32 sweeps started from the basis of quaternion Q (4 per matrix, x y z w),
+// no FP64 fallback; the new basis back as a quaternion to Qout. Returns how many lanes did not converge.
+int svd_warm_batch(int n, const float* A, const float* Q, float* U, float* s, float* d, float* V, float* Qout) {
+    unsigned int missed = 0;
+    for (int k = 0; k < n; ++k) {
+        float a[3][3], u[3][3], v[3][3], v0[3][3];
+        for (int i = 0; i < 9; ++i) a[i / 3][i % 3] = A[9 * k + i];
+        quat_to_rotation(&Q[4 * k], v0);
+        svd3<false>(a, u, &s[3 * k], &d[3 * k], v, &missed, v0);
+        rotation_to_quat(v, &Qout[4 * k]);
+        for (int i = 0; i < 9; ++i) {
+            U[9 * k + i] = u[i / 3][i % 3];
+            V[9 * k + i] = v[i / 3][i % 3];
+        }
+    }
+    return (int)missed;
+}
+
 // n row-major 3x3 matrices -> U, sigma, d = sigma - 1, V; returns how many lanes took the FP64 path
 int svd_batch(int n, const float* A, float* U, float* s, float* d, float* V) {
     unsigned int fp64 = 0;

@@ -35,6 +35,7 @@ def lib():
     L = C.CDLL(str(OUT))
     P = C.c_void_p
     L.svd_batch.argtypes = [C.c_int, P, P, P, P, P]
+    L.svd_warm_batch.argtypes = [C.c_int, P, P, P, P, P, P, P]
     L.svd_batch.restype = C.c_int
     L.stress_batch.argtypes = [C.c_int, C.c_int, P, C.c_float, C.c_float, P]
     L.mesh_build.argtypes = [C.c_int, P, C.c_int, P]
@@ -71,6 +72,17 @@ def svd(A):
     s, d = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32)
     fp64 = lib().svd_batch(n, _p(A), _p(U), _p(s), _p(d), _p(V))
     return U, s, d, V, fp64
+
+
+def svd_warm(A, Q):
+    """The G2P path of the SVD from the stored bases Q (n, 4; x y z w): U, s, d, V, the new bases, missed."""
+    A = np.ascontiguousarray(np.asarray(A, np.float32).reshape(-1, 3, 3))
+    Q = np.ascontiguousarray(np.asarray(Q, np.float32).reshape(-1, 4))
+    n = len(A)
+    U, V = np.zeros((n, 3, 3), np.float32), np.zeros((n, 3, 3), np.float32)
+    s, d, Qo = np.zeros((n, 3), np.float32), np.zeros((n, 3), np.float32), np.zeros((n, 4), np.float32)
+    missed = lib().svd_warm_batch(n, _p(A), _p(Q), _p(U), _p(s), _p(d), _p(V), _p(Qo))
+    return U, s, d, V, Qo, missed
 
 
 def stress(F, model, mu, lam):

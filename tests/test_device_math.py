@@ -236,3 +236,33 @@ def test_return_mapping_marginal_decisions():
     delta, changed, marginal = project(3, ds, (lo, hi))
     assert not marginal.any()
     assert changed.tolist() == [False, False, False, True]
+
+
+def test_svd_from_the_stored_basis():
+    """The G2P path of the SVD: started from the previous substep's right basis (a unit quaternion), from the
+    identity, or from a garbage quaternion (a cold start), it gives the cold SVD's singular values and a
+    reconstruction of F within the same bounds, and returns its basis as a quaternion that rebuilds V."""
+    from device_math import svd_warm
+
+    F = _rand_F(5000, 1e-2, 7)
+    _, s0, _, _, _ = svd(F)
+    # the previous basis: V of F a step earlier (F perturbed back by a small velocity gradient)
+    rng = np.random.default_rng(8)
+    C = rng.normal(0.0, 1e-3, (len(F), 3, 3)).astype(np.float32)
+    F_prev = np.einsum("nij,njk->nik", np.eye(3, dtype=np.float32) - C, F)
+    Q_prev = svd_warm(F_prev, np.tile([0, 0, 0, 1], (len(F), 1)))[4]
+    F64 = F.astype(np.float64)
+    size = np.maximum(np.abs(F64).max(axis=(1, 2)), 1.0)
+    for Q in (Q_prev, np.tile([0, 0, 0, 1], (len(F), 1)), np.full((len(F), 4), np.nan)):
+        U, s, d, V, Qo, missed = svd_warm(F, Q)
+        rec = np.einsum("nij,nj,nkj->nik", U.astype(np.float64), s.astype(np.float64), V.astype(np.float64))
+        assert (np.abs(rec - F64).max(axis=(1, 2)) / size).max() < 4e-6
+        np.testing.assert_allclose(s, s0, rtol=0, atol=2e-6)
+        assert missed == 0
+        # the returned quaternion rebuilds V (unit length, the same rotation)
+        assert np.abs(np.linalg.norm(Qo, axis=1) - 1.0).max() < 1e-5
+        x, y, z, w = Qo.T.astype(np.float64) / np.linalg.norm(Qo, axis=1)
+        R = np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),
+                      np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], -1),
+                      np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], -1)], 1)
+        assert np.abs(R - V).max() < 2e-6
