@@ -162,3 +162,56 @@ def test_contact_changes_the_result(name):
     e_v, e_x = rel_err(out_c["v"][near], out["v"][near]), rel_err(out_c["x"][inside], out["x"][inside])
     print(name, "collider vs none: v near", f"{e_v:.1e}", "x inside", f"{e_x:.1e}")
     assert e_v > 1e3 * TOL and e_x > 10 * TOL  # contact and projection both acted
+
+
+def test_collider_poses_are_reused_only_while_their_inputs_hold():
+    """Explicit substeps at the same substep fraction with unchanged transforms reuse the poses already on the
+    device (no pose launch); a new fraction, new transforms or a multi-substep call compute them again, and
+    every pose read back equals the one a fresh solver computes for the same inputs, bit for bit."""
+    from scenes import preset
+
+    from mpm_plugin_gb300 import _abi, create
+    from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
+
+    d = domain(res=32)
+
+    def box(x, ang):
+        return translate(x, 0.5, 0.3) @ rot_z(ang) @ scale(0.2, 0.2, 0.1)
+
+    def make(xf0, xf1):
+        s = create(domain=d, materials=[preset("sand_dry")], gravity=(0.0, 0.0, -9.81), device="cuda:0")
+        s.set_option(_abi.OPT_SORT_INTERVAL, 0)
+        add(s, box_particles((0.3, 0.3, 0.4), (0.7, 0.7, 0.5), d.dx))
+        s.set_colliders([ColliderGeometry(MeshData(*unit_cube_mesh(centered=True)), closed=True, friction=0.5)])
+        s.set_collider_transforms(xf0[None], xf1[None])
+        return s
+
+    def fresh_pose(xf0, xf1, sfrac):
+        f = make(xf0, xf1)
+        f.substep(1e-4, sfrac, 1 / 24)
+        return f.read_collider_pose(0)
+
+    def same(a, b):
+        return all(np.array_equal(x, y) for x, y in zip(a, b))
+
+    a0, a1 = box(0.45, 0.0), box(0.55, 20.0)
+    s = make(a0, a1)
+    s.substep(1e-4, 0.5, 1 / 24)  # builds the voxel grid and the graph
+    n0 = s.launch_count()
+    s.substep(1e-4, 0.5, 1 / 24)
+    n_same = s.launch_count() - n0
+    assert same(s.read_collider_pose(0), fresh_pose(a0, a1, 0.5))
+    n0 = s.launch_count()
+    s.substep(1e-4, 0.75, 1 / 24)
+    assert s.launch_count() - n0 == n_same + 1  # the pose launch
+    p75 = s.read_collider_pose(0)
+    assert same(p75, fresh_pose(a0, a1, 0.75)) and not np.array_equal(p75[0], fresh_pose(a0, a1, 0.5)[0])
+    b0, b1 = box(0.5, 10.0), box(0.6, 30.0)
+    s.set_collider_transforms(b0[None], b1[None])
+    n0 = s.launch_count()
+    s.substep(1e-4, 0.75, 1 / 24)
+    assert s.launch_count() - n0 == n_same + 1
+    assert same(s.read_collider_pose(0), fresh_pose(b0, b1, 0.75))
+    s.run_substeps(1e-4, 4, 1 / 24)  # poses of four substeps ending at s = 1
+    s.substep(1e-4, 0.75, 1 / 24)  # recomputed after the multi-substep call
+    assert same(s.read_collider_pose(0), fresh_pose(b0, b1, 0.75))
