@@ -642,6 +642,14 @@ __device__ __forceinline__ unsigned int warp_shape_items() {
     return 128u * sms;
 }
 
+// Rank of this warp among the launch's warps for the one-warp-per-item shape, CTA-major: warp 0 of every
+// CTA first, then warp 1, ... A short list (a few hundred items) then lands one query warp per CTA, spread
+// over all SMs, instead of four to a CTA on the first SMs, where the queries' FP64 evaluations of the winning
+// face shared an SM's FP64 pipe (1/64 of the FP32 rate) and made the slowest SM the kernel's length.
+__device__ __forceinline__ unsigned int contact_warp_rank() {
+    return (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+}
+
 // Mesh-collider contact of one listed node.
 template <bool kWarp>
 __device__ __forceinline__ void grid_collider_node(const SubstepArgs& a, unsigned int i) {
@@ -662,7 +670,7 @@ template <class Scenes>
 __global__ void __launch_bounds__(128) k_grid_colliders(Scenes sc) {
     pdl_begin();
     const unsigned int tid = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
-    const unsigned int warp = tid >> 5, warps = threads >> 5;
+    const unsigned int warp = contact_warp_rank(), warps = threads >> 5;
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[2];
@@ -785,7 +793,7 @@ template <class Scenes>
 __global__ void __launch_bounds__(128) k_project_particles(Scenes sc) {
     pdl_begin();
     const unsigned int tid = blockIdx.x * blockDim.x + threadIdx.x, threads = gridDim.x * blockDim.x;
-    const unsigned int warp = tid >> 5, warps = threads >> 5;
+    const unsigned int warp = contact_warp_rank(), warps = threads >> 5;
     if constexpr (!Scenes::kTable) {
         const SubstepArgs a = sc.get(0);
         const unsigned int n = a.wl.counts[3];
