@@ -843,17 +843,24 @@ def run_gpu(args, world, rank, local):
 
 def run_profile_case(args) -> None:
     """A fixed case for profilers (no timing, no output but one line): `--profile-case mix128` (the headline
-    scene) or `pour256` (the large workload's 7.45M-particle pile and torus, no inflow), with the given launch
-    choices, `--profile-substeps` explicit substeps without graphs, so each kernel is its own launch and a
-    profiler can select launches by kernel name and count."""
+    scene), `mix128_late` (the same scene after five 24 fps frames through the solver API, the snowball and
+    the column pressing on the collider; only its profiled substeps run between cudaProfilerStart and
+    cudaProfilerStop, for `ncu --profile-from-start off`) or `pour256` (the large workload's 7.45M-particle
+    pile and torus, no inflow), with the given launch choices, `--profile-substeps` explicit substeps without
+    graphs, so each kernel is its own launch and a profiler can select launches by kernel name and count."""
+    import torch
     from mpm_plugin_gb300 import _abi
     from mpm_plugin_gb300.interface import ColliderGeometry, MeshData
     from mpm_plugin_gb300.solver import Gb300Solver
 
     device = "cuda:0"
-    if args.profile_case == "mix128":
-        s, _ = make_gpu_solver(device)
+    if args.profile_case in ("mix128", "mix128_late"):
+        s, xf = make_gpu_solver(device)
         dt = DT
+        if args.profile_case == "mix128_late":
+            for _ in range(5):
+                s.set_collider_transforms(xf[None], xf[None])
+                s.advance(FRAME_DT)
     else:
         d, mats, pile, (tv, tt), pose, _ = large_scene(256, 0.155)
         s = Gb300Solver(d, mats, (0.0, 0.0, -9.81), 8, device=device)
@@ -871,9 +878,15 @@ def run_profile_case(args) -> None:
     s.set_option(_abi.OPT_P2G_MERGE, args.p2g_merge)
     s.set_option(_abi.OPT_DETERMINISTIC, args.deterministic)
     s.set_option(_abi.OPT_FP64_CLAMP, args.fp64_clamp)
+    late = args.profile_case == "mix128_late"
+    if late:
+        s.synchronize()
+        torch.cuda.profiler.start()
     for k in range(args.profile_substeps):
         s.substep(dt, (k + 1) / args.profile_substeps, 1 / 96)
     s.synchronize()
+    if late:
+        torch.cuda.profiler.stop()
     print(f"profile case {args.profile_case}: {s.particle_count} particles, {args.profile_substeps} substeps")
     s.close()
 
@@ -897,7 +910,7 @@ def main():
     ap.add_argument("--batched-frames", type=int, default=3,
                     help="frames of the 64-scene batched workload, plain and batched (0: skip)")
     ap.add_argument("--surface", type=int, default=1, help="measure the surfacer (0: skip)")
-    ap.add_argument("--profile-case", choices=["mix128", "pour256"], default=None,
+    ap.add_argument("--profile-case", choices=["mix128", "mix128_late", "pour256"], default=None,
                     help="run a fixed case for a profiler instead of the benchmark (see run_profile_case)")
     ap.add_argument("--profile-substeps", type=int, default=30)
     ap.add_argument("--g2p-variant", type=int, default=0)
