@@ -263,6 +263,23 @@ void emu_collider_sdf(void* ev, int c, float s, int use_sdf, int n, const float*
     }
 }
 
+// Narrow-band voxel grid of collider c as built: desc = lo (3), voxel edge, contact cutoff, dims (3); cells
+// (n, 2) = first candidate, count (or kSdfFar / kSdfUseBvh) when cap >= n. Returns the voxel count n.
+int64_t emu_sdf_cells(void* ev, int c, float* desc, int32_t* cells, int64_t cap) {
+    Emu* e = static_cast<Emu*>(ev);
+    const SdfGridDev& g = e->cols[c].sdf;
+    for (int a = 0; a < 3; ++a) { desc[a] = g.lo[a]; desc[5 + a] = (float)g.dims[a]; }
+    desc[3] = g.h;
+    desc[4] = g.cutoff;
+    const int64_t n = (int64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    if (cells && cap >= n && g.built)
+        for (int64_t v = 0; v < n; ++v) {
+            cells[2 * v] = e->cells[g.cell_offset + v].x;
+            cells[2 * v + 1] = e->cells[g.cell_offset + v].y;
+        }
+    return n;
+}
+
 // The C++ host decomposition of a world matrix (mpm_host.h decompose): t (3), q (4, x y z w), S (9)
 void host_decompose(const float* m16, double* t, double* q, double* S) {
     double min_sv;

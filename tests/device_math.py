@@ -54,6 +54,8 @@ def lib():
     L.emu_use_sdf.argtypes = [P, C.c_int]
     L.emu_particle_stress.argtypes = [P, C.c_int64, P, P, P, P]
     L.emu_collider_sdf.argtypes = [P, C.c_int, C.c_float, C.c_int, C.c_int, P, P]
+    L.emu_sdf_cells.argtypes = [P, C.c_int, P, P, C.c_int64]
+    L.emu_sdf_cells.restype = C.c_int64
     L.host_decompose.argtypes = [P, P, P, P]
     L.host_collider_matrix.argtypes = [P, P, C.c_double, C.c_float, P]
     L.host_project.argtypes = [C.c_int, C.c_int, P, P, P, P, P, P]
@@ -224,6 +226,15 @@ class SubstepEmulator:
         out = np.zeros((len(pts), 4), np.float32)
         lib().emu_collider_sdf(self.h, c, s, int(use_sdf), len(pts), _p(pts), _p(out))
         return out
+
+    def sdf_cells(self, c=0):
+        """Collider c's narrow-band voxel grid as built: (lo, voxel edge, contact cutoff, dims, cells (n, 2) of
+        (first candidate, count or -1 far / -2 BVH walk)), all in the collider's local units."""
+        desc = np.zeros(8, np.float32)
+        n = lib().emu_sdf_cells(self.h, c, _p(desc), None, 0)
+        cells = np.zeros((n, 2), np.int32)
+        lib().emu_sdf_cells(self.h, c, _p(desc), _p(cells), n)
+        return desc[:3], float(desc[3]), float(desc[4]), desc[5:8].astype(int), cells
 
     def read_grid(self):
         dims = np.zeros(3, np.int32)

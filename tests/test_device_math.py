@@ -137,6 +137,36 @@ def test_narrow_band_grid_matches_full_query(mesh, closed):
         assert (~far).sum() > 100
 
 
+def test_narrow_band_voxels_list_the_contact_band():
+    """The mixed workload's collider (5,120-triangle perturbed sphere, radius 0.12 at 128^3): voxels half the
+    contact cutoff wide, at most about 193 per axis, and every voxel within three grid cells of the surface,
+    inside or out, answers from a candidate list of at most 128 triangles or as FAR: none falls back to the
+    BVH walk, whose one-lane chain was the slowest contact query."""
+    from device_math import SubstepEmulator
+
+    from mpm_plugin_gb300.workloads import mixed_scene
+
+    d, mats, _, (cv, ct, xf) = mixed_scene(128, sample=lambda v, t, spacing, seed: np.zeros((1, 3), np.float32))
+    e = SubstepEmulator(d, mats)
+    e.set_colliders([(cv, ct, True, 0.5)])
+    xf = np.asarray(xf, np.float32)
+    e.set_collider_transforms(xf[None], xf[None])
+    lo, h, cutoff, dims, cells = e.sdf_cells(0)
+    assert h == pytest.approx(0.5 * cutoff, rel=1e-6) and dims.max() <= 194
+    cell = (1.0 / 128) / 0.12  # one grid cell in the collider's local units
+    assert cutoff == pytest.approx(1.25 * cell, rel=1e-4)
+    i, j, k = np.meshgrid(*(np.arange(n) for n in dims), indexing="ij")
+    centre = np.stack([lo[0] + (i + 0.5) * h, lo[1] + (j + 0.5) * h, lo[2] + (k + 0.5) * h], -1).reshape(-1, 3)
+    # the perturbed surface lies within 0.97-1.03 of the centre (vertex jitter 0.03)
+    r = np.linalg.norm(centre, axis=1)
+    band = (r > 1.03 - 3 * cell) & (r < 0.97 + 3 * cell)
+    count = cells[band, 1]
+    assert band.sum() > 10000
+    assert (count != -2).all() and count.max() <= 128
+    listed = count[count > 0]
+    assert len(listed) > 0.5 * band.sum() and np.median(listed) < 40
+
+
 def _closest_point_independent(p, a, b, c):
     """Closest point on a triangle without region tests: the plane projection if it falls inside, else the
     nearest of the closest points on the three edges."""
